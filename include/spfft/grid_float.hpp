@@ -1,0 +1,47 @@
+/* C++ single-precision Grid handle (reference include/spfft/grid_float.hpp:49-203, local constructor only). A Grid owns
+ * the device scratch, the internal space-domain buffer and its pinned host mirror. Copies share the
+ * memory; transforms created from a grid keep it alive. */
+#ifndef SPFFT_GRID_FLOAT_HPP
+#define SPFFT_GRID_FLOAT_HPP
+
+#include <memory>
+#include "spfft/config.h"
+#include "spfft/transform_float.hpp"
+#include "spfft/types.h"
+
+namespace spfft {
+
+template <typename T>
+class GridInternal;
+
+class SPFFT_EXPORT GridFloat {
+public:
+  GridFloat(int maxDimX, int maxDimY, int maxDimZ, int maxNumLocalZColumns,
+       SpfftProcessingUnitType processingUnit, int maxNumThreads);
+
+  /* Copying a Grid allocates new memory of the same size (reference grid.cpp copy semantics). */
+  GridFloat(const GridFloat&);
+  GridFloat(GridFloat&&) = default;
+  GridFloat& operator=(const GridFloat&);
+  GridFloat& operator=(GridFloat&&) = default;
+
+  TransformFloat create_transform(SpfftProcessingUnitType processingUnit,
+                             SpfftTransformType transformType, int dimX, int dimY, int dimZ,
+                             int localZLength, int numLocalElements,
+                             SpfftIndexFormatType indexFormat, const int* indices) const;
+
+  int max_dim_x() const;
+  int max_dim_y() const;
+  int max_dim_z() const;
+  int max_num_local_z_columns() const;
+  int max_local_z_length() const;
+  SpfftProcessingUnitType processing_unit() const;
+  int device_id() const;
+  int num_threads() const;
+
+private:
+  std::shared_ptr<GridInternal<float>> grid_;
+};
+
+}  // namespace spfft
+#endif

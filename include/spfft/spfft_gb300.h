@@ -1,0 +1,57 @@
+/* Extensions of this GB300 library beyond the reference's C interface. None of these functions has
+ * a counterpart in the reference; each says what it adds. All return SpfftError. */
+#ifndef SPFFT_GB300_H
+#define SPFFT_GB300_H
+
+#include "spfft/config.h"
+#include "spfft/errors.h"
+#include "spfft/transform.h"
+#include "spfft/transform_float.h"
+#include "spfft/types.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Host-only index planning: the z-stick layout a transform of these parameters uses. Runs without
+ * a GPU. valueIndices receives numLocalElements ints (stick * dimZ + z per value, in input order),
+ * stickKeys receives up to maxSticks ints (sorted x * dimY + y storage keys); numSticks and
+ * zeroZeroStick (position of key 0, or numSticks if absent) may be NULL. Errors are those of
+ * transform creation (invalid indices, invalid parameters). */
+SPFFT_EXPORT SpfftError spfft_gb300_plan_indices(SpfftTransformType transformType, int dimX,
+                                                 int dimY, int dimZ, int numLocalElements,
+                                                 const int* indices, int* valueIndices,
+                                                 int* stickKeys, int maxSticks, int* numSticks,
+                                                 int* zeroZeroStick);
+
+/* Attach a CUDA stream (a cudaStream_t passed as void*). Afterwards every call of the transform is
+ * enqueued on that stream only: no internal stream and no ordering against the legacy default
+ * stream. In SPFFT_EXEC_ASYNCHRONOUS mode calls then return without waiting, which makes them
+ * usable inside CUDA graph capture. NULL restores the default protocol. */
+SPFFT_EXPORT SpfftError spfft_gb300_transform_set_stream(SpfftTransform transform, void* stream);
+SPFFT_EXPORT SpfftError spfft_gb300_float_transform_set_stream(SpfftFloatTransform transform,
+                                                               void* stream);
+
+/* Kernel-only execution on device pointers and a given stream: no pointer inspection, no copies,
+ * no synchronisation, no preceding-error check. values: interleaved complex frequency values;
+ * space: the space domain in the layout of the transform. */
+SPFFT_EXPORT SpfftError spfft_gb300_transform_backward_device(SpfftTransform transform,
+                                                              const double* values, double* space,
+                                                              void* stream);
+SPFFT_EXPORT SpfftError spfft_gb300_transform_forward_device(SpfftTransform transform,
+                                                             const double* space, double* values,
+                                                             SpfftScalingType scaling,
+                                                             void* stream);
+SPFFT_EXPORT SpfftError spfft_gb300_float_transform_backward_device(SpfftFloatTransform transform,
+                                                                    const float* values,
+                                                                    float* space, void* stream);
+SPFFT_EXPORT SpfftError spfft_gb300_float_transform_forward_device(SpfftFloatTransform transform,
+                                                                   const float* space,
+                                                                   float* values,
+                                                                   SpfftScalingType scaling,
+                                                                   void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

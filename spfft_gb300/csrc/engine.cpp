@@ -1,0 +1,177 @@
+// GpuPlan: uploads the planner's tables and the twiddles once, picks tile shapes, and issues the
+// kernel sequence of each transform.
+#include "engine.hpp"
+
+#include <algorithm>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include "fft_plan.hpp"
+
+namespace spfft {
+namespace gb300 {
+
+namespace {
+
+constexpr size_t kAlign = 256;
+inline size_t align_up(size_t v) { return (v + kAlign - 1) / kAlign * kAlign; }
+
+// Shared memory budget per block of the generic kernels: two blocks per SM.
+constexpr size_t kSmemBudget = 100 * 1024;
+
+int max_smem_optin(int device) {
+  int v = 0;
+  check_cuda(cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, device));
+  return v;
+}
+
+template <typename T>
+void prepare_once(int device) {
+  static std::mutex mutex;
+  static std::vector<int> done;
+  std::lock_guard<std::mutex> lock(mutex);
+  if (std::find(done.begin(), done.end(), device) != done.end()) return;
+  check_cuda(prepare_kernels<T>(static_cast<size_t>(max_smem_optin(device))));
+  done.push_back(device);
+}
+
+inline int odd_pitch(int n) { return n % 2 == 0 ? n + 1 : n; }
+
+template <typename T>
+LaunchConfig choose_launch_config(const IndexPlan& p, int device) {
+  const size_t c = 2 * sizeof(T);
+  const size_t optin = static_cast<size_t>(max_smem_optin(device));
+  LaunchConfig cfg{};
+  cfg.threads = 256;
+
+  const int nz = p.dimZ, ny = p.dimY, nx = p.dimX;
+  cfg.zPitch = odd_pitch(nz);
+  cfg.xPitch = odd_pitch(nx);
+  // Every pass needs at least one sequence plus its ping-pong copy and the twiddles on chip.
+  const size_t minZ = (nz + 2 * static_cast<size_t>(cfg.zPitch)) * c;
+  const size_t minY = (ny + 2 * static_cast<size_t>(ny)) * c;
+  const size_t minX = (nx + 2 * static_cast<size_t>(cfg.xPitch)) * c;
+  if (minZ > optin || minY > optin || minX > optin) throw InvalidParameterError();
+
+  auto fit = [&](size_t fixed, size_t per, int cap) {
+    const size_t budget = std::max(kSmemBudget, fixed + per);
+    int k = static_cast<int>((budget - fixed) / per);
+    return std::max(1, std::min(k, cap));
+  };
+  cfg.sticksPerBlock = fit(nz * c, 2 * cfg.zPitch * c, 32);
+  cfg.sticksPerBlock = std::min(cfg.sticksPerBlock, std::max(1, p.num_sticks()));
+  cfg.columnsPerBlock = fit(ny * c, 2 * static_cast<size_t>(ny) * c, 32);
+  cfg.columnsPerBlock = std::min(cfg.columnsPerBlock, std::max(1, p.num_columns()));
+  cfg.rowsPerBlock = fit(nx * c, 2 * cfg.xPitch * c, 16);
+  cfg.rowsPerBlock = std::min(cfg.rowsPerBlock, ny);
+
+  cfg.smemZ = (nz + 2 * static_cast<size_t>(cfg.sticksPerBlock) * cfg.zPitch) * c;
+  cfg.smemY = (ny + 2 * static_cast<size_t>(cfg.columnsPerBlock) * ny) * c;
+  cfg.smemX = (nx + 2 * static_cast<size_t>(cfg.rowsPerBlock) * cfg.xPitch) * c;
+  return cfg;
+}
+
+}  // namespace
+
+template <typename T>
+GpuPlan<T>::GpuPlan(const IndexPlan& p, int device) {
+  prepare_once<T>(device);
+  config_ = choose_launch_config<T>(p, device);
+
+  const int ns = p.num_sticks(), ncol = p.num_columns(), nv = p.numValues;
+  const size_t c = 2 * sizeof(T);
+
+  // Scratch: sticks, then compact planes, then the value staging area.
+  layout_.sticksOffset = 0;
+  layout_.planesOffset = align_up(static_cast<size_t>(ns) * p.dimZ * c);
+  layout_.valuesOffset =
+      layout_.planesOffset + align_up(static_cast<size_t>(p.dimZ) * p.dimY * ncol * c);
+  layout_.total = layout_.valuesOffset + align_up(static_cast<size_t>(nv) * c);
+
+  // One allocation for every table: twiddles (T) then int arrays.
+  const std::vector<double> twz = make_twiddles(p.dimZ), twy = make_twiddles(p.dimY),
+                            twx = make_twiddles(p.dimX);
+  struct Part {
+    const void* src;
+    size_t bytes;
+    size_t offset;
+  };
+  std::vector<T> tz(twz.begin(), twz.end()), ty(twy.begin(), twy.end()), tx(twx.begin(), twx.end());
+  std::vector<Part> parts = {
+      {tz.data(), tz.size() * sizeof(T), 0},
+      {ty.data(), ty.size() * sizeof(T), 0},
+      {tx.data(), tx.size() * sizeof(T), 0},
+      {p.stickColumn.data(), p.stickColumn.size() * sizeof(int), 0},
+      {p.stickY.data(), p.stickY.size() * sizeof(int), 0},
+      {p.columnX.data(), p.columnX.size() * sizeof(int), 0},
+      {p.columnStickStart.data(), p.columnStickStart.size() * sizeof(int), 0},
+      {p.entryPos.data(), p.entryPos.size() * sizeof(int), 0},
+      {p.entryUser.data(), p.entryUser.size() * sizeof(int), 0},
+      {p.stickEntryStart.data(), p.stickEntryStart.size() * sizeof(int), 0},
+  };
+  size_t total = 0;
+  for (auto& part : parts) {
+    part.offset = total;
+    total += align_up(std::max<size_t>(part.bytes, 1));
+  }
+  std::vector<char> host(total, 0);
+  for (auto& part : parts) {
+    if (part.bytes) std::memcpy(host.data() + part.offset, part.src, part.bytes);
+  }
+  tables_ = DeviceBuffer(total);
+  check_cuda(cudaMemcpy(tables_.get(), host.data(), total, cudaMemcpyHostToDevice));
+  char* d = static_cast<char*>(tables_.get());
+
+  base_.dimX = p.dimX;
+  base_.dimY = p.dimY;
+  base_.dimZ = p.dimZ;
+  base_.dimXFreq = p.dimXFreq;
+  base_.numSticks = ns;
+  base_.numColumns = ncol;
+  base_.r2c = p.type == SPFFT_TRANS_R2C ? 1 : 0;
+  base_.zeroZeroStick = (base_.r2c && p.zeroZeroStick < ns) ? p.zeroZeroStick : -1;
+  base_.fz = make_radix_plan(p.dimZ);
+  base_.fy = make_radix_plan(p.dimY);
+  base_.fx = make_radix_plan(p.dimX);
+  base_.twz = reinterpret_cast<const T*>(d + parts[0].offset);
+  base_.twy = reinterpret_cast<const T*>(d + parts[1].offset);
+  base_.twx = reinterpret_cast<const T*>(d + parts[2].offset);
+  base_.stickColumn = reinterpret_cast<const int*>(d + parts[3].offset);
+  base_.stickY = reinterpret_cast<const int*>(d + parts[4].offset);
+  base_.columnX = reinterpret_cast<const int*>(d + parts[5].offset);
+  base_.columnStickStart = reinterpret_cast<const int*>(d + parts[6].offset);
+  base_.entryPos = reinterpret_cast<const int*>(d + parts[7].offset);
+  base_.entryUser = reinterpret_cast<const int*>(d + parts[8].offset);
+  base_.stickEntryStart = reinterpret_cast<const int*>(d + parts[9].offset);
+
+  // Forward scaling factor T(1 / (Nx Ny Nz)) computed in double (execution_gpu.cpp:58-59).
+  scale_ = static_cast<T>(1.0 / (static_cast<double>(p.dimX) * p.dimY * p.dimZ));
+}
+
+template <typename T>
+PlanView<T> GpuPlan<T>::view(void* scratch) const {
+  PlanView<T> v = base_;
+  char* s = static_cast<char*>(scratch);
+  v.sticks = reinterpret_cast<T*>(s + layout_.sticksOffset);
+  v.planes = reinterpret_cast<T*>(s + layout_.planesOffset);
+  return v;
+}
+
+template <typename T>
+void GpuPlan<T>::backward(const T* values, T* space, void* scratch, cudaStream_t stream) const {
+  check_launch(launch_backward<T>(view(scratch), config_, values, space, stream));
+}
+
+template <typename T>
+void GpuPlan<T>::forward(const T* space, T* values, bool scaled, void* scratch,
+                         cudaStream_t stream) const {
+  check_launch(launch_forward<T>(view(scratch), config_, space, values, scaled ? scale_ : T(0),
+                                 stream));
+}
+
+template class GpuPlan<double>;
+template class GpuPlan<float>;
+
+}  // namespace gb300
+}  // namespace spfft

@@ -1,0 +1,54 @@
+// Device-resident plan of one transform: index tables, twiddles and tile shapes, plus the launch
+// sequence of a backward or forward transform on a stream. Replaces the reference's GPU execution
+// engine (src/execution/execution_gpu.cpp:47-115 construction, :253-410 execution) with this
+// library's fused kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <memory>
+
+#include "kernels.hpp"
+#include "planner.hpp"
+#include "runtime.hpp"
+
+namespace spfft {
+namespace gb300 {
+
+// Bytes of scratch one transform needs, and where each part starts inside it.
+struct ScratchLayout {
+  size_t sticksOffset = 0, planesOffset = 0, valuesOffset = 0, total = 0;
+};
+
+template <typename T>
+class GpuPlan {
+public:
+  GpuPlan(const IndexPlan& plan, int device);
+
+  const ScratchLayout& scratch_layout() const { return layout_; }
+  const LaunchConfig& launch_config() const { return config_; }
+
+  // values/space are device pointers; scratch points to scratch_layout().total bytes.
+  void backward(const T* values, T* space, void* scratch, cudaStream_t stream) const;
+  void forward(const T* space, T* values, bool scaled, void* scratch, cudaStream_t stream) const;
+
+  // Device pointer of the value staging area inside `scratch` (host input / output path).
+  T* staging(void* scratch) const {
+    return reinterpret_cast<T*>(static_cast<char*>(scratch) + layout_.valuesOffset);
+  }
+
+private:
+  PlanView<T> view(void* scratch) const;
+
+  PlanView<T> base_{};
+  LaunchConfig config_{};
+  ScratchLayout layout_{};
+  T scale_ = T(1);
+  DeviceBuffer tables_;
+};
+
+extern template class GpuPlan<double>;
+extern template class GpuPlan<float>;
+
+}  // namespace gb300
+}  // namespace spfft

@@ -1,0 +1,64 @@
+// Device-side view of a transform plan and the launch entry points of the transform kernels.
+// Shared between the host engine (engine.cpp) and the kernels (kernels_generic.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "fft_plan.hpp"
+
+namespace spfft {
+namespace gb300 {
+
+// Everything a kernel needs to know about one transform. Device pointers only.
+//
+// HBM layouts:
+//   sticks  [dimZ][numSticks]          complex  z-major: row z holds every stick's value at z
+//   planes  [dimZ][dimY][numColumns]   complex  y-transformed compact columns (x = columnX[c])
+//   space   [dimZ][dimY][dimX]         complex (C2C) or real (R2C), the user's layout
+//   values  [numValues]                interleaved complex, user order
+template <typename T>
+struct PlanView {
+  int dimX, dimY, dimZ, dimXFreq;
+  int numSticks, numColumns;
+  int zeroZeroStick;  // -1 when absent or C2C
+  int r2c;
+  RadixPlan fz, fy, fx;
+  const T* twz;  // interleaved (cos, -sin) tables of length dimZ / dimY / dimX
+  const T* twy;
+  const T* twx;
+  const int* stickColumn;
+  const int* stickY;
+  const int* columnX;
+  const int* columnStickStart;
+  const int* entryPos;
+  const int* entryUser;
+  const int* stickEntryStart;
+  T* sticks;
+  T* planes;
+};
+
+// Tile shapes of the generic kernels, chosen by the host (engine.cpp: choose_launch_config).
+struct LaunchConfig {
+  int threads;            // threads per block (all kernels)
+  int sticksPerBlock;     // z kernels
+  int zPitch;             // padded stick length in shared memory
+  int columnsPerBlock;    // y kernels
+  int rowsPerBlock;       // x kernels
+  int xPitch;             // padded row length in shared memory
+  size_t smemZ, smemY, smemX;
+};
+
+// Backward (frequency -> space). `values` is the interleaved input, `space` the output buffer.
+template <typename T>
+cudaError_t launch_backward(const PlanView<T>& p, const LaunchConfig& c, const T* values, T* space,
+                            cudaStream_t stream);
+// Forward (space -> frequency). scale == 0 means no scaling.
+template <typename T>
+cudaError_t launch_forward(const PlanView<T>& p, const LaunchConfig& c, const T* space, T* values,
+                           T scale, cudaStream_t stream);
+// One-time per-process attribute setup (dynamic shared memory limits).
+template <typename T>
+cudaError_t prepare_kernels(size_t maxSmem);
+
+}  // namespace gb300
+}  // namespace spfft

@@ -1,0 +1,80 @@
+"""CPU tests of the library's host planner against the reference's own planner output (golden
+fixtures) -- bit-exact -- and of the C interface's error codes on paths that need no GPU."""
+import ctypes
+
+import numpy as np
+import pytest
+
+import spfft_gb300 as sp
+from util import load_npz_group, random_indices
+
+
+def test_planner_matches_reference_test_cases(lib):
+    for key, c in load_npz_group("ref_cases.npz").items():
+        t = sp.SPFFT_TRANS_R2C if key.startswith("r2c") else sp.SPFFT_TRANS_C2C
+        _, _, dx, dy, dz = key.split("_")
+        vi, sk, zz = sp.plan_indices(t, int(dx), int(dy), int(dz), c["indices"])
+        np.testing.assert_array_equal(vi, c["value_indices"], err_msg=key)
+        np.testing.assert_array_equal(sk, c["stick_keys"], err_msg=key)
+        assert zz == int(c["zz"][0]), key
+
+
+def test_planner_edge_cases_and_error_codes(lib):
+    for name, c in load_npz_group("ref_edges.npz").items():
+        t, dx, dy, dz = map(int, c["args"])
+        if "error" in c:
+            with pytest.raises(sp.SpfftError) as e:
+                sp.plan_indices(t, dx, dy, dz, c["indices"])
+            assert e.value.error_code() == int(c["error"][0]), name
+        else:
+            vi, sk, zz = sp.plan_indices(t, dx, dy, dz, c["indices"])
+            np.testing.assert_array_equal(vi, c["value_indices"], err_msg=name)
+            np.testing.assert_array_equal(sk, c["stick_keys"], err_msg=name)
+            assert zz == int(c["zz"][0]), name
+
+
+def test_planner_matches_oracle_on_large_sets(lib):
+    from oracle import indices as ix
+
+    rng = np.random.default_rng(11)
+    for t, dims in [(0, (64, 64, 64)), (1, (96, 90, 80)), (0, (100, 2, 13)), (1, (1, 100, 11))]:
+        idx = random_indices(rng, *dims, r2c=(t == 1), centered=(dims[0] % 2 == 0))
+        vi, sk, zz = sp.plan_indices(t, *dims, idx)
+        p = ix.convert(t, *dims, idx)
+        np.testing.assert_array_equal(vi, p["value_indices"])
+        np.testing.assert_array_equal(sk, p["stick_keys"])
+        assert zz == p["zero_zero_stick"]
+
+
+def test_shuffled_value_order_keeps_mapping(lib):
+    rng = np.random.default_rng(5)
+    idx = random_indices(rng, 12, 11, 13, r2c=False)
+    perm = rng.permutation(idx.shape[0])
+    vi, sk, _ = sp.plan_indices(0, 12, 11, 13, idx)
+    vi2, sk2, _ = sp.plan_indices(0, 12, 11, 13, idx[perm])
+    np.testing.assert_array_equal(sk, sk2)
+    np.testing.assert_array_equal(vi[perm], vi2)
+
+
+def test_null_handles_and_bad_arguments(lib):
+    E = sp.ErrorCode
+    v = ctypes.c_int(0)
+    assert lib.spfft_transform_dim_x(None, ctypes.byref(v)) == E.SPFFT_INVALID_HANDLE_ERROR
+    assert lib.spfft_transform_destroy(None) == E.SPFFT_INVALID_HANDLE_ERROR
+    assert lib.spfft_grid_destroy(None) == E.SPFFT_INVALID_HANDLE_ERROR
+    assert lib.spfft_float_grid_max_dim_x(None, ctypes.byref(v)) == E.SPFFT_INVALID_HANDLE_ERROR
+    assert lib.spfft_transform_backward(None, None, 2) == E.SPFFT_INVALID_HANDLE_ERROR
+    h = ctypes.c_void_p()
+    # negative sizes are rejected before any device work (transform.cpp:74-77)
+    assert lib.spfft_transform_create_independent(ctypes.byref(h), 1, 2, 0, -1, 4, 4, 0, 0, None) == \
+        E.SPFFT_INVALID_PARAMETER_ERROR
+    # indices missing while elements are announced
+    assert lib.spfft_transform_create_independent(ctypes.byref(h), 1, 2, 0, 4, 4, 4, 3, 0, None) == \
+        E.SPFFT_INVALID_PARAMETER_ERROR
+    # invalid indices are reported as such, before device allocation
+    bad = (ctypes.c_int * 3)(9, 0, 0)
+    assert lib.spfft_transform_create_independent(ctypes.byref(h), 1, 2, 0, 4, 4, 4, 1, 0, bad) == \
+        E.SPFFT_INVALID_INDICES_ERROR
+    # grid limits are validated first (grid_internal.cpp:61-67)
+    assert lib.spfft_grid_create(ctypes.byref(h), 0, 4, 4, 1, 2, 1) == E.SPFFT_INVALID_PARAMETER_ERROR
+    assert lib.spfft_grid_create(ctypes.byref(h), 4, 4, 4, 1, 4, 1) == E.SPFFT_INVALID_PARAMETER_ERROR
