@@ -53,6 +53,8 @@ LaunchConfig choose_launch_config(const IndexPlan& p, int device) {
   const size_t minY = (ny + 2 * static_cast<size_t>(ny)) * c;
   const size_t minX = (nx + 2 * static_cast<size_t>(cfg.xPitch)) * c;
   if (minZ > optin || minY > optin || minX > optin) throw InvalidParameterError();
+  // The y and x passes put z on gridDim.y.
+  if (nz > 65535) throw InvalidParameterError();
 
   auto fit = [&](size_t fixed, size_t per, int cap) {
     const size_t budget = std::max(kSmemBudget, fixed + per);
