@@ -51,6 +51,20 @@ SPFFT_EXPORT SpfftError spfft_gb300_float_transform_forward_device(SpfftFloatTra
                                                                    SpfftScalingType scaling,
                                                                    void* stream);
 
+/* Profiling aid: run one backward (direction 0: input = values, output = space) or forward
+ * (direction 1: input = space, output = values) on device pointers and `stream`, with CUDA events
+ * around each of the three kernels of the pass; waits and writes the three kernel times (ms) to
+ * stageMs. The pass order is z, y, x for backward and x, y, z for forward. */
+SPFFT_EXPORT SpfftError spfft_gb300_transform_stage_times(SpfftTransform transform, int direction,
+                                                          const double* input, double* output,
+                                                          SpfftScalingType scaling, void* stream,
+                                                          float* stageMs);
+SPFFT_EXPORT SpfftError spfft_gb300_float_transform_stage_times(SpfftFloatTransform transform,
+                                                                int direction, const float* input,
+                                                                float* output,
+                                                                SpfftScalingType scaling,
+                                                                void* stream, float* stageMs);
+
 #ifdef __cplusplus
 }
 #endif

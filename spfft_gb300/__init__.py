@@ -130,6 +130,8 @@ def _declare(lib: ctypes.CDLL) -> None:
         getattr(lib, prefix + "transform_set_stream").argtypes = [_vp, _vp]
         getattr(lib, prefix + "transform_backward_device").argtypes = [_vp, _vp, _vp, _vp]
         getattr(lib, prefix + "transform_forward_device").argtypes = [_vp, _vp, _vp, _i, _vp]
+        getattr(lib, prefix + "transform_stage_times").argtypes = [_vp, _i, _vp, _vp, _i, _vp,
+                                                                   ctypes.POINTER(ctypes.c_float)]
     lib.spfft_gb300_plan_indices.argtypes = [_i, _i, _i, _i, _i, _vp, _vp, _vp, _i, _ip, _ip]
 
 
@@ -350,6 +352,17 @@ class Transform:
         s = None if stream is None else int(getattr(stream, "cuda_stream", stream))
         _call("spfft_gb300_" + self._p[len("spfft_"):] + "transform_forward_device", self._h,
               address(space), address(values), scaling, s)
+
+
+def stage_times(transform: "Transform", direction: int, input: Any, output: Any,
+                scaling: int = SPFFT_NO_SCALING, stream: Any = None) -> list:
+    """Kernel times (ms) of one backward (direction 0) or forward (1) pass: [z, y, x] for
+    backward, [x, y, z] for forward."""
+    ms = (ctypes.c_float * 3)()
+    s = None if stream is None else int(getattr(stream, "cuda_stream", stream))
+    _call("spfft_gb300_" + transform._p[len("spfft_"):] + "transform_stage_times", transform._h,
+          direction, address(input), address(output), scaling, s, ms)
+    return [float(v) for v in ms]
 
 
 def _handles(transforms) -> ctypes.Array:

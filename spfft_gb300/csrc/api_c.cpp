@@ -211,6 +211,15 @@ SPFFT_GB300_GRID_C_API(spfft_float_grid_, GridFloat)
                                                      static_cast<cudaStream_t>(stream));          \
     });                                                                                           \
   }                                                                                               \
+  SpfftError GPREFIX##stage_times(void* transform, int direction, const T* input, T* output,     \
+                                  SpfftScalingType scaling, void* stream, float* stageMs) {       \
+    if (!stageMs || (direction != 0 && direction != 1)) return SPFFT_INVALID_PARAMETER_ERROR;     \
+    return with_handle<spfft::TRANSFORM>(transform, [&](spfft::TRANSFORM& t) {                    \
+      spfft::TransformAccess::get(t).stage_times(direction, input, output,                        \
+                                                 scaling == SPFFT_FULL_SCALING,                   \
+                                                 static_cast<cudaStream_t>(stream), stageMs);     \
+    });                                                                                           \
+  }                                                                                               \
   SpfftError GPREFIX##forward_device(void* transform, const T* space, T* values,                  \
                                      SpfftScalingType scaling, void* stream) {                    \
     return with_handle<spfft::TRANSFORM>(transform, [&](spfft::TRANSFORM& t) {                    \

@@ -161,15 +161,16 @@ PlanView<T> GpuPlan<T>::view(void* scratch) const {
 }
 
 template <typename T>
-void GpuPlan<T>::backward(const T* values, T* space, void* scratch, cudaStream_t stream) const {
-  check_launch(launch_backward<T>(view(scratch), config_, values, space, stream));
+void GpuPlan<T>::backward(const T* values, T* space, void* scratch, cudaStream_t stream,
+                          const StageEvents* events) const {
+  check_launch(launch_backward<T>(view(scratch), config_, values, space, stream, events));
 }
 
 template <typename T>
 void GpuPlan<T>::forward(const T* space, T* values, bool scaled, void* scratch,
-                         cudaStream_t stream) const {
+                         cudaStream_t stream, const StageEvents* events) const {
   check_launch(launch_forward<T>(view(scratch), config_, space, values, scaled ? scale_ : T(0),
-                                 stream));
+                                 stream, events));
 }
 
 template class GpuPlan<double>;

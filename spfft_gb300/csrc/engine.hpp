@@ -29,8 +29,10 @@ public:
   const LaunchConfig& launch_config() const { return config_; }
 
   // values/space are device pointers; scratch points to scratch_layout().total bytes.
-  void backward(const T* values, T* space, void* scratch, cudaStream_t stream) const;
-  void forward(const T* space, T* values, bool scaled, void* scratch, cudaStream_t stream) const;
+  void backward(const T* values, T* space, void* scratch, cudaStream_t stream,
+                const StageEvents* events = nullptr) const;
+  void forward(const T* space, T* values, bool scaled, void* scratch, cudaStream_t stream,
+               const StageEvents* events = nullptr) const;
 
   // Device pointer of the value staging area inside `scratch` (host input / output path).
   T* staging(void* scratch) const {

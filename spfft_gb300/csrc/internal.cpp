@@ -232,6 +232,27 @@ void TransformInternal<T>::forward_device(const T* space, T* values, bool scaled
   gpu_->forward(space, values, scaled, grid_->scratch(), stream);
 }
 
+template <typename T>
+void TransformInternal<T>::stage_times(int direction, const T* in, T* out, bool scaled,
+                                       cudaStream_t stream, float ms[3]) {
+  DeviceGuard guard(grid_->device_id());
+  gb300::StageEvents ev{};
+  for (auto& e : ev.ev) check_cuda(cudaEventCreate(&e));
+  try {
+    if (direction == 0) {
+      gpu_->backward(in, out, grid_->scratch(), stream, &ev);
+    } else {
+      gpu_->forward(in, out, scaled, grid_->scratch(), stream, &ev);
+    }
+    check_cuda(cudaEventSynchronize(ev.ev[3]));
+    for (int i = 0; i < 3; ++i) check_cuda(cudaEventElapsedTime(&ms[i], ev.ev[i], ev.ev[i + 1]));
+  } catch (...) {
+    for (auto& e : ev.ev) (void)cudaEventDestroy(e);
+    throw;
+  }
+  for (auto& e : ev.ev) (void)cudaEventDestroy(e);
+}
+
 template class GridInternal<double>;
 template class GridInternal<float>;
 template class TransformInternal<double>;

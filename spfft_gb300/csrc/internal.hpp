@@ -103,6 +103,10 @@ public:
   // Kernel-only entry points on device pointers, on the stream the caller gives.
   void backward_device(const T* values, T* space, cudaStream_t stream);
   void forward_device(const T* space, T* values, bool scaled, cudaStream_t stream);
+  // One pass in `direction` (0 backward, 1 forward) on device pointers with events between the
+  // three kernels; waits for completion and returns the kernel times in milliseconds.
+  void stage_times(int direction, const T* in, T* out, bool scaled, cudaStream_t stream,
+                   float ms[3]);
 
 private:
   cudaStream_t begin();       // preceding-error check, stream ordering; returns the exec stream

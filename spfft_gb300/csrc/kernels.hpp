@@ -48,14 +48,19 @@ struct LaunchConfig {
   size_t smemZ, smemY, smemX;
 };
 
+// Optional events recorded before pass 0 and after each pass (stage timing).
+struct StageEvents {
+  cudaEvent_t ev[4];
+};
+
 // Backward (frequency -> space). `values` is the interleaved input, `space` the output buffer.
 template <typename T>
 cudaError_t launch_backward(const PlanView<T>& p, const LaunchConfig& c, const T* values, T* space,
-                            cudaStream_t stream);
+                            cudaStream_t stream, const StageEvents* events = nullptr);
 // Forward (space -> frequency). scale == 0 means no scaling.
 template <typename T>
 cudaError_t launch_forward(const PlanView<T>& p, const LaunchConfig& c, const T* space, T* values,
-                           T scale, cudaStream_t stream);
+                           T scale, cudaStream_t stream, const StageEvents* events = nullptr);
 // One-time per-process attribute setup (dynamic shared memory limits).
 template <typename T>
 cudaError_t prepare_kernels(size_t maxSmem);
