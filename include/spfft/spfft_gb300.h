@@ -65,6 +65,25 @@ SPFFT_EXPORT SpfftError spfft_gb300_float_transform_stage_times(SpfftFloatTransf
                                                                 SpfftScalingType scaling,
                                                                 void* stream, float* stageMs);
 
+/* Allocation-free backward transform (no counterpart in the reference). Runs the backward transform
+ * of an existing double-precision transform on device pointers (values: interleaved complex
+ * frequency values; space: the space domain in the transform's layout) on `stream` (a
+ * cudaStream_t; NULL is the default stream), keeping the z-stick and plane intermediates in a
+ * static 64 MiB device array that is part of the library, instead of memory the library allocates.
+ * For callers that cannot let the library call cudaMalloc: applications whose device memory is
+ * owned by their own pool allocator, or code running inside CUDA stream capture, where cudaMalloc
+ * is not permitted. The call allocates nothing and does not synchronise.
+ * Limits and rules:
+ *  - transforms whose intermediates exceed 64 MiB are rejected with SPFFT_INVALID_PARAMETER_ERROR;
+ *  - every GPU that loads the library holds the 64 MiB array until the process exits;
+ *  - all calls share the one array per GPU: calls that overlap on the GPU (different streams, or
+ *    different transforms in flight at once) race and corrupt each other's results;
+ *  - the first call on each device looks up the array's device address; make that first call
+ *    before any stream capture. */
+SPFFT_EXPORT SpfftError spfft_gb300_transform_backward_noalloc(SpfftTransform transform,
+                                                               const double* values,
+                                                               double* space, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
