@@ -65,6 +65,13 @@ SPFFT_EXPORT SpfftError spfft_gb300_float_transform_stage_times(SpfftFloatTransf
                                                                 SpfftScalingType scaling,
                                                                 void* stream, float* stageMs);
 
+/* Which kernels a transform runs (no counterpart in the reference): bit 0 set = size-specialised
+ * z pass, bit 1 set = fused size-specialised plane pass (y and x in one kernel); otherwise the
+ * generic kernels. */
+SPFFT_EXPORT SpfftError spfft_gb300_transform_path_info(SpfftTransform transform, int* flags);
+SPFFT_EXPORT SpfftError spfft_gb300_float_transform_path_info(SpfftFloatTransform transform,
+                                                              int* flags);
+
 /* Allocation-free backward transform (no counterpart in the reference). Runs the backward transform
  * of an existing double-precision transform on device pointers (values: interleaved complex
  * frequency values; space: the space domain in the transform's layout) on `stream` (a

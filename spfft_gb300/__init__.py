@@ -130,6 +130,7 @@ def _declare(lib: ctypes.CDLL) -> None:
         getattr(lib, prefix + "transform_set_stream").argtypes = [_vp, _vp]
         getattr(lib, prefix + "transform_backward_device").argtypes = [_vp, _vp, _vp, _vp]
         getattr(lib, prefix + "transform_forward_device").argtypes = [_vp, _vp, _vp, _i, _vp]
+        getattr(lib, prefix + "transform_path_info").argtypes = [_vp, _ip]
         getattr(lib, prefix + "transform_stage_times").argtypes = [_vp, _i, _vp, _vp, _i, _vp,
                                                                    ctypes.POINTER(ctypes.c_float)]
     lib.spfft_gb300_plan_indices.argtypes = [_i, _i, _i, _i, _i, _vp, _vp, _vp, _i, _ip, _ip]
@@ -337,6 +338,12 @@ class Transform:
             _call(self._p + "transform_forward_ptr", self._h, address(input), address(output), scaling)
 
     # ---- extensions ----------------------------------------------------------------------------
+    def path_info(self) -> dict:
+        """Which kernels run: size-specialised z pass, fused plane pass (else the generic ones)."""
+        v = ctypes.c_int(0)
+        _call("spfft_gb300_" + self._p[len("spfft_"):] + "transform_path_info", self._h, ctypes.byref(v))
+        return {"fast_z": bool(v.value & 1), "fused_plane": bool(v.value & 2)}
+
     def set_stream(self, stream: Any) -> None:
         """Run every later call on this CUDA stream (torch.cuda.Stream, cudaStream_t int or None)."""
         ptr = None if stream is None else int(getattr(stream, "cuda_stream", stream))

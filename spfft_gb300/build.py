@@ -28,7 +28,8 @@ def nvcc() -> str:
 
 
 def _headers() -> list[Path]:
-    hs = list(CSRC.glob("*.hpp")) + list(CSRC.glob("*.cuh")) + list((ROOT / "include" / "spfft").glob("*.h*"))
+    hs = (list(CSRC.glob("*.hpp")) + list(CSRC.glob("*.cuh")) + list(CSRC.glob("*.inc")) +
+          list((ROOT / "include" / "spfft").glob("*.h*")))
     return hs
 
 

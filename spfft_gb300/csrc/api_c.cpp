@@ -220,6 +220,11 @@ SPFFT_GB300_GRID_C_API(spfft_float_grid_, GridFloat)
                                                  static_cast<cudaStream_t>(stream), stageMs);     \
     });                                                                                           \
   }                                                                                               \
+  SpfftError GPREFIX##path_info(void* transform, int* flags) {                                    \
+    return with_handle<spfft::TRANSFORM>(transform, [&](spfft::TRANSFORM& t) {                    \
+      *flags = spfft::TransformAccess::get(t).path_flags();                                       \
+    });                                                                                           \
+  }                                                                                               \
   SpfftError GPREFIX##forward_device(void* transform, const T* space, T* values,                  \
                                      SpfftScalingType scaling, void* stream) {                    \
     return with_handle<spfft::TRANSFORM>(transform, [&](spfft::TRANSFORM& t) {                    \

@@ -1,0 +1,201 @@
+// Register DFTs of compile-time size: Dft<R, SIGN>::run(v) replaces v[0..R) by its length-R DFT
+// with root exp(SIGN * 2 pi i / R), in natural order. Sizes 2, 3, 4, 5, 7, 8 are hand-written
+// butterflies (fft_core.cuh); composite sizes are built as R = R1 * R2 from two register passes and
+// constant twiddles (Cooley-Tukey), fully unrolled so that every value stays in registers.
+#pragma once
+
+#include "fft_core.cuh"
+#include "twiddle_constants.hpp"
+
+namespace spfft {
+namespace gb300 {
+
+// Multiply by exp(SIGN * 2 pi i * m / R) with m, R compile-time constants after unrolling.
+template <int R, int SIGN, typename C>
+__host__ __device__ __forceinline__ C twiddle_const(C a, int m) {
+  using T = decltype(a.x);
+  m %= R;
+  if (m == 0) return a;
+  if (2 * m == R) return make_c(-a.x, -a.y);
+  if (4 * m == R) return cmul_i<SIGN>(a);
+  if (4 * m == 3 * R) return cmul_i<-SIGN>(a);
+  const T c = T(tw_cos(R, m));
+  const T s = T(SIGN * tw_sin(R, m));
+  return make_c(a.x * c - a.y * s, a.x * s + a.y * c);
+}
+
+template <int R>
+struct Factor;  // R = first * second for composite register sizes
+template <> struct Factor<6> { static constexpr int first = 3, second = 2; };
+template <> struct Factor<9> { static constexpr int first = 3, second = 3; };
+template <> struct Factor<10> { static constexpr int first = 5, second = 2; };
+template <> struct Factor<12> { static constexpr int first = 4, second = 3; };
+template <> struct Factor<15> { static constexpr int first = 5, second = 3; };
+template <> struct Factor<16> { static constexpr int first = 4, second = 4; };
+template <> struct Factor<18> { static constexpr int first = 9, second = 2; };
+template <> struct Factor<20> { static constexpr int first = 5, second = 4; };
+template <> struct Factor<24> { static constexpr int first = 8, second = 3; };
+template <> struct Factor<25> { static constexpr int first = 5, second = 5; };
+template <> struct Factor<27> { static constexpr int first = 9, second = 3; };
+template <> struct Factor<30> { static constexpr int first = 6, second = 5; };
+template <> struct Factor<32> { static constexpr int first = 8, second = 4; };
+
+template <int R, int SIGN>
+struct Dft {
+  // Composite: R2 DFTs of size R1 on stride-R2 elements, twiddles, R1 DFTs of size R2.
+  template <typename C>
+  __host__ __device__ __forceinline__ static void run(C* v);
+};
+
+template <int SIGN>
+struct Dft<1, SIGN> {
+  template <typename C>
+  __host__ __device__ __forceinline__ static void run(C*) {}
+};
+template <int SIGN>
+struct Dft<2, SIGN> {
+  template <typename C>
+  __host__ __device__ __forceinline__ static void run(C* v) { dft2<SIGN>(v); }
+};
+template <int SIGN>
+struct Dft<3, SIGN> {
+  template <typename C>
+  __host__ __device__ __forceinline__ static void run(C* v) { dft3<SIGN>(v); }
+};
+template <int SIGN>
+struct Dft<4, SIGN> {
+  template <typename C>
+  __host__ __device__ __forceinline__ static void run(C* v) { dft4<SIGN>(v); }
+};
+template <int SIGN>
+struct Dft<5, SIGN> {
+  template <typename C>
+  __host__ __device__ __forceinline__ static void run(C* v) { dft5<SIGN>(v); }
+};
+template <int SIGN>
+struct Dft<7, SIGN> {
+  template <typename C>
+  __host__ __device__ __forceinline__ static void run(C* v) { dft7<SIGN>(v); }
+};
+template <int SIGN>
+struct Dft<8, SIGN> {
+  template <typename C>
+  __host__ __device__ __forceinline__ static void run(C* v) { dft8<SIGN>(v); }
+};
+
+template <int R, int SIGN>
+template <typename C>
+__host__ __device__ __forceinline__ void Dft<R, SIGN>::run(C* v) {
+  constexpr int R1 = Factor<R>::first, R2 = Factor<R>::second;
+  C t[R];
+#pragma unroll
+  for (int i2 = 0; i2 < R2; ++i2) {
+    C a[R1];
+#pragma unroll
+    for (int i1 = 0; i1 < R1; ++i1) a[i1] = v[i1 * R2 + i2];
+    Dft<R1, SIGN>::run(a);
+#pragma unroll
+    for (int k1 = 0; k1 < R1; ++k1) t[k1 * R2 + i2] = twiddle_const<R, SIGN>(a[k1], k1 * i2);
+  }
+#pragma unroll
+  for (int k1 = 0; k1 < R1; ++k1) {
+    C b[R2];
+#pragma unroll
+    for (int i2 = 0; i2 < R2; ++i2) b[i2] = t[k1 * R2 + i2];
+    Dft<R2, SIGN>::run(b);
+#pragma unroll
+    for (int k2 = 0; k2 < R2; ++k2) v[k1 + R1 * k2] = b[k2];
+  }
+}
+
+// ---- two-pass FFT of length N = A * B on data in shared memory ---------------------------------
+//
+// Input element n = a*B + b sits at buf[n * stride]. Pass 1 (one work item per b): DFT_A over a,
+// multiply by w_N^(k1*b), store back at the same places (k1*B + b). Pass 2 (one work item per
+// k1): DFT_B over b; the result X[k1 + A*k2] is left in registers (v[k2]) for the caller, which
+// either emits it or stores it back in place at buf[(k1*B + k2) * stride] -- the "transposed"
+// order, where X[k] lives at position (k mod A)*B + k div A. tw is the w_N table (forward sign).
+template <int N>
+struct Shape;  // N = A * B
+#define SPFFT_GB300_SHAPE(N_, A_, B_)        \
+  template <>                              \
+  struct Shape<N_> {                       \
+    static constexpr int A = A_, B = B_;   \
+  };
+SPFFT_GB300_SHAPE(3, 3, 1)
+SPFFT_GB300_SHAPE(4, 4, 1)
+SPFFT_GB300_SHAPE(6, 6, 1)
+SPFFT_GB300_SHAPE(8, 8, 1)
+SPFFT_GB300_SHAPE(12, 12, 1)
+SPFFT_GB300_SHAPE(16, 16, 1)
+SPFFT_GB300_SHAPE(24, 8, 3)
+SPFFT_GB300_SHAPE(30, 6, 5)
+SPFFT_GB300_SHAPE(32, 8, 4)
+SPFFT_GB300_SHAPE(36, 6, 6)
+SPFFT_GB300_SHAPE(45, 9, 5)
+SPFFT_GB300_SHAPE(48, 8, 6)
+SPFFT_GB300_SHAPE(50, 10, 5)
+SPFFT_GB300_SHAPE(54, 9, 6)
+SPFFT_GB300_SHAPE(60, 10, 6)
+SPFFT_GB300_SHAPE(64, 8, 8)
+SPFFT_GB300_SHAPE(72, 9, 8)
+SPFFT_GB300_SHAPE(75, 15, 5)
+SPFFT_GB300_SHAPE(80, 10, 8)
+SPFFT_GB300_SHAPE(90, 10, 9)
+SPFFT_GB300_SHAPE(96, 12, 8)
+SPFFT_GB300_SHAPE(100, 10, 10)
+SPFFT_GB300_SHAPE(108, 12, 9)
+SPFFT_GB300_SHAPE(120, 12, 10)
+SPFFT_GB300_SHAPE(128, 16, 8)
+SPFFT_GB300_SHAPE(144, 12, 12)
+SPFFT_GB300_SHAPE(150, 15, 10)
+SPFFT_GB300_SHAPE(160, 16, 10)
+SPFFT_GB300_SHAPE(180, 15, 12)
+SPFFT_GB300_SHAPE(192, 16, 12)
+SPFFT_GB300_SHAPE(240, 16, 15)
+SPFFT_GB300_SHAPE(256, 16, 16)
+#undef SPFFT_GB300_SHAPE
+
+// Position of X[k] after pass 2 stored back in place.
+template <int N>
+__host__ __device__ __forceinline__ int transposed_pos(int k) {
+  constexpr int A = Shape<N>::A, B = Shape<N>::B;
+  return (k % A) * B + k / A;
+}
+
+template <int N, int SIGN, typename C>
+__host__ __device__ __forceinline__ void fft_pass1(C* buf, int stride, int b, const C* __restrict__ tw) {
+  constexpr int A = Shape<N>::A, B = Shape<N>::B;
+  C v[A];
+#pragma unroll
+  for (int a = 0; a < A; ++a) v[a] = buf[(a * B + b) * stride];
+  Dft<A, SIGN>::run(v);
+  if (B > 1) {
+#pragma unroll
+    for (int k1 = 1; k1 < A; ++k1) v[k1] = ctw<SIGN>(v[k1], tw[k1 * b]);
+  }
+#pragma unroll
+  for (int k1 = 0; k1 < A; ++k1) buf[(k1 * B + b) * stride] = v[k1];
+}
+
+// Pass 1 with the inputs already in registers (loaded by the caller from elsewhere).
+template <int N, int SIGN, typename C>
+__host__ __device__ __forceinline__ void fft_pass1_regs(C (&v)[Shape<N>::A], int b, const C* __restrict__ tw) {
+  constexpr int A = Shape<N>::A, B = Shape<N>::B;
+  Dft<A, SIGN>::run(v);
+  if (B > 1) {
+#pragma unroll
+    for (int k1 = 1; k1 < A; ++k1) v[k1] = ctw<SIGN>(v[k1], tw[k1 * b]);
+  }
+}
+
+template <int N, int SIGN, typename C>
+__host__ __device__ __forceinline__ void fft_pass2(const C* buf, int stride, int k1, C (&v)[Shape<N>::B]) {
+  constexpr int B = Shape<N>::B;
+#pragma unroll
+  for (int b = 0; b < B; ++b) v[b] = buf[(k1 * B + b) * stride];
+  Dft<B, SIGN>::run(v);
+}
+
+}  // namespace gb300
+}  // namespace spfft

@@ -8,6 +8,7 @@
 #include <vector>
 
 #include "fft_plan.hpp"
+#include "kernels_fast.hpp"
 
 namespace spfft {
 namespace gb300 {
@@ -35,6 +36,23 @@ void prepare_once(int device) {
   check_cuda(prepare_kernels<T>(static_cast<size_t>(max_smem_optin(device))));
   done.push_back(device);
 }
+
+// Per (device, size) attribute setup of the specialised kernels.
+template <typename T>
+bool prepare_fast_once(int device, int n) {
+  static std::mutex mutex;
+  static std::vector<std::pair<int, int>> done;
+  std::lock_guard<std::mutex> lock(mutex);
+  if (std::find(done.begin(), done.end(), std::make_pair(device, n)) != done.end()) return true;
+  FastArgs<T> a;
+  a.maxSmem = static_cast<size_t>(max_smem_optin(device));
+  if (!fast_dispatch<T>(FastOp::Prepare, n, false, a)) return false;
+  done.emplace_back(device, n);
+  return true;
+}
+
+// Shared memory budget of one specialised z-pass block (four blocks per SM).
+constexpr size_t kFastZBudget = 56 * 1024;
 
 inline int odd_pitch(int n) { return n % 2 == 0 ? n + 1 : n; }
 
@@ -133,6 +151,48 @@ GpuPlan<T>::GpuPlan(const IndexPlan& p, int device) {
   base_.numColumns = ncol;
   base_.r2c = p.type == SPFFT_TRANS_R2C ? 1 : 0;
   base_.zeroZeroStick = (base_.r2c && p.zeroZeroStick < ns) ? p.zeroZeroStick : -1;
+  // Size-specialised kernels where the lengths are supported and shared memory allows.
+  {
+    const size_t optin = static_cast<size_t>(max_smem_optin(device));
+    FastArgs<T> a;
+    const int nz = p.dimZ;
+    if (ns > 0 && fast_dispatch<T>(FastOp::Has, nz, false, a) && prepare_fast_once<T>(device, nz)) {
+      size_t sm = 0;
+      a.smemOut = &sm;
+      // Largest group of sticks per block (<= 32) that still gives one block per SM.
+      int spb = 32;
+      for (; spb > 4; spb /= 2) {
+        a.param = spb;
+        fast_dispatch<T>(FastOp::ZSmem, nz, false, a);
+        const int blocks = (ns + spb - 1) / spb;
+        if (sm <= kFastZBudget && blocks >= 152) break;
+      }
+      a.param = spb;
+      fast_dispatch<T>(FastOp::ZSmem, nz, false, a);
+      if (sm <= optin) {
+        fastZ_ = true;
+        fastSpb_ = spb;
+      }
+    }
+    const bool r2c = p.type == SPFFT_TRANS_R2C;
+    if (ns > 0 && p.dimX == p.dimY && fast_dispatch<T>(FastOp::Has, p.dimX, r2c, a) &&
+        prepare_fast_once<T>(device, p.dimX)) {
+      size_t sm = 0;
+      a.smemOut = &sm;
+      a.numColumns = ncol;
+      // Rows per x chunk: enough work items for the block, fewer if shared memory is short.
+      for (int rows = 32; rows >= 1; rows /= 2) {
+        a.param = rows;
+        fast_dispatch<T>(FastOp::PlaneSmem, p.dimX, r2c, a);
+        if (sm <= optin) {
+          fastPlane_ = true;
+          fastRows_ = rows;
+          break;
+        }
+      }
+    }
+  }
+
   base_.fz = make_radix_plan(p.dimZ);
   base_.fy = make_radix_plan(p.dimY);
   base_.fx = make_radix_plan(p.dimX);
@@ -160,17 +220,92 @@ PlanView<T> GpuPlan<T>::view(void* scratch) const {
   return v;
 }
 
+namespace {
+inline void mark(const StageEvents* e, int i, cudaStream_t s) {
+  if (e) check_cuda(cudaEventRecord(e->ev[i], s));
+}
+}  // namespace
+
+// Complex data must be aligned to its complex size (the kernels move whole complex values). A
+// real R2C space buffer only needs T alignment; unaligned ones take the generic plane passes.
+template <typename T>
+void GpuPlan<T>::check_alignment(const T* values, const T* space, bool* planeAligned) const {
+  const uintptr_t c = 2 * sizeof(T);
+  if (base_.numSticks > 0 && values && reinterpret_cast<uintptr_t>(values) % c != 0) {
+    throw InvalidParameterError();
+  }
+  const bool aligned = reinterpret_cast<uintptr_t>(space) % c == 0;
+  if (!base_.r2c && !aligned) throw InvalidParameterError();
+  if (reinterpret_cast<uintptr_t>(space) % sizeof(T) != 0) throw InvalidParameterError();
+  *planeAligned = aligned;
+}
+
 template <typename T>
 void GpuPlan<T>::backward(const T* values, T* space, void* scratch, cudaStream_t stream,
                           const StageEvents* events) const {
-  check_launch(launch_backward<T>(view(scratch), config_, values, space, stream, events));
+  bool aligned = true;
+  check_alignment(values, space, &aligned);
+  const PlanView<T> v = view(scratch);
+  FastArgs<T> a;
+  a.plan = &v;
+  a.stream = stream;
+  mark(events, 0, stream);
+  if (fastZ_) {
+    a.param = fastSpb_;
+    a.in = values;
+    fast_dispatch<T>(FastOp::ZBackward, base_.dimZ, base_.r2c != 0, a);
+  } else {
+    check_launch(launch_generic<T>(GenericPass::ZBackward, v, config_, values, nullptr, T(0), stream));
+  }
+  check_launch(cudaGetLastError());
+  mark(events, 1, stream);
+  if (fastPlane_ && aligned) {
+    a.param = fastRows_;
+    a.out = space;
+    fast_dispatch<T>(FastOp::PlaneBackward, base_.dimX, base_.r2c != 0, a);
+    check_launch(cudaGetLastError());
+    mark(events, 2, stream);
+  } else {
+    check_launch(launch_generic<T>(GenericPass::YBackward, v, config_, nullptr, nullptr, T(0), stream));
+    mark(events, 2, stream);
+    check_launch(launch_generic<T>(GenericPass::XBackward, v, config_, nullptr, space, T(0), stream));
+  }
+  mark(events, 3, stream);
 }
 
 template <typename T>
 void GpuPlan<T>::forward(const T* space, T* values, bool scaled, void* scratch,
                          cudaStream_t stream, const StageEvents* events) const {
-  check_launch(launch_forward<T>(view(scratch), config_, space, values, scaled ? scale_ : T(0),
-                                 stream, events));
+  bool aligned = true;
+  check_alignment(values, space, &aligned);
+  const PlanView<T> v = view(scratch);
+  FastArgs<T> a;
+  a.plan = &v;
+  a.stream = stream;
+  mark(events, 0, stream);
+  if (fastPlane_ && aligned) {
+    a.param = fastRows_;
+    a.in = space;
+    fast_dispatch<T>(FastOp::PlaneForward, base_.dimX, base_.r2c != 0, a);
+    check_launch(cudaGetLastError());
+    mark(events, 1, stream);
+  } else {
+    check_launch(launch_generic<T>(GenericPass::XForward, v, config_, space, nullptr, T(0), stream));
+    mark(events, 1, stream);
+    check_launch(launch_generic<T>(GenericPass::YForward, v, config_, nullptr, nullptr, T(0), stream));
+  }
+  mark(events, 2, stream);
+  const T scale = scaled ? scale_ : T(0);
+  if (fastZ_) {
+    a.param = fastSpb_;
+    a.out = values;
+    a.scale = scale;
+    fast_dispatch<T>(FastOp::ZForward, base_.dimZ, base_.r2c != 0, a);
+    check_launch(cudaGetLastError());
+  } else {
+    check_launch(launch_generic<T>(GenericPass::ZForward, v, config_, nullptr, values, scale, stream));
+  }
+  mark(events, 3, stream);
 }
 
 template class GpuPlan<double>;

@@ -34,6 +34,9 @@ public:
   void forward(const T* space, T* values, bool scaled, void* scratch, cudaStream_t stream,
                const StageEvents* events = nullptr) const;
 
+  // Which kernels run: bit 0 = size-specialised z pass, bit 1 = fused size-specialised plane pass.
+  int path_flags() const { return (fastZ_ ? 1 : 0) | (fastPlane_ ? 2 : 0); }
+
   // Device pointer of the value staging area inside `scratch` (host input / output path).
   T* staging(void* scratch) const {
     return reinterpret_cast<T*>(static_cast<char*>(scratch) + layout_.valuesOffset);
@@ -42,8 +45,12 @@ public:
 private:
   PlanView<T> view(void* scratch) const;
 
+  void check_alignment(const T* values, const T* space, bool* planeAligned) const;
+
   PlanView<T> base_{};
   LaunchConfig config_{};
+  bool fastZ_ = false, fastPlane_ = false;
+  int fastSpb_ = 0, fastRows_ = 0;
   ScratchLayout layout_{};
   T scale_ = T(1);
   DeviceBuffer tables_;

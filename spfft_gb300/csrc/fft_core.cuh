@@ -30,60 +30,60 @@ struct Complex<float> {
   using type = float2;
 };
 
-__device__ __forceinline__ double2 make_c(double x, double y) { return make_double2(x, y); }
-__device__ __forceinline__ float2 make_c(float x, float y) { return make_float2(x, y); }
+__host__ __device__ __forceinline__ double2 make_c(double x, double y) { return make_double2(x, y); }
+__host__ __device__ __forceinline__ float2 make_c(float x, float y) { return make_float2(x, y); }
 
 template <typename C>
-__device__ __forceinline__ C cadd(C a, C b) {
+__host__ __device__ __forceinline__ C cadd(C a, C b) {
   return make_c(a.x + b.x, a.y + b.y);
 }
 template <typename C>
-__device__ __forceinline__ C csub(C a, C b) {
+__host__ __device__ __forceinline__ C csub(C a, C b) {
   return make_c(a.x - b.x, a.y - b.y);
 }
 template <typename C>
-__device__ __forceinline__ C cmul(C a, C b) {
+__host__ __device__ __forceinline__ C cmul(C a, C b) {
   return make_c(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
 // a * conj(b)
 template <typename C>
-__device__ __forceinline__ C cmulc(C a, C b) {
+__host__ __device__ __forceinline__ C cmulc(C a, C b) {
   return make_c(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y);
 }
 template <typename C, typename T>
-__device__ __forceinline__ C cscale(C a, T s) {
+__host__ __device__ __forceinline__ C cscale(C a, T s) {
   return make_c(a.x * s, a.y * s);
 }
 template <typename C>
-__device__ __forceinline__ C cconj(C a) {
+__host__ __device__ __forceinline__ C cconj(C a) {
   return make_c(a.x, -a.y);
 }
 // Multiply by sign * i.
 template <int SIGN, typename C>
-__device__ __forceinline__ C cmul_i(C a) {
+__host__ __device__ __forceinline__ C cmul_i(C a) {
   return SIGN > 0 ? make_c(-a.y, a.x) : make_c(a.y, -a.x);
 }
 // Multiply by the stage twiddle tw (stored for the forward sign); conjugated for SIGN = +1.
 template <int SIGN, typename C>
-__device__ __forceinline__ C ctw(C a, C tw) {
+__host__ __device__ __forceinline__ C ctw(C a, C tw) {
   return SIGN < 0 ? cmul(a, tw) : cmulc(a, tw);
 }
 template <typename C>
-__device__ __forceinline__ bool cnonzero(C a) {
+__host__ __device__ __forceinline__ bool cnonzero(C a) {
   return a.x != 0 || a.y != 0;
 }
 
 // ---- fixed-radix DFTs on registers (in place, natural output order) ---------------------------
 
 template <int SIGN, typename C>
-__device__ __forceinline__ void dft2(C* v) {
+__host__ __device__ __forceinline__ void dft2(C* v) {
   C a = v[0], b = v[1];
   v[0] = cadd(a, b);
   v[1] = csub(a, b);
 }
 
 template <int SIGN, typename C>
-__device__ __forceinline__ void dft3(C* v) {
+__host__ __device__ __forceinline__ void dft3(C* v) {
   using T = decltype(v[0].x);
   const T h = T(0.8660254037844386467637232);  // sin(2 pi / 3)
   C t1 = cadd(v[1], v[2]);
@@ -96,7 +96,7 @@ __device__ __forceinline__ void dft3(C* v) {
 }
 
 template <int SIGN, typename C>
-__device__ __forceinline__ void dft4(C* v) {
+__host__ __device__ __forceinline__ void dft4(C* v) {
   C t0 = cadd(v[0], v[2]);
   C t1 = csub(v[0], v[2]);
   C t2 = cadd(v[1], v[3]);
@@ -108,7 +108,7 @@ __device__ __forceinline__ void dft4(C* v) {
 }
 
 template <int SIGN, typename C>
-__device__ __forceinline__ void dft5(C* v) {
+__host__ __device__ __forceinline__ void dft5(C* v) {
   using T = decltype(v[0].x);
   const T c1 = T(0.3090169943749474241022934), c2 = T(-0.8090169943749474241022934);
   const T s1 = T(0.9510565162951535721164393), s2 = T(0.5877852522924731291687060);
@@ -127,7 +127,7 @@ __device__ __forceinline__ void dft5(C* v) {
 }
 
 template <int SIGN, typename C>
-__device__ __forceinline__ void dft7(C* v) {
+__host__ __device__ __forceinline__ void dft7(C* v) {
   using T = decltype(v[0].x);
   const T C1 = T(0.6234898018587335305250049), C2 = T(-0.2225209339563144042889026),
           C3 = T(-0.9009688679024191262361023);
@@ -155,7 +155,7 @@ __device__ __forceinline__ void dft7(C* v) {
 }
 
 template <int SIGN, typename C>
-__device__ __forceinline__ void dft8(C* v) {
+__host__ __device__ __forceinline__ void dft8(C* v) {
   using T = decltype(v[0].x);
   const T r = T(0.7071067811865475244008444);
   C b[4], c[4];

@@ -99,6 +99,7 @@ public:
   void set_stream(cudaStream_t stream) { userStream_ = stream; hasUserStream_ = (stream != nullptr); }
   const gb300::IndexPlan& index_plan() const { return *plan_; }
   const gb300::GpuPlan<T>& gpu_plan() const { return *gpu_; }
+  int path_flags() const { return gpu_->path_flags(); }
   GridInternal<T>& grid() { return *grid_; }
   // Kernel-only entry points on device pointers, on the stream the caller gives.
   void backward_device(const T* values, T* space, cudaStream_t stream);

@@ -53,14 +53,14 @@ struct StageEvents {
   cudaEvent_t ev[4];
 };
 
-// Backward (frequency -> space). `values` is the interleaved input, `space` the output buffer.
+// The six passes of the generic kernels. Backward: z (values -> sticks), y (sticks -> planes),
+// x (planes -> space). Forward: x (space -> planes), y (planes -> sticks), z (sticks -> values,
+// scaled unless scale == 0). `in` / `out` are the values or space pointers where a pass touches
+// them and are ignored otherwise.
+enum class GenericPass { ZBackward, YBackward, XBackward, XForward, YForward, ZForward };
 template <typename T>
-cudaError_t launch_backward(const PlanView<T>& p, const LaunchConfig& c, const T* values, T* space,
-                            cudaStream_t stream, const StageEvents* events = nullptr);
-// Forward (space -> frequency). scale == 0 means no scaling.
-template <typename T>
-cudaError_t launch_forward(const PlanView<T>& p, const LaunchConfig& c, const T* space, T* values,
-                           T scale, cudaStream_t stream, const StageEvents* events = nullptr);
+cudaError_t launch_generic(GenericPass pass, const PlanView<T>& p, const LaunchConfig& c,
+                           const T* in, T* out, T scale, cudaStream_t stream);
 // One-time per-process attribute setup (dynamic shared memory limits).
 template <typename T>
 cudaError_t prepare_kernels(size_t maxSmem);

@@ -1,0 +1,45 @@
+// Host interface of the size-specialised kernels (kernels_fast.cuh), instantiated in size groups
+// (kernels_fast_group_*.cu) so the library's translation units compile in parallel.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "kernels.hpp"
+
+namespace spfft {
+namespace gb300 {
+
+enum class FastOp { Has, Prepare, ZBackward, ZForward, PlaneBackward, PlaneForward, PlaneSmem, ZSmem };
+
+template <typename T>
+struct FastArgs {
+  const PlanView<T>* plan = nullptr;
+  int param = 0;  // sticks per block (z) or rows per chunk (plane)
+  const T* in = nullptr;
+  T* out = nullptr;
+  T scale = T(0);
+  cudaStream_t stream = nullptr;
+  size_t maxSmem = 0;
+  int numColumns = 0;
+  size_t* smemOut = nullptr;
+};
+
+// Each group handles its own sizes: returns true if `n` (the z length for z ops, the cubic plane
+// size for plane ops) belongs to the group and the op was performed.
+template <typename T>
+bool fast_group_a(FastOp op, int n, bool r2c, const FastArgs<T>& args);
+template <typename T>
+bool fast_group_b(FastOp op, int n, bool r2c, const FastArgs<T>& args);
+template <typename T>
+bool fast_group_c(FastOp op, int n, bool r2c, const FastArgs<T>& args);
+template <typename T>
+bool fast_group_d(FastOp op, int n, bool r2c, const FastArgs<T>& args);
+
+template <typename T>
+inline bool fast_dispatch(FastOp op, int n, bool r2c, const FastArgs<T>& args) {
+  return fast_group_a<T>(op, n, r2c, args) || fast_group_b<T>(op, n, r2c, args) ||
+         fast_group_c<T>(op, n, r2c, args) || fast_group_d<T>(op, n, r2c, args);
+}
+
+}  // namespace gb300
+}  // namespace spfft

@@ -315,69 +315,46 @@ cudaError_t prepare_kernels(size_t maxSmem) {
   return err;
 }
 
-namespace {
-inline void mark(const StageEvents* e, int i, cudaStream_t s) {
-  if (e) cudaEventRecord(e->ev[i], s);
-}
-}  // namespace
-
 template <typename T>
-cudaError_t launch_backward(const PlanView<T>& p, const LaunchConfig& c, const T* values, T* space,
-                            cudaStream_t stream, const StageEvents* events) {
-  mark(events, 0, stream);
-  if (p.numSticks > 0) {
-    const int gz = (p.numSticks + c.sticksPerBlock - 1) / c.sticksPerBlock;
-    z_backward_kernel<T><<<gz, c.threads, c.smemZ, stream>>>(p, values, c.sticksPerBlock, c.zPitch);
-  }
-  mark(events, 1, stream);
-  if (p.numSticks > 0) {
-    const dim3 gy((p.numColumns + c.columnsPerBlock - 1) / c.columnsPerBlock, p.dimZ);
-    y_backward_kernel<T><<<gy, c.threads, c.smemY, stream>>>(p, c.columnsPerBlock);
-  }
-  mark(events, 2, stream);
+cudaError_t launch_generic(GenericPass pass, const PlanView<T>& p, const LaunchConfig& c,
+                           const T* in, T* out, T scale, cudaStream_t stream) {
+  const int gz = (p.numSticks + c.sticksPerBlock - 1) / c.sticksPerBlock;
+  const dim3 gy((p.numColumns + c.columnsPerBlock - 1) / c.columnsPerBlock, p.dimZ);
   const dim3 gx((p.dimY + c.rowsPerBlock - 1) / c.rowsPerBlock, p.dimZ);
-  x_backward_kernel<T><<<gx, c.threads, c.smemX, stream>>>(p, space, c.rowsPerBlock, c.xPitch);
-  mark(events, 3, stream);
-  return cudaGetLastError();
-}
-
-template <typename T>
-cudaError_t launch_forward(const PlanView<T>& p, const LaunchConfig& c, const T* space, T* values,
-                           T scale, cudaStream_t stream, const StageEvents* events) {
-  mark(events, 0, stream);
-  if (p.numSticks > 0) {
-    const dim3 gx((p.dimY + c.rowsPerBlock - 1) / c.rowsPerBlock, p.dimZ);
-    x_forward_kernel<T><<<gx, c.threads, c.smemX, stream>>>(p, space, c.rowsPerBlock, c.xPitch);
+  switch (pass) {
+    case GenericPass::ZBackward:
+      if (p.numSticks > 0)
+        z_backward_kernel<T><<<gz, c.threads, c.smemZ, stream>>>(p, in, c.sticksPerBlock, c.zPitch);
+      break;
+    case GenericPass::YBackward:
+      if (p.numSticks > 0) y_backward_kernel<T><<<gy, c.threads, c.smemY, stream>>>(p, c.columnsPerBlock);
+      break;
+    case GenericPass::XBackward:
+      x_backward_kernel<T><<<gx, c.threads, c.smemX, stream>>>(p, out, c.rowsPerBlock, c.xPitch);
+      break;
+    case GenericPass::XForward:
+      if (p.numSticks > 0)
+        x_forward_kernel<T><<<gx, c.threads, c.smemX, stream>>>(p, in, c.rowsPerBlock, c.xPitch);
+      break;
+    case GenericPass::YForward:
+      if (p.numSticks > 0) y_forward_kernel<T><<<gy, c.threads, c.smemY, stream>>>(p, c.columnsPerBlock);
+      break;
+    case GenericPass::ZForward:
+      if (p.numSticks > 0)
+        z_forward_kernel<T><<<gz, c.threads, c.smemZ, stream>>>(p, out, scale, c.sticksPerBlock,
+                                                                c.zPitch);
+      break;
   }
-  mark(events, 1, stream);
-  if (p.numSticks > 0) {
-    const dim3 gy((p.numColumns + c.columnsPerBlock - 1) / c.columnsPerBlock, p.dimZ);
-    y_forward_kernel<T><<<gy, c.threads, c.smemY, stream>>>(p, c.columnsPerBlock);
-  }
-  mark(events, 2, stream);
-  if (p.numSticks > 0) {
-    const int gz = (p.numSticks + c.sticksPerBlock - 1) / c.sticksPerBlock;
-    z_forward_kernel<T><<<gz, c.threads, c.smemZ, stream>>>(p, values, scale, c.sticksPerBlock,
-                                                            c.zPitch);
-  }
-  mark(events, 3, stream);
   return cudaGetLastError();
 }
 
 template cudaError_t prepare_kernels<double>(size_t);
 template cudaError_t prepare_kernels<float>(size_t);
-template cudaError_t launch_backward<double>(const PlanView<double>&, const LaunchConfig&,
-                                             const double*, double*, cudaStream_t,
-                                             const StageEvents*);
-template cudaError_t launch_backward<float>(const PlanView<float>&, const LaunchConfig&,
-                                            const float*, float*, cudaStream_t,
-                                            const StageEvents*);
-template cudaError_t launch_forward<double>(const PlanView<double>&, const LaunchConfig&,
-                                            const double*, double*, double, cudaStream_t,
-                                            const StageEvents*);
-template cudaError_t launch_forward<float>(const PlanView<float>&, const LaunchConfig&,
-                                           const float*, float*, float, cudaStream_t,
-                                           const StageEvents*);
+template cudaError_t launch_generic<double>(GenericPass, const PlanView<double>&,
+                                            const LaunchConfig&, const double*, double*, double,
+                                            cudaStream_t);
+template cudaError_t launch_generic<float>(GenericPass, const PlanView<float>&, const LaunchConfig&,
+                                           const float*, float*, float, cudaStream_t);
 
 }  // namespace gb300
 }  // namespace spfft

@@ -251,3 +251,48 @@ def test_buffers_locations_inplace_and_modes(lib):
     assert rel_l2(fa.cpu().numpy(), oracle.forward(want)) <= 1e-12
     with pytest.raises(sp.SpfftError):
         sp.multi_transform_backward([t1, t2], [vin, vin], [oa, ob])
+
+
+def test_kernel_paths_and_fallbacks(lib):
+    """The size-specialised kernels serve the benchmark shapes; shapes they do not cover (odd or
+    non-cubic sizes, planes too large for shared memory, an R2C space buffer aligned to 8 bytes
+    only) fall back to the generic kernels with the same results."""
+    rng = np.random.default_rng(31)
+    # fast paths
+    for dims, ttype in [((64, 64, 64), 0), ((192, 192, 192), 1), ((12, 12, 12), 1), ((100, 100, 13), 0)]:
+        idx = sphere_indices(dims[0], dims[0] // 4, r2c=(ttype == 1)) if dims[2] == dims[0] else \
+            random_indices(rng, *dims, r2c=(ttype == 1))
+        tr = _transform("float64", ttype, dims, idx)
+        info = tr.path_info()
+        assert info["fused_plane"] == (dims[0] == dims[1]), (dims, info)
+        assert info["fast_z"] == (dims[2] in (12, 64, 100, 192)), (dims, info)
+    # 192^3 C2C |k| <= 48 FP64: 97 columns do not fit one block's shared memory -> generic planes
+    idx = sphere_indices(192, 48)
+    tr = _transform("float64", 0, (192, 192, 192), idx)
+    assert tr.path_info() == {"fast_z": True, "fused_plane": False}
+    vals = _values(rng, len(idx))
+    oracle = pipeline.HostPipeline(0, 192, 192, 192, idx)
+    out = torch.empty((192, 192, 192), dtype=torch.complex128, device="cuda")
+    tr.backward(torch.from_numpy(vals).cuda(), out)
+    want = oracle.backward(vals)
+    assert rel_l2(out.cpu().numpy(), want) <= 1e-12
+    # R2C space buffer that is 8-byte but not 16-byte aligned: generic plane passes
+    dims = (48, 48, 48)
+    idx = sphere_indices(48, 12, r2c=True)
+    tr = _transform("float64", 1, dims, idx)
+    assert tr.path_info()["fused_plane"]
+    vals = _values(rng, len(idx))
+    oracle = pipeline.HostPipeline(1, *dims, idx)
+    big = torch.zeros(48 ** 3 + 1, dtype=torch.float64, device="cuda")
+    shifted = big[1:]
+    assert shifted.data_ptr() % 16 == 8
+    tr.backward(torch.from_numpy(vals).cuda(), shifted)
+    assert rel_l2(shifted.cpu().numpy().reshape(48, 48, 48), oracle.backward(vals)) <= 1e-12
+    f = torch.empty(len(idx), dtype=torch.complex128, device="cuda")
+    tr.forward(shifted, f)
+    assert rel_l2(f.cpu().numpy(), oracle.forward(shifted.cpu().numpy().reshape(48, 48, 48))) <= 1e-12
+    # misaligned complex data is rejected, not faulted
+    vbig = torch.zeros(2 * len(idx) + 1, dtype=torch.float64, device="cuda")
+    with pytest.raises(sp.SpfftError) as e:
+        tr.backward(vbig[1:], torch.empty((48, 48, 48), dtype=torch.float64, device="cuda"))
+    assert e.value.code == sp.ErrorCode.SPFFT_INVALID_PARAMETER_ERROR
