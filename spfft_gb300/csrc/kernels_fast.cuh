@@ -36,6 +36,21 @@ __device__ __forceinline__ C<T> czero() {
   return make_c(T(0), T(0));
 }
 
+// Asynchronous global -> shared copy of one complex value (cp.async, 8 or 16 bytes). Lets a
+// thread keep many loads in flight instead of waiting on each.
+template <typename T>
+__device__ __forceinline__ void cp_async_c(C<T>* smemDst, const C<T>* gmemSrc) {
+  const unsigned dst = static_cast<unsigned>(__cvta_generic_to_shared(smemDst));
+  asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(dst), "l"(gmemSrc),
+               "n"(static_cast<int>(sizeof(C<T>)))
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int PENDING>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(PENDING) : "memory");
+}
+
 // Conditional conjugate fill along one line, two ordered halves (symmetry_host.hpp:42-90).
 template <typename T>
 __device__ __forceinline__ void line_fill(C<T>* v, int n, int stride) {
@@ -76,11 +91,25 @@ __global__ void __launch_bounds__(kThreads) z_backward(const PlanView<T> p,
   const C<T>* vals = reinterpret_cast<const C<T>*>(values);
   const int e0 = p.stickEntryStart[s0], e1 = p.stickEntryStart[s0 + nsb];
   const int base = s0 * NZ;
-  for (int e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
-    const int pos = p.entryPos[e] - base;
-    const int sl = pos / NZ;
-    buf[sl * PZ + (pos - sl * NZ)] = vals[p.entryUser[e]];
+  // Index loads four at a time, then asynchronous value copies straight to their stick slots.
+  for (int e = e0 + threadIdx.x; e < e1; e += 4 * blockDim.x) {
+    int pos[4], usr[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int eu = e + u * blockDim.x;
+      pos[u] = eu < e1 ? p.entryPos[eu] - base : -1;
+      usr[u] = eu < e1 ? p.entryUser[eu] : 0;
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      if (pos[u] >= 0) {
+        const int sl = pos[u] / NZ;
+        cp_async_c<T>(buf + sl * PZ + (pos[u] - sl * NZ), vals + usr[u]);
+      }
+    }
   }
+  cp_async_commit();
+  cp_async_wait<0>();
   __syncthreads();
   const int zz = p.zeroZeroStick - s0;
   if (p.r2c && zz >= 0 && zz < nsb) line_fill<T>(buf + zz * PZ, NZ, 1);
@@ -114,8 +143,10 @@ __global__ void __launch_bounds__(kThreads) z_forward(const PlanView<T> p, T* __
   const C<T>* sticks = reinterpret_cast<const C<T>*>(p.sticks) + s0;
   for (int i = threadIdx.x; i < NZ * nsb; i += blockDim.x) {
     const int z = i / nsb, sl = i - z * nsb;
-    buf[sl * PZ + z] = sticks[static_cast<size_t>(z) * p.numSticks + sl];
+    cp_async_c<T>(buf + sl * PZ + z, sticks + static_cast<size_t>(z) * p.numSticks + sl);
   }
+  cp_async_commit();
+  cp_async_wait<0>();
   __syncthreads();
   for (int i = threadIdx.x; i < nsb * B; i += blockDim.x) {
     const int sl = i / B, b = i - sl * B;
@@ -146,7 +177,9 @@ __global__ void __launch_bounds__(kThreads) z_forward(const PlanView<T> p, T* __
 // plane pass (one block per plane z)
 // ================================================================================================
 // Shared memory: twy[NY] | twx[NX] | (R2C) twm[M] | colOf[NXF] (int) | P[NY][numColumns] |
-//                W[rows][LX], with LX = NX (C2C) or M = NX/2 (R2C).
+//                W[2][rows][LX], with LX = NX (C2C) or M = NX/2 (R2C). The forward pass streams row
+//                chunks into the two W halves with cp.async (one chunk in flight while the other
+//                is transformed); the backward pass uses one half.
 template <int NX, int NY, bool R2C>
 struct PlaneLayout {
   static constexpr int M = NX / 2;
@@ -158,7 +191,7 @@ struct PlaneLayout {
     size_t b = (NY + NX + (R2C ? M : 0)) * c;
     b += ((NXF * sizeof(int) + c - 1) / c) * c;
     b += static_cast<size_t>(NY) * numColumns * c;
-    b += static_cast<size_t>(rows) * LX * c;
+    b += 2 * static_cast<size_t>(rows) * LX * c;
     return b;
   }
 };
@@ -212,11 +245,13 @@ __global__ void __launch_bounds__(kThreads) plane_backward(const PlanView<T> p, 
   for (int i = threadIdx.x; i < NY * nc; i += blockDim.x) s.P[i] = czero<T>();
   __syncthreads();
 
-  // sticks of this plane -> compact columns
+  // sticks of this plane -> compact columns, all copies in flight at once
   const C<T>* sticks = reinterpret_cast<const C<T>*>(p.sticks) + static_cast<size_t>(z) * p.numSticks;
   for (int st = threadIdx.x; st < p.numSticks; st += blockDim.x) {
-    s.P[p.stickY[st] * nc + p.stickColumn[st]] = sticks[st];
+    cp_async_c<T>(s.P + p.stickY[st] * nc + p.stickColumn[st], sticks + st);
   }
+  cp_async_commit();
+  cp_async_wait<0>();
   __syncthreads();
   if (R2C && p.columnX[0] == 0) line_fill<T>(s.P, NY, nc);
 
@@ -297,24 +332,37 @@ __global__ void __launch_bounds__(kThreads) plane_forward(const PlanView<T> p,
   __syncthreads();
 
   const C<T>* twl = R2C ? s.twm : s.twx;
-  for (int r0 = 0; r0 < NY; r0 += rows) {
-    const int nr = min(rows, NY - r0);
+  // Row chunks of plane z are contiguous in the space buffer: stream chunk i+1 into the other
+  // half of W while chunk i is transformed.
+  const C<T>* plane = reinterpret_cast<const C<T>*>(space + static_cast<size_t>(z) * NY * NX * (R2C ? 1 : 2));
+  const int nchunks = (NY + rows - 1) / rows;
+  auto issue_chunk = [&](int chunk) {
+    const int r0 = chunk * rows, nr = min(rows, NY - r0);
+    C<T>* dst = s.W + (chunk & 1) * rows * L::LX;
+    const C<T>* src = plane + static_cast<size_t>(r0) * L::LX;
+    for (int i = threadIdx.x; i < nr * L::LX; i += blockDim.x) cp_async_c<T>(dst + i, src + i);
+    cp_async_commit();
+  };
+  issue_chunk(0);
+  for (int chunk = 0; chunk < nchunks; ++chunk) {
+    const int r0 = chunk * rows, nr = min(rows, NY - r0);
+    C<T>* wbase = s.W + (chunk & 1) * rows * L::LX;
+    if (chunk + 1 < nchunks) {
+      issue_chunk(chunk + 1);
+      cp_async_wait<1>();
+    } else {
+      cp_async_wait<0>();
+    }
+    __syncthreads();
     for (int i = threadIdx.x; i < nr * Bx; i += blockDim.x) {
       const int rl = i / Bx, b = i - rl * Bx;
-      const C<T>* in = reinterpret_cast<const C<T>*>(space + (static_cast<size_t>(z) * NY + r0 + rl) * NX * (R2C ? 1 : 2));
-      C<T> v[Ax];
-#pragma unroll
-      for (int a = 0; a < Ax; ++a) v[a] = in[a * Bx + b];
-      fft_pass1_regs<L::LX, -1>(v, b, twl);
-      C<T>* wrow = s.W + rl * L::LX;
-#pragma unroll
-      for (int k1 = 0; k1 < Ax; ++k1) wrow[k1 * Bx + b] = v[k1];
+      fft_pass1<L::LX, -1>(wbase + rl * L::LX, 1, b, twl);
     }
     __syncthreads();
     for (int i = threadIdx.x; i < nr * Ax; i += blockDim.x) {
       const int rl = i / Ax, k1 = i - rl * Ax;
       C<T> v[Bx];
-      C<T>* wrow = s.W + rl * L::LX;
+      C<T>* wrow = wbase + rl * L::LX;
       fft_pass2<L::LX, -1>(wrow, 1, k1, v);
       if (!R2C) {
         C<T>* prow = s.P + (r0 + rl) * nc;
@@ -334,7 +382,7 @@ __global__ void __launch_bounds__(kThreads) plane_forward(const PlanView<T> p,
       for (int i = threadIdx.x; i < nr * nc; i += blockDim.x) {
         const int rl = i / nc, c = i - rl * nc;
         const int k = p.columnX[c];
-        const C<T>* wrow = s.W + rl * L::LX;
+        const C<T>* wrow = wbase + rl * L::LX;
         const C<T> zk = wrow[transposed_pos<L::LX>(k % L::M)];
         const C<T> zm = wrow[transposed_pos<L::LX>((L::M - k) % L::M)];
         const C<T> dif = make_c(zk.x - zm.x, zk.y + zm.y);
