@@ -180,18 +180,14 @@ GpuPlan<T>::GpuPlan(const IndexPlan& p, int device) {
       size_t sm = 0;
       a.smemOut = &sm;
       a.numColumns = ncol;
-      // Rows per x chunk: the largest (<= 32) that keeps two blocks per SM, else the largest
-      // that fits at all.
-      const size_t twoPerSm = optin / 2 - 1024;
-      for (int pass = 0; pass < 2 && !fastPlane_; ++pass) {
-        for (int rows = 32; rows >= 1; rows /= 2) {
-          a.param = rows;
-          fast_dispatch<T>(FastOp::PlaneSmem, p.dimX, r2c, a);
-          if (sm <= (pass == 0 ? twoPerSm : optin)) {
-            fastPlane_ = true;
-            fastRows_ = rows;
-            break;
-          }
+      // Rows per x chunk: the largest (<= 64, one 512-thread block per SM) that fits.
+      for (int rows = 64; rows >= 1; rows /= 2) {
+        a.param = rows;
+        fast_dispatch<T>(FastOp::PlaneSmem, p.dimX, r2c, a);
+        if (sm <= optin) {
+          fastPlane_ = true;
+          fastRows_ = rows;
+          break;
         }
       }
     }

@@ -27,7 +27,8 @@ namespace fast {
 template <typename T>
 using C = typename Complex<T>::type;
 
-constexpr int kThreads = 256;
+constexpr int kThreads = 256;       // z-pass blocks
+constexpr int kPlaneThreads = 512;  // plane blocks (one plane per block, so more warps per SM)
 
 extern __shared__ __align__(16) unsigned char g_fast_smem[];
 
@@ -185,13 +186,21 @@ struct PlaneLayout {
   static constexpr int M = NX / 2;
   static constexpr int LX = R2C ? M : NX;
   static constexpr int NXF = R2C ? M + 1 : NX;
+  // W rows: element e of the x-FFT row sits at e + PAD * (e / Bx), so pass 2 (which reads
+  // e = k1*Bx + b across threads k1) strides by an odd number of slots; row pitch WP = Bx mod 16 so
+  // two rows of pass 1 fall into different halves of the banks.
+  static constexpr int Bx = Shape<LX>::B, Ax = Shape<LX>::A;
+  static constexpr int PAD = (Bx % 2 == 0 && Bx > 1) ? 1 : 0;
+  static constexpr int ROW = LX + PAD * Ax;
+  static constexpr int WP = ROW + ((Bx % 16) - ROW % 16 + 16) % 16;
+  __host__ __device__ static constexpr int wpos(int e) { return e + PAD * (e / Bx); }
   template <typename T>
   static size_t bytes(int numColumns, int rows) {
     const size_t c = sizeof(C<T>);
     size_t b = (NY + NX + (R2C ? M : 0)) * c;
     b += ((NXF * sizeof(int) + c - 1) / c) * c;
     b += static_cast<size_t>(NY) * numColumns * c;
-    b += 2 * static_cast<size_t>(rows) * LX * c;
+    b += 2 * static_cast<size_t>(rows) * WP * c;
     return b;
   }
 };
@@ -233,7 +242,7 @@ __device__ __forceinline__ void plane_load_tables(const PlanView<T>& p, PlaneSme
 }
 
 template <typename T, int NX, int NY, bool R2C>
-__global__ void __launch_bounds__(kThreads) plane_backward(const PlanView<T> p, T* __restrict__ space,
+__global__ void __launch_bounds__(kPlaneThreads) plane_backward(const PlanView<T> p, T* __restrict__ space,
                                                            int rows) {
   using L = PlaneLayout<NX, NY, R2C>;
   constexpr int Ay = Shape<NY>::A, By = Shape<NY>::B;
@@ -301,15 +310,15 @@ __global__ void __launch_bounds__(kThreads) plane_backward(const PlanView<T> p, 
         }
       }
       fft_pass1_regs<L::LX, +1>(v, b, twl);
-      C<T>* wrow = s.W + rl * L::LX;
+      C<T>* wrow = s.W + rl * L::WP;
 #pragma unroll
-      for (int k1 = 0; k1 < Ax; ++k1) wrow[k1 * Bx + b] = v[k1];
+      for (int k1 = 0; k1 < Ax; ++k1) wrow[L::wpos(k1 * Bx + b)] = v[k1];
     }
     __syncthreads();
     for (int i = threadIdx.x; i < nr * Ax; i += blockDim.x) {
       const int rl = i / Ax, k1 = i - rl * Ax;
       C<T> v[Bx];
-      fft_pass2<L::LX, +1>(s.W + rl * L::LX, 1, k1, v);
+      fft_pass2<L::LX, +1>(s.W + rl * L::WP + k1 * L::PAD, 1, k1, v);
       // C2C: complex x row; C2R: pairs (x[2m], x[2m+1]) of the real row
       C<T>* out = reinterpret_cast<C<T>*>(space + (static_cast<size_t>(z) * NY + r0 + rl) * NX * (R2C ? 1 : 2));
 #pragma unroll
@@ -320,7 +329,7 @@ __global__ void __launch_bounds__(kThreads) plane_backward(const PlanView<T> p, 
 }
 
 template <typename T, int NX, int NY, bool R2C>
-__global__ void __launch_bounds__(kThreads) plane_forward(const PlanView<T> p,
+__global__ void __launch_bounds__(kPlaneThreads) plane_forward(const PlanView<T> p,
                                                           const T* __restrict__ space, int rows) {
   using L = PlaneLayout<NX, NY, R2C>;
   constexpr int Ay = Shape<NY>::A, By = Shape<NY>::B;
@@ -338,15 +347,18 @@ __global__ void __launch_bounds__(kThreads) plane_forward(const PlanView<T> p,
   const int nchunks = (NY + rows - 1) / rows;
   auto issue_chunk = [&](int chunk) {
     const int r0 = chunk * rows, nr = min(rows, NY - r0);
-    C<T>* dst = s.W + (chunk & 1) * rows * L::LX;
+    C<T>* dst = s.W + (chunk & 1) * rows * L::WP;
     const C<T>* src = plane + static_cast<size_t>(r0) * L::LX;
-    for (int i = threadIdx.x; i < nr * L::LX; i += blockDim.x) cp_async_c<T>(dst + i, src + i);
+    for (int i = threadIdx.x; i < nr * L::LX; i += blockDim.x) {
+      const int rl = i / L::LX, e = i - rl * L::LX;
+      cp_async_c<T>(dst + rl * L::WP + L::wpos(e), src + i);
+    }
     cp_async_commit();
   };
   issue_chunk(0);
   for (int chunk = 0; chunk < nchunks; ++chunk) {
     const int r0 = chunk * rows, nr = min(rows, NY - r0);
-    C<T>* wbase = s.W + (chunk & 1) * rows * L::LX;
+    C<T>* wbase = s.W + (chunk & 1) * rows * L::WP;
     if (chunk + 1 < nchunks) {
       issue_chunk(chunk + 1);
       cp_async_wait<1>();
@@ -356,13 +368,20 @@ __global__ void __launch_bounds__(kThreads) plane_forward(const PlanView<T> p,
     __syncthreads();
     for (int i = threadIdx.x; i < nr * Bx; i += blockDim.x) {
       const int rl = i / Bx, b = i - rl * Bx;
-      fft_pass1<L::LX, -1>(wbase + rl * L::LX, 1, b, twl);
+      // padded row: element a*Bx + b sits at a*(Bx + PAD) + b
+      C<T>* wrow = wbase + rl * L::WP;
+      C<T> v[Ax];
+#pragma unroll
+      for (int a = 0; a < Ax; ++a) v[a] = wrow[a * (Bx + L::PAD) + b];
+      fft_pass1_regs<L::LX, -1>(v, b, twl);
+#pragma unroll
+      for (int k1 = 0; k1 < Ax; ++k1) wrow[k1 * (Bx + L::PAD) + b] = v[k1];
     }
     __syncthreads();
     for (int i = threadIdx.x; i < nr * Ax; i += blockDim.x) {
       const int rl = i / Ax, k1 = i - rl * Ax;
       C<T> v[Bx];
-      C<T>* wrow = wbase + rl * L::LX;
+      C<T>* wrow = wbase + rl * L::WP + k1 * L::PAD;
       fft_pass2<L::LX, -1>(wrow, 1, k1, v);
       if (!R2C) {
         C<T>* prow = s.P + (r0 + rl) * nc;
@@ -373,7 +392,7 @@ __global__ void __launch_bounds__(kThreads) plane_forward(const PlanView<T> p,
         }
       } else {
 #pragma unroll
-        for (int k2 = 0; k2 < Bx; ++k2) wrow[k1 * Bx + k2] = v[k2];
+        for (int k2 = 0; k2 < Bx; ++k2) wrow[k1 * Bx + k2] = v[k2];  // wrow is offset by k1*PAD
       }
     }
     __syncthreads();
@@ -382,9 +401,9 @@ __global__ void __launch_bounds__(kThreads) plane_forward(const PlanView<T> p,
       for (int i = threadIdx.x; i < nr * nc; i += blockDim.x) {
         const int rl = i / nc, c = i - rl * nc;
         const int k = p.columnX[c];
-        const C<T>* wrow = wbase + rl * L::LX;
-        const C<T> zk = wrow[transposed_pos<L::LX>(k % L::M)];
-        const C<T> zm = wrow[transposed_pos<L::LX>((L::M - k) % L::M)];
+        const C<T>* wrow = wbase + rl * L::WP;
+        const C<T> zk = wrow[L::wpos(transposed_pos<L::LX>(k % L::M))];
+        const C<T> zm = wrow[L::wpos(transposed_pos<L::LX>((L::M - k) % L::M))];
         const C<T> dif = make_c(zk.x - zm.x, zk.y + zm.y);
         const C<T> u = cmul(dif, s.twx[k]);
         s.P[(r0 + rl) * nc + c] = make_c(T(0.5) * (zk.x + zm.x + u.y), T(0.5) * (zk.y - zm.y - u.x));
@@ -447,10 +466,10 @@ struct PlaneKernels {
     return e1 != cudaSuccess ? e1 : e2;
   }
   static void backward(const PlanView<T>& p, int rows, T* space, cudaStream_t st) {
-    plane_backward<T, NX, NY, R2C><<<NY == 0 ? 0 : p.dimZ, kThreads, smem(p.numColumns, rows), st>>>(p, space, rows);
+    plane_backward<T, NX, NY, R2C><<<p.dimZ, kPlaneThreads, smem(p.numColumns, rows), st>>>(p, space, rows);
   }
   static void forward(const PlanView<T>& p, int rows, const T* space, cudaStream_t st) {
-    plane_forward<T, NX, NY, R2C><<<p.dimZ, kThreads, smem(p.numColumns, rows), st>>>(p, space, rows);
+    plane_forward<T, NX, NY, R2C><<<p.dimZ, kPlaneThreads, smem(p.numColumns, rows), st>>>(p, space, rows);
   }
 };
 
