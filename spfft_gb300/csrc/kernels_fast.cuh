@@ -13,10 +13,19 @@
 // local_transpose_kernels.cu:43-201 and the cuFFT calls of transform_1d_gpu.hpp /
 // transform_2d_gpu.hpp / transform_real_2d_gpu.hpp (all in the reference's src/). Compared with the
 // generic kernels, the y and x passes are one kernel, so the compact plane never goes to HBM.
+//
+// Types: S is the storage type in HBM (values, sticks, space), A the arithmetic type of the FFTs
+// (float for FP32; dd, double-float on the FP32 pipes, for FP64). With A = dd every block finds
+// the largest binary64 exponent of the data it loads, converts with an exact power-of-two scale
+// that brings that maximum into [1, 2), and undoes the scale when it stores -- so every double
+// magnitude is handled, and the FFT arithmetic never touches GB300's slow FP64 pipe.
 #pragma once
 
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
+#include "dd.cuh"
 #include "dft.cuh"
 #include "kernels.hpp"
 
@@ -24,26 +33,67 @@ namespace spfft {
 namespace gb300 {
 namespace fast {
 
-template <typename T>
-using C = typename Complex<T>::type;
-
 constexpr int kThreads = 256;       // z-pass blocks
 constexpr int kPlaneThreads = 512;  // plane blocks (one plane per block, so more warps per SM)
 
 extern __shared__ __align__(16) unsigned char g_fast_smem[];
 
-template <typename T>
-__device__ __forceinline__ C<T> czero() {
-  return make_c(T(0), T(0));
+// ---- types and conversions ----------------------------------------------------------------------
+template <typename A>
+struct ArithC;
+template <>
+struct ArithC<float> {
+  using type = float2;
+};
+template <>
+struct ArithC<dd> {
+  using type = ddc;
+};
+
+template <typename S, typename A>
+struct Types {
+  using CS = typename Complex<S>::type;
+  using CA = typename ArithC<A>::type;
+  static constexpr bool kScaled = !std::is_same<S, A>::value;
+  static_assert(sizeof(CS) == sizeof(CA), "storage and arithmetic complex must have equal size");
+};
+
+template <typename A>
+__device__ __forceinline__ typename ArithC<A>::type czero() {
+  return make_c(A(0), A(0));
 }
+
+// storage -> arithmetic with the block scale 2^k
+__device__ __forceinline__ float2 to_arith(float2 v, int) { return v; }
+__device__ __forceinline__ ddc to_arith(double2 v, int k) {
+  return make_c(dd_from_double(v.x, k), dd_from_double(v.y, k));
+}
+// arithmetic -> storage, undoing the block scale
+__device__ __forceinline__ float2 to_storage(float2 v, int) { return v; }
+__device__ __forceinline__ double2 to_storage(ddc v, int k) {
+  return make_double2(dd_to_double(v.x, -k), dd_to_double(v.y, -k));
+}
+// twiddles: double tables -> dd, float tables as they are
+__device__ __forceinline__ float2 tw_arith(float2 v) { return v; }
+__device__ __forceinline__ ddc tw_arith(double2 v) {
+  return make_c(dd_from_double(v.x, 0), dd_from_double(v.y, 0));
+}
+
+__device__ __forceinline__ int max_exponent(float2) { return 0; }
+__device__ __forceinline__ int max_exponent(double2 v) {
+  return max(dd_exponent_field(v.x), dd_exponent_field(v.y));
+}
+// Scale exponent k for a block whose largest biased binary64 exponent is e: 2^k * max in [1, 2).
+// Zero, subnormal-only and non-finite blocks use k = 0.
+__device__ __forceinline__ int block_scale(int e) { return (e == 0 || e == 2047) ? 0 : 1023 - e; }
 
 // Asynchronous global -> shared copy of one complex value (cp.async, 8 or 16 bytes). Lets a
 // thread keep many loads in flight instead of waiting on each.
-template <typename T>
-__device__ __forceinline__ void cp_async_c(C<T>* smemDst, const C<T>* gmemSrc) {
+template <typename CS>
+__device__ __forceinline__ void cp_async_c(void* smemDst, const CS* gmemSrc) {
   const unsigned dst = static_cast<unsigned>(__cvta_generic_to_shared(smemDst));
   asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(dst), "l"(gmemSrc),
-               "n"(static_cast<int>(sizeof(C<T>)))
+               "n"(static_cast<int>(sizeof(CS)))
                : "memory");
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
@@ -52,19 +102,48 @@ __device__ __forceinline__ void cp_async_wait() {
   asm volatile("cp.async.wait_group %0;\n" ::"n"(PENDING) : "memory");
 }
 
+// After raw storage values were copied into n arithmetic slots: find the block scale (dd only)
+// and convert in place. Ends with __syncthreads(). Returns the scale exponent k.
+template <typename S, typename A>
+__device__ __forceinline__ int convert_block(typename Types<S, A>::CA* slots, int n, int* sExp) {
+  using TT = Types<S, A>;
+  if (!TT::kScaled) return 0;
+  using CS = typename TT::CS;
+  if (threadIdx.x == 0) *sExp = 0;
+  __syncthreads();
+  int e = 0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) e = max(e, max_exponent(reinterpret_cast<const CS*>(slots)[i]));
+  atomicMax(sExp, e);
+  __syncthreads();
+  const int k = block_scale(*sExp);
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const CS raw = reinterpret_cast<const CS*>(slots)[i];
+    slots[i] = to_arith(raw, k);
+  }
+  __syncthreads();
+  return k;
+}
+
 // Conditional conjugate fill along one line, two ordered halves (symmetry_host.hpp:42-90).
-template <typename T>
-__device__ __forceinline__ void line_fill(C<T>* v, int n, int stride) {
+template <typename CA>
+__device__ __forceinline__ void line_fill(CA* v, int n, int stride) {
   for (int k = 1 + threadIdx.x; k < n / 2 + 1; k += blockDim.x) {
-    C<T> a = v[k * stride];
+    CA a = v[k * stride];
     if (cnonzero(a)) v[(n - k) * stride] = cconj(a);
   }
   __syncthreads();
   for (int k = n / 2 + 1 + threadIdx.x; k < n; k += blockDim.x) {
-    C<T> a = v[k * stride];
+    CA a = v[k * stride];
     if (cnonzero(a)) v[(n - k) * stride] = cconj(a);
   }
   __syncthreads();
+}
+
+template <typename S, typename A>
+__device__ __forceinline__ void load_twiddles(typename Types<S, A>::CA* dst, const S* src, int n) {
+  using CS = typename Types<S, A>::CS;
+  const CS* s = reinterpret_cast<const CS*>(src);
+  for (int i = threadIdx.x; i < n; i += blockDim.x) dst[i] = tw_arith(s[i]);
 }
 
 // ================================================================================================
@@ -75,21 +154,24 @@ struct ZLayout {
   static constexpr int pitch = NZ | 1;  // odd: conflict-free column access across sticks
 };
 
-template <typename T, int NZ>
-__global__ void __launch_bounds__(kThreads) z_backward(const PlanView<T> p,
-                                                       const T* __restrict__ values, int spb) {
-  constexpr int A = Shape<NZ>::A, B = Shape<NZ>::B, PZ = ZLayout<NZ>::pitch;
-  C<T>* tw = reinterpret_cast<C<T>*>(g_fast_smem);
-  C<T>* buf = tw + NZ;
+template <typename S, typename A, int NZ>
+__global__ void __launch_bounds__(kThreads) z_backward(const PlanView<S> p,
+                                                       const S* __restrict__ values, int spb) {
+  using TT = Types<S, A>;
+  using CS = typename TT::CS;
+  using CA = typename TT::CA;
+  constexpr int Az = Shape<NZ>::A, Bz = Shape<NZ>::B, PZ = ZLayout<NZ>::pitch;
+  __shared__ int sExp;
+  CA* tw = reinterpret_cast<CA*>(g_fast_smem);
+  CA* buf = tw + NZ;
   const int s0 = blockIdx.x * spb;
   const int nsb = min(spb, p.numSticks - s0);
 
-  const C<T>* twg = reinterpret_cast<const C<T>*>(p.twz);
-  for (int i = threadIdx.x; i < NZ; i += blockDim.x) tw[i] = twg[i];
-  for (int i = threadIdx.x; i < nsb * PZ; i += blockDim.x) buf[i] = czero<T>();
+  load_twiddles<S, A>(tw, p.twz, NZ);
+  for (int i = threadIdx.x; i < nsb * PZ; i += blockDim.x) buf[i] = czero<A>();
   __syncthreads();
 
-  const C<T>* vals = reinterpret_cast<const C<T>*>(values);
+  const CS* vals = reinterpret_cast<const CS*>(values);
   const int e0 = p.stickEntryStart[s0], e1 = p.stickEntryStart[s0 + nsb];
   const int base = s0 * NZ;
   // Index loads four at a time, then asynchronous value copies straight to their stick slots.
@@ -105,71 +187,85 @@ __global__ void __launch_bounds__(kThreads) z_backward(const PlanView<T> p,
     for (int u = 0; u < 4; ++u) {
       if (pos[u] >= 0) {
         const int sl = pos[u] / NZ;
-        cp_async_c<T>(buf + sl * PZ + (pos[u] - sl * NZ), vals + usr[u]);
+        cp_async_c(buf + sl * PZ + (pos[u] - sl * NZ), vals + usr[u]);
       }
     }
   }
   cp_async_commit();
   cp_async_wait<0>();
   __syncthreads();
-  const int zz = p.zeroZeroStick - s0;
-  if (p.r2c && zz >= 0 && zz < nsb) line_fill<T>(buf + zz * PZ, NZ, 1);
+  const int k = convert_block<S, A>(buf, nsb * PZ, &sExp);
 
-  for (int i = threadIdx.x; i < nsb * B; i += blockDim.x) {
-    const int sl = i / B, b = i - sl * B;
+  const int zz = p.zeroZeroStick - s0;
+  if (p.r2c && zz >= 0 && zz < nsb) line_fill(buf + zz * PZ, NZ, 1);
+
+  for (int i = threadIdx.x; i < nsb * Bz; i += blockDim.x) {
+    const int sl = i / Bz, b = i - sl * Bz;
     fft_pass1<NZ, +1>(buf + sl * PZ, 1, b, tw);
   }
   __syncthreads();
-  C<T>* sticks = reinterpret_cast<C<T>*>(p.sticks) + s0;
-  for (int i = threadIdx.x; i < nsb * A; i += blockDim.x) {
+  CS* sticks = reinterpret_cast<CS*>(p.sticks) + s0;
+  for (int i = threadIdx.x; i < nsb * Az; i += blockDim.x) {
     const int k1 = i / nsb, sl = i - k1 * nsb;
-    C<T> v[B];
+    CA v[Bz];
     fft_pass2<NZ, +1>(buf + sl * PZ, 1, k1, v);
 #pragma unroll
-    for (int k2 = 0; k2 < B; ++k2) sticks[static_cast<size_t>(k1 + A * k2) * p.numSticks + sl] = v[k2];
+    for (int k2 = 0; k2 < Bz; ++k2) {
+      sticks[static_cast<size_t>(k1 + Az * k2) * p.numSticks + sl] = to_storage(v[k2], k);
+    }
   }
 }
 
-template <typename T, int NZ>
-__global__ void __launch_bounds__(kThreads) z_forward(const PlanView<T> p, T* __restrict__ values,
-                                                      T scale, int spb) {
-  constexpr int A = Shape<NZ>::A, B = Shape<NZ>::B, PZ = ZLayout<NZ>::pitch;
-  C<T>* tw = reinterpret_cast<C<T>*>(g_fast_smem);
-  C<T>* buf = tw + NZ;
+template <typename S, typename A, int NZ>
+__global__ void __launch_bounds__(kThreads) z_forward(const PlanView<S> p, S* __restrict__ values,
+                                                      S scale, int spb) {
+  using TT = Types<S, A>;
+  using CS = typename TT::CS;
+  using CA = typename TT::CA;
+  constexpr int Az = Shape<NZ>::A, Bz = Shape<NZ>::B, PZ = ZLayout<NZ>::pitch;
+  __shared__ int sExp;
+  CA* tw = reinterpret_cast<CA*>(g_fast_smem);
+  CA* buf = tw + NZ;
   const int s0 = blockIdx.x * spb;
   const int nsb = min(spb, p.numSticks - s0);
 
-  const C<T>* twg = reinterpret_cast<const C<T>*>(p.twz);
-  for (int i = threadIdx.x; i < NZ; i += blockDim.x) tw[i] = twg[i];
-  const C<T>* sticks = reinterpret_cast<const C<T>*>(p.sticks) + s0;
+  load_twiddles<S, A>(tw, p.twz, NZ);
+  const CS* sticks = reinterpret_cast<const CS*>(p.sticks) + s0;
   for (int i = threadIdx.x; i < NZ * nsb; i += blockDim.x) {
     const int z = i / nsb, sl = i - z * nsb;
-    cp_async_c<T>(buf + sl * PZ + z, sticks + static_cast<size_t>(z) * p.numSticks + sl);
+    cp_async_c(buf + sl * PZ + z, sticks + static_cast<size_t>(z) * p.numSticks + sl);
+  }
+  // the pitch padding slots are never read; zero them so the block scale ignores them
+  for (int i = threadIdx.x; i < nsb; i += blockDim.x) {
+    if (PZ > NZ) buf[i * PZ + NZ] = czero<A>();
   }
   cp_async_commit();
   cp_async_wait<0>();
   __syncthreads();
-  for (int i = threadIdx.x; i < nsb * B; i += blockDim.x) {
-    const int sl = i / B, b = i - sl * B;
+  const int k = convert_block<S, A>(buf, nsb * PZ, &sExp);
+  for (int i = threadIdx.x; i < nsb * Bz; i += blockDim.x) {
+    const int sl = i / Bz, b = i - sl * Bz;
     fft_pass1<NZ, -1>(buf + sl * PZ, 1, b, tw);
   }
   __syncthreads();
-  for (int i = threadIdx.x; i < nsb * A; i += blockDim.x) {
+  for (int i = threadIdx.x; i < nsb * Az; i += blockDim.x) {
     const int k1 = i / nsb, sl = i - k1 * nsb;
-    C<T> v[B];
+    CA v[Bz];
     fft_pass2<NZ, -1>(buf + sl * PZ, 1, k1, v);
 #pragma unroll
-    for (int k2 = 0; k2 < B; ++k2) buf[sl * PZ + k1 * B + k2] = v[k2];
+    for (int k2 = 0; k2 < Bz; ++k2) buf[sl * PZ + k1 * Bz + k2] = v[k2];
   }
   __syncthreads();
-  C<T>* out = reinterpret_cast<C<T>*>(values);
+  CS* out = reinterpret_cast<CS*>(values);
   const int e0 = p.stickEntryStart[s0], e1 = p.stickEntryStart[s0 + nsb];
   const int base = s0 * NZ;
   for (int e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
     const int pos = p.entryPos[e] - base;
     const int sl = pos / NZ;
-    C<T> v = buf[sl * PZ + transposed_pos<NZ>(pos - sl * NZ)];
-    if (scale != T(0)) v = cscale(v, scale);
+    CS v = to_storage(buf[sl * PZ + transposed_pos<NZ>(pos - sl * NZ)], k);
+    // scaling multiplies by S(1 / (Nx Ny Nz)) in S, like compress_kernel_scaled
+    // (compression_kernels.cu:106-128)
+    if (scale != S(0)) v = cscale(v, scale);
     out[p.entryUser[e]] = v;
   }
 }
@@ -178,9 +274,9 @@ __global__ void __launch_bounds__(kThreads) z_forward(const PlanView<T> p, T* __
 // plane pass (one block per plane z)
 // ================================================================================================
 // Shared memory: twy[NY] | twx[NX] | (R2C) twm[M] | colOf[NXF] (int) | P[NY][numColumns] |
-//                W[2][rows][LX], with LX = NX (C2C) or M = NX/2 (R2C). The forward pass streams row
-//                chunks into the two W halves with cp.async (one chunk in flight while the other
-//                is transformed); the backward pass uses one half.
+//                W[2][rows][WP], with LX = NX (C2C) or M = NX/2 (R2C). The forward pass streams
+//                row chunks into the two W halves with cp.async (one chunk in flight while the
+//                other is transformed); the backward pass uses one half.
 template <int NX, int NY, bool R2C>
 struct PlaneLayout {
   static constexpr int M = NX / 2;
@@ -194,9 +290,9 @@ struct PlaneLayout {
   static constexpr int ROW = LX + PAD * Ax;
   static constexpr int WP = ROW + ((Bx % 16) - ROW % 16 + 16) % 16;
   __host__ __device__ static constexpr int wpos(int e) { return e + PAD * (e / Bx); }
-  template <typename T>
+  template <typename CA>
   static size_t bytes(int numColumns, int rows) {
-    const size_t c = sizeof(C<T>);
+    const size_t c = sizeof(CA);
     size_t b = (NY + NX + (R2C ? M : 0)) * c;
     b += ((NXF * sizeof(int) + c - 1) / c) * c;
     b += static_cast<size_t>(NY) * numColumns * c;
@@ -205,64 +301,70 @@ struct PlaneLayout {
   }
 };
 
-template <typename T, int NX, int NY, bool R2C>
+template <typename CA, int NX, int NY, bool R2C>
 struct PlaneSmem {
   using L = PlaneLayout<NX, NY, R2C>;
-  C<T>* twy;
-  C<T>* twx;
-  C<T>* twm;
+  CA* twy;
+  CA* twx;
+  CA* twm;
   int* colOf;
-  C<T>* P;
-  C<T>* W;
-  __device__ __forceinline__ PlaneSmem(int numColumns) {
-    const size_t c = sizeof(C<T>);
-    twy = reinterpret_cast<C<T>*>(g_fast_smem);
+  CA* P;
+  CA* W;
+  __device__ __forceinline__ explicit PlaneSmem(int numColumns) {
+    const size_t c = sizeof(CA);
+    twy = reinterpret_cast<CA*>(g_fast_smem);
     twx = twy + NY;
     twm = twx + NX;
     colOf = reinterpret_cast<int*>(twm + (R2C ? L::M : 0));
-    P = reinterpret_cast<C<T>*>(reinterpret_cast<unsigned char*>(colOf) +
-                                ((L::NXF * sizeof(int) + c - 1) / c) * c);
+    P = reinterpret_cast<CA*>(reinterpret_cast<unsigned char*>(colOf) +
+                              ((L::NXF * sizeof(int) + c - 1) / c) * c);
     W = P + NY * numColumns;
   }
 };
 
-template <typename T, int NX, int NY, bool R2C>
-__device__ __forceinline__ void plane_load_tables(const PlanView<T>& p, PlaneSmem<T, NX, NY, R2C>& s) {
+template <typename S, typename A, int NX, int NY, bool R2C>
+__device__ __forceinline__ void plane_load_tables(const PlanView<S>& p,
+                                                  PlaneSmem<typename Types<S, A>::CA, NX, NY, R2C>& s) {
   using L = PlaneLayout<NX, NY, R2C>;
-  const C<T>* ty = reinterpret_cast<const C<T>*>(p.twy);
-  const C<T>* tx = reinterpret_cast<const C<T>*>(p.twx);
-  for (int i = threadIdx.x; i < NY; i += blockDim.x) s.twy[i] = ty[i];
-  for (int i = threadIdx.x; i < NX; i += blockDim.x) s.twx[i] = tx[i];
+  using CS = typename Types<S, A>::CS;
+  load_twiddles<S, A>(s.twy, p.twy, NY);
+  load_twiddles<S, A>(s.twx, p.twx, NX);
   if (R2C) {
-    for (int i = threadIdx.x; i < L::M; i += blockDim.x) s.twm[i] = tx[2 * i];  // w_M = w_N^2
+    const CS* tx = reinterpret_cast<const CS*>(p.twx);
+    for (int i = threadIdx.x; i < L::M; i += blockDim.x) s.twm[i] = tw_arith(tx[2 * i]);  // w_M = w_N^2
   }
   for (int i = threadIdx.x; i < L::NXF; i += blockDim.x) s.colOf[i] = -1;
   __syncthreads();
   for (int c = threadIdx.x; c < p.numColumns; c += blockDim.x) s.colOf[p.columnX[c]] = c;
 }
 
-template <typename T, int NX, int NY, bool R2C>
-__global__ void __launch_bounds__(kPlaneThreads) plane_backward(const PlanView<T> p, T* __restrict__ space,
-                                                           int rows) {
+template <typename S, typename A, int NX, int NY, bool R2C>
+__global__ void __launch_bounds__(kPlaneThreads) plane_backward(const PlanView<S> p,
+                                                                S* __restrict__ space, int rows) {
+  using TT = Types<S, A>;
+  using CS = typename TT::CS;
+  using CA = typename TT::CA;
   using L = PlaneLayout<NX, NY, R2C>;
   constexpr int Ay = Shape<NY>::A, By = Shape<NY>::B;
-  constexpr int Ax = Shape<L::LX>::A, Bx = Shape<L::LX>::B;
+  constexpr int Ax = L::Ax, Bx = L::Bx;
+  __shared__ int sExp;
   const int z = blockIdx.x;
   const int nc = p.numColumns;
-  PlaneSmem<T, NX, NY, R2C> s(nc);
-  plane_load_tables<T, NX, NY, R2C>(p, s);
-  for (int i = threadIdx.x; i < NY * nc; i += blockDim.x) s.P[i] = czero<T>();
+  PlaneSmem<CA, NX, NY, R2C> s(nc);
+  plane_load_tables<S, A, NX, NY, R2C>(p, s);
+  for (int i = threadIdx.x; i < NY * nc; i += blockDim.x) s.P[i] = czero<A>();
   __syncthreads();
 
   // sticks of this plane -> compact columns, all copies in flight at once
-  const C<T>* sticks = reinterpret_cast<const C<T>*>(p.sticks) + static_cast<size_t>(z) * p.numSticks;
+  const CS* sticks = reinterpret_cast<const CS*>(p.sticks) + static_cast<size_t>(z) * p.numSticks;
   for (int st = threadIdx.x; st < p.numSticks; st += blockDim.x) {
-    cp_async_c<T>(s.P + p.stickY[st] * nc + p.stickColumn[st], sticks + st);
+    cp_async_c(s.P + p.stickY[st] * nc + p.stickColumn[st], sticks + st);
   }
   cp_async_commit();
   cp_async_wait<0>();
   __syncthreads();
-  if (R2C && p.columnX[0] == 0) line_fill<T>(s.P, NY, nc);
+  const int k = convert_block<S, A>(s.P, NY * nc, &sExp);
+  if (R2C && p.columnX[0] == 0) line_fill(s.P, NY, nc);
 
   // y-FFT on every compact column, result rows left in transposed order
   for (int i = threadIdx.x; i < nc * By; i += blockDim.x) {
@@ -272,7 +374,7 @@ __global__ void __launch_bounds__(kPlaneThreads) plane_backward(const PlanView<T
   __syncthreads();
   for (int i = threadIdx.x; i < nc * Ay; i += blockDim.x) {
     const int k1 = i / nc, c = i - k1 * nc;
-    C<T> v[By];
+    CA v[By];
     fft_pass2<NY, +1>(s.P + c, nc, k1, v);
 #pragma unroll
     for (int k2 = 0; k2 < By; ++k2) s.P[(k1 * By + k2) * nc + c] = v[k2];
@@ -280,85 +382,102 @@ __global__ void __launch_bounds__(kPlaneThreads) plane_backward(const PlanView<T
   __syncthreads();
 
   // x-FFT of every row
-  const C<T>* twl = R2C ? s.twm : s.twx;
+  const CA* twl = R2C ? s.twm : s.twx;
   for (int r0 = 0; r0 < NY; r0 += rows) {
     const int nr = min(rows, NY - r0);
     for (int i = threadIdx.x; i < nr * Bx; i += blockDim.x) {
       const int rl = i / Bx, b = i - rl * Bx;
-      const C<T>* prow = s.P + transposed_pos<NY>(r0 + rl) * nc;
-      C<T> v[Ax];
+      const CA* prow = s.P + transposed_pos<NY>(r0 + rl) * nc;
+      CA v[Ax];
 #pragma unroll
       for (int a = 0; a < Ax; ++a) {
-        const int k = a * Bx + b;
+        const int kk = a * Bx + b;
         if (!R2C) {
-          const int col = s.colOf[k];
-          v[a] = col >= 0 ? prow[col] : czero<T>();
+          const int col = s.colOf[kk];
+          v[a] = col >= 0 ? prow[col] : czero<A>();
         } else {
           // Half-length C2R: Z'[k] = (X[k] + conj X[M-k]) + i e^{+2 pi i k/N} (X[k] - conj X[M-k]),
           // with only the real parts of X[0] and X[M] (the C2R convention).
-          const int ck = s.colOf[k], cm = s.colOf[L::M - k];
-          const C<T> xk = ck >= 0 ? prow[ck] : czero<T>();
-          const C<T> xm = cm >= 0 ? prow[cm] : czero<T>();
-          if (k == 0) {
+          const int ck = s.colOf[kk], cm = s.colOf[L::M - kk];
+          const CA xk = ck >= 0 ? prow[ck] : czero<A>();
+          const CA xm = cm >= 0 ? prow[cm] : czero<A>();
+          if (kk == 0) {
             v[a] = make_c(xk.x + xm.x, xk.x - xm.x);
           } else {
-            const C<T> sum = make_c(xk.x + xm.x, xk.y - xm.y);
-            const C<T> dif = make_c(xk.x - xm.x, xk.y + xm.y);
-            const C<T> u = cmulc(dif, s.twx[k]);
+            const CA sum = make_c(xk.x + xm.x, xk.y - xm.y);
+            const CA dif = make_c(xk.x - xm.x, xk.y + xm.y);
+            const CA u = cmulc(dif, s.twx[kk]);
             v[a] = make_c(sum.x - u.y, sum.y + u.x);
           }
         }
       }
       fft_pass1_regs<L::LX, +1>(v, b, twl);
-      C<T>* wrow = s.W + rl * L::WP;
+      CA* wrow = s.W + rl * L::WP;
 #pragma unroll
       for (int k1 = 0; k1 < Ax; ++k1) wrow[L::wpos(k1 * Bx + b)] = v[k1];
     }
     __syncthreads();
     for (int i = threadIdx.x; i < nr * Ax; i += blockDim.x) {
       const int rl = i / Ax, k1 = i - rl * Ax;
-      C<T> v[Bx];
+      CA v[Bx];
       fft_pass2<L::LX, +1>(s.W + rl * L::WP + k1 * L::PAD, 1, k1, v);
       // C2C: complex x row; C2R: pairs (x[2m], x[2m+1]) of the real row
-      C<T>* out = reinterpret_cast<C<T>*>(space + (static_cast<size_t>(z) * NY + r0 + rl) * NX * (R2C ? 1 : 2));
+      CS* out = reinterpret_cast<CS*>(space + (static_cast<size_t>(z) * NY + r0 + rl) * NX * (R2C ? 1 : 2));
 #pragma unroll
-      for (int k2 = 0; k2 < Bx; ++k2) out[k1 + Ax * k2] = v[k2];
+      for (int k2 = 0; k2 < Bx; ++k2) out[k1 + Ax * k2] = to_storage(v[k2], k);
     }
     __syncthreads();
   }
 }
 
-template <typename T, int NX, int NY, bool R2C>
-__global__ void __launch_bounds__(kPlaneThreads) plane_forward(const PlanView<T> p,
-                                                          const T* __restrict__ space, int rows) {
+template <typename S, typename A, int NX, int NY, bool R2C>
+__global__ void __launch_bounds__(kPlaneThreads) plane_forward(const PlanView<S> p,
+                                                               const S* __restrict__ space, int rows) {
+  using TT = Types<S, A>;
+  using CS = typename TT::CS;
+  using CA = typename TT::CA;
   using L = PlaneLayout<NX, NY, R2C>;
   constexpr int Ay = Shape<NY>::A, By = Shape<NY>::B;
-  constexpr int Ax = Shape<L::LX>::A, Bx = Shape<L::LX>::B;
+  constexpr int Ax = L::Ax, Bx = L::Bx;
+  __shared__ int sExp;
   const int z = blockIdx.x;
   const int nc = p.numColumns;
-  PlaneSmem<T, NX, NY, R2C> s(nc);
-  plane_load_tables<T, NX, NY, R2C>(p, s);
-  __syncthreads();
+  PlaneSmem<CA, NX, NY, R2C> s(nc);
+  plane_load_tables<S, A, NX, NY, R2C>(p, s);
 
-  const C<T>* twl = R2C ? s.twm : s.twx;
   // Row chunks of plane z are contiguous in the space buffer: stream chunk i+1 into the other
   // half of W while chunk i is transformed.
-  const C<T>* plane = reinterpret_cast<const C<T>*>(space + static_cast<size_t>(z) * NY * NX * (R2C ? 1 : 2));
+  const CS* plane = reinterpret_cast<const CS*>(space + static_cast<size_t>(z) * NY * NX * (R2C ? 1 : 2));
   const int nchunks = (NY + rows - 1) / rows;
   auto issue_chunk = [&](int chunk) {
     const int r0 = chunk * rows, nr = min(rows, NY - r0);
-    C<T>* dst = s.W + (chunk & 1) * rows * L::WP;
-    const C<T>* src = plane + static_cast<size_t>(r0) * L::LX;
+    CA* dst = s.W + (chunk & 1) * rows * L::WP;
+    const CS* src = plane + static_cast<size_t>(r0) * L::LX;
     for (int i = threadIdx.x; i < nr * L::LX; i += blockDim.x) {
       const int rl = i / L::LX, e = i - rl * L::LX;
-      cp_async_c<T>(dst + rl * L::WP + L::wpos(e), src + i);
+      cp_async_c(dst + rl * L::WP + L::wpos(e), src + i);
     }
     cp_async_commit();
   };
   issue_chunk(0);
+
+  // Block scale (double-float only): the largest exponent of the whole plane, read once up front
+  // while the first chunk is in flight (the plane then stays in L2 for the chunk loads).
+  int k = 0;
+  if (TT::kScaled) {
+    if (threadIdx.x == 0) sExp = 0;
+    __syncthreads();
+    int e = 0;
+    for (int i = threadIdx.x; i < NY * L::LX; i += blockDim.x) e = max(e, max_exponent(plane[i]));
+    atomicMax(&sExp, e);
+  }
+  __syncthreads();
+  if (TT::kScaled) k = block_scale(sExp);
+
+  const CA* twl = R2C ? s.twm : s.twx;
   for (int chunk = 0; chunk < nchunks; ++chunk) {
     const int r0 = chunk * rows, nr = min(rows, NY - r0);
-    C<T>* wbase = s.W + (chunk & 1) * rows * L::WP;
+    CA* wbase = s.W + (chunk & 1) * rows * L::WP;
     if (chunk + 1 < nchunks) {
       issue_chunk(chunk + 1);
       cp_async_wait<1>();
@@ -368,11 +487,13 @@ __global__ void __launch_bounds__(kPlaneThreads) plane_forward(const PlanView<T>
     __syncthreads();
     for (int i = threadIdx.x; i < nr * Bx; i += blockDim.x) {
       const int rl = i / Bx, b = i - rl * Bx;
-      // padded row: element a*Bx + b sits at a*(Bx + PAD) + b
-      C<T>* wrow = wbase + rl * L::WP;
-      C<T> v[Ax];
+      // padded row: element a*Bx + b sits at a*(Bx + PAD) + b (raw storage values until here)
+      CA* wrow = wbase + rl * L::WP;
+      CA v[Ax];
 #pragma unroll
-      for (int a = 0; a < Ax; ++a) v[a] = wrow[a * (Bx + L::PAD) + b];
+      for (int a = 0; a < Ax; ++a) {
+        v[a] = to_arith(reinterpret_cast<const CS*>(wrow)[a * (Bx + L::PAD) + b], k);
+      }
       fft_pass1_regs<L::LX, -1>(v, b, twl);
 #pragma unroll
       for (int k1 = 0; k1 < Ax; ++k1) wrow[k1 * (Bx + L::PAD) + b] = v[k1];
@@ -380,11 +501,11 @@ __global__ void __launch_bounds__(kPlaneThreads) plane_forward(const PlanView<T>
     __syncthreads();
     for (int i = threadIdx.x; i < nr * Ax; i += blockDim.x) {
       const int rl = i / Ax, k1 = i - rl * Ax;
-      C<T> v[Bx];
-      C<T>* wrow = wbase + rl * L::WP + k1 * L::PAD;
+      CA v[Bx];
+      CA* wrow = wbase + rl * L::WP + k1 * L::PAD;
       fft_pass2<L::LX, -1>(wrow, 1, k1, v);
       if (!R2C) {
-        C<T>* prow = s.P + (r0 + rl) * nc;
+        CA* prow = s.P + (r0 + rl) * nc;
 #pragma unroll
         for (int k2 = 0; k2 < Bx; ++k2) {
           const int col = s.colOf[k1 + Ax * k2];
@@ -398,15 +519,16 @@ __global__ void __launch_bounds__(kPlaneThreads) plane_forward(const PlanView<T>
     __syncthreads();
     if (R2C) {
       // X[k] = (Z[k] + conj Z[M-k]) / 2 - i/2 e^{-2 pi i k/N} (Z[k] - conj Z[M-k]), Z[M] = Z[0]
+      const A half = A(0.5);
       for (int i = threadIdx.x; i < nr * nc; i += blockDim.x) {
         const int rl = i / nc, c = i - rl * nc;
-        const int k = p.columnX[c];
-        const C<T>* wrow = wbase + rl * L::WP;
-        const C<T> zk = wrow[L::wpos(transposed_pos<L::LX>(k % L::M))];
-        const C<T> zm = wrow[L::wpos(transposed_pos<L::LX>((L::M - k) % L::M))];
-        const C<T> dif = make_c(zk.x - zm.x, zk.y + zm.y);
-        const C<T> u = cmul(dif, s.twx[k]);
-        s.P[(r0 + rl) * nc + c] = make_c(T(0.5) * (zk.x + zm.x + u.y), T(0.5) * (zk.y - zm.y - u.x));
+        const int kk = p.columnX[c];
+        const CA* wrow = wbase + rl * L::WP;
+        const CA zk = wrow[L::wpos(transposed_pos<L::LX>(kk % L::M))];
+        const CA zm = wrow[L::wpos(transposed_pos<L::LX>((L::M - kk) % L::M))];
+        const CA dif = make_c(zk.x - zm.x, zk.y + zm.y);
+        const CA u = cmul(dif, s.twx[kk]);
+        s.P[(r0 + rl) * nc + c] = make_c(half * (zk.x + zm.x + u.y), half * (zk.y - zm.y - u.x));
       }
       __syncthreads();
     }
@@ -419,58 +541,73 @@ __global__ void __launch_bounds__(kPlaneThreads) plane_forward(const PlanView<T>
   __syncthreads();
   for (int i = threadIdx.x; i < nc * Ay; i += blockDim.x) {
     const int k1 = i / nc, c = i - k1 * nc;
-    C<T> v[By];
+    CA v[By];
     fft_pass2<NY, -1>(s.P + c, nc, k1, v);
 #pragma unroll
     for (int k2 = 0; k2 < By; ++k2) s.P[(k1 * By + k2) * nc + c] = v[k2];
   }
   __syncthreads();
-  C<T>* sticks = reinterpret_cast<C<T>*>(p.sticks) + static_cast<size_t>(z) * p.numSticks;
+  CS* sticks = reinterpret_cast<CS*>(p.sticks) + static_cast<size_t>(z) * p.numSticks;
   for (int st = threadIdx.x; st < p.numSticks; st += blockDim.x) {
-    sticks[st] = s.P[transposed_pos<NY>(p.stickY[st]) * nc + p.stickColumn[st]];
+    sticks[st] = to_storage(s.P[transposed_pos<NY>(p.stickY[st]) * nc + p.stickColumn[st]], k);
   }
 }
 
 // ================================================================================================
-// host-side launchers (instantiated per size in kernels_fast_*.cu)
+// host-side launchers (instantiated per size in kernels_fast_group_*.cu)
 // ================================================================================================
-template <typename T, int NZ>
+template <typename S, typename A, int NZ>
 struct ZKernels {
-  static size_t smem(int spb) { return (NZ + static_cast<size_t>(spb) * ZLayout<NZ>::pitch) * sizeof(C<T>); }
+  using CA = typename Types<S, A>::CA;
+  static size_t smem(int spb) { return (NZ + static_cast<size_t>(spb) * ZLayout<NZ>::pitch) * sizeof(CA); }
   static cudaError_t prepare(size_t maxSmem) {
-    cudaError_t e1 = cudaFuncSetAttribute(z_backward<T, NZ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaError_t e1 = cudaFuncSetAttribute(z_backward<S, A, NZ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           static_cast<int>(maxSmem));
-    cudaError_t e2 = cudaFuncSetAttribute(z_forward<T, NZ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaError_t e2 = cudaFuncSetAttribute(z_forward<S, A, NZ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           static_cast<int>(maxSmem));
     return e1 != cudaSuccess ? e1 : e2;
   }
-  static void backward(const PlanView<T>& p, int spb, const T* values, cudaStream_t st) {
+  static void backward(const PlanView<S>& p, int spb, const S* values, cudaStream_t st) {
     const int g = (p.numSticks + spb - 1) / spb;
-    z_backward<T, NZ><<<g, kThreads, smem(spb), st>>>(p, values, spb);
+    z_backward<S, A, NZ><<<g, kThreads, smem(spb), st>>>(p, values, spb);
   }
-  static void forward(const PlanView<T>& p, int spb, T* values, T scale, cudaStream_t st) {
+  static void forward(const PlanView<S>& p, int spb, S* values, S scale, cudaStream_t st) {
     const int g = (p.numSticks + spb - 1) / spb;
-    z_forward<T, NZ><<<g, kThreads, smem(spb), st>>>(p, values, scale, spb);
+    z_forward<S, A, NZ><<<g, kThreads, smem(spb), st>>>(p, values, scale, spb);
   }
 };
 
-template <typename T, int NX, int NY, bool R2C>
+template <typename S, typename A, int NX, int NY, bool R2C>
 struct PlaneKernels {
   using L = PlaneLayout<NX, NY, R2C>;
-  static size_t smem(int numColumns, int rows) { return L::template bytes<T>(numColumns, rows); }
+  using CA = typename Types<S, A>::CA;
+  static size_t smem(int numColumns, int rows) { return L::template bytes<CA>(numColumns, rows); }
   static cudaError_t prepare(size_t maxSmem) {
-    cudaError_t e1 = cudaFuncSetAttribute(plane_backward<T, NX, NY, R2C>,
+    cudaError_t e1 = cudaFuncSetAttribute(plane_backward<S, A, NX, NY, R2C>,
                                           cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(maxSmem));
-    cudaError_t e2 = cudaFuncSetAttribute(plane_forward<T, NX, NY, R2C>,
+    cudaError_t e2 = cudaFuncSetAttribute(plane_forward<S, A, NX, NY, R2C>,
                                           cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(maxSmem));
     return e1 != cudaSuccess ? e1 : e2;
   }
-  static void backward(const PlanView<T>& p, int rows, T* space, cudaStream_t st) {
-    plane_backward<T, NX, NY, R2C><<<p.dimZ, kPlaneThreads, smem(p.numColumns, rows), st>>>(p, space, rows);
+  static void backward(const PlanView<S>& p, int rows, S* space, cudaStream_t st) {
+    plane_backward<S, A, NX, NY, R2C><<<p.dimZ, kPlaneThreads, smem(p.numColumns, rows), st>>>(p, space, rows);
   }
-  static void forward(const PlanView<T>& p, int rows, const T* space, cudaStream_t st) {
-    plane_forward<T, NX, NY, R2C><<<p.dimZ, kPlaneThreads, smem(p.numColumns, rows), st>>>(p, space, rows);
+  static void forward(const PlanView<S>& p, int rows, const S* space, cudaStream_t st) {
+    plane_forward<S, A, NX, NY, R2C><<<p.dimZ, kPlaneThreads, smem(p.numColumns, rows), st>>>(p, space, rows);
   }
+};
+
+// Arithmetic type of the specialised kernels for a storage type: float for FP32, double-float
+// for FP64.
+template <typename S>
+struct FastArith;
+template <>
+struct FastArith<float> {
+  using type = float;
+};
+template <>
+struct FastArith<double> {
+  using type = dd;
 };
 
 }  // namespace fast

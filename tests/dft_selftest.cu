@@ -6,6 +6,7 @@
 #include <cstdio>
 #include <vector>
 
+#include "dd.cuh"
 #include "dft.cuh"
 #include "fft_plan.hpp"
 
@@ -91,7 +92,45 @@ static bool check_two_pass() {
   return true;
 }
 
+// Double-float arithmetic: the same register DFTs and two-pass shapes in dd, against the same
+// long-double reference, at a bound set by the ~48-bit dd mantissa.
+template <int N, int SIGN>
+static bool check_two_pass_dd() {
+  constexpr int A = Shape<N>::A, B = Shape<N>::B;
+  std::vector<double> twd = make_twiddles(N);
+  std::vector<ddc> tw(N), buf(N);
+  for (int i = 0; i < N; ++i) tw[i] = make_c(to_dd(twd[2 * i]), to_dd(twd[2 * i + 1]));
+  std::vector<cd> x(N);
+  for (int i = 0; i < N; ++i) {
+    x[i] = cd(std::sin(0.5 + 1.3 * i), std::cos(2.0 - 0.7 * i));
+    buf[i] = make_c(to_dd((double)x[i].real()), to_dd((double)x[i].imag()));
+  }
+  for (int b = 0; b < B; ++b) fft_pass1<N, SIGN>(buf.data(), 1, b, tw.data());
+  std::vector<ddc> out(N);
+  for (int k1 = 0; k1 < A; ++k1) {
+    ddc v[B];
+    fft_pass2<N, SIGN>(buf.data(), 1, k1, v);
+    for (int k2 = 0; k2 < B; ++k2) out[k1 + A * k2] = v[k2];
+  }
+  auto y = direct(x, SIGN);
+  long double num = 0, den = 0;
+  for (int i = 0; i < N; ++i) {
+    const long double er = (long double)to_double(out[i].x) - y[i].real();
+    const long double ei = (long double)to_double(out[i].y) - y[i].imag();
+    num += er * er + ei * ei;
+    den += std::norm(y[i]);
+  }
+  const double rel = std::sqrt((double)(num / den));
+  if (rel > 2e-14) {
+    std::printf("dd two-pass FFT %d sign %d: rel-L2 error %g\n", N, SIGN, rel);
+    return false;
+  }
+  ++checks;
+  return true;
+}
+
 #define REG(R) (check_register<R, -1>() && check_register<R, 1>())
+#define DD(N) (check_two_pass_dd<N, -1>() && check_two_pass_dd<N, 1>())
 #define TWO(N) (check_two_pass<N, -1>() && check_two_pass<N, 1>())
 
 int main() {
@@ -103,6 +142,9 @@ int main() {
        TWO(72) && TWO(75) && TWO(80) && TWO(90) && TWO(96) && TWO(100) && TWO(108) && TWO(120) &&
        TWO(128) && TWO(144) && TWO(150) && TWO(160) && TWO(180) && TWO(192) && TWO(240) &&
        TWO(256);
+  ok = ok && DD(12) && DD(48) && DD(60) && DD(64) && DD(72) && DD(90) && DD(96) && DD(100) &&
+       DD(108) && DD(120) && DD(128) && DD(150) && DD(160) && DD(192) && DD(24) && DD(30) &&
+       DD(36) && DD(45) && DD(50) && DD(54) && DD(75) && DD(80) && DD(6);
   if (!ok) return 1;
   std::printf("ok %d\n", checks);
   return 0;
