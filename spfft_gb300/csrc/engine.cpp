@@ -46,7 +46,10 @@ bool prepare_fast_once(int device, int n) {
   if (std::find(done.begin(), done.end(), std::make_pair(device, n)) != done.end()) return true;
   FastArgs<T> a;
   a.maxSmem = static_cast<size_t>(max_smem_optin(device));
-  if (!fast_dispatch<T>(FastOp::Prepare, n, false, a)) return false;
+  if (!fast_dispatch<T>(FastOp::Prepare, n, false, a)) {
+    (void)cudaGetLastError();
+    return false;
+  }
   done.emplace_back(device, n);
   return true;
 }
@@ -151,9 +154,10 @@ GpuPlan<T>::GpuPlan(const IndexPlan& p, int device) {
   base_.numColumns = ncol;
   base_.r2c = p.type == SPFFT_TRANS_R2C ? 1 : 0;
   base_.zeroZeroStick = (base_.r2c && p.zeroZeroStick < ns) ? p.zeroZeroStick : -1;
-  // Size-specialised kernels where the lengths are supported and shared memory allows.
+  // Size-specialised kernels where the lengths are supported and shared memory allows (keeping
+  // 1 KB of the opt-in maximum for the kernels' static shared memory).
   {
-    const size_t optin = static_cast<size_t>(max_smem_optin(device));
+    const size_t optin = static_cast<size_t>(max_smem_optin(device)) - 1024;
     FastArgs<T> a;
     const int nz = p.dimZ;
     if (ns > 0 && fast_dispatch<T>(FastOp::Has, nz, false, a) && prepare_fast_once<T>(device, nz)) {

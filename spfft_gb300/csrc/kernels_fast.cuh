@@ -556,15 +556,23 @@ __global__ void __launch_bounds__(kPlaneThreads) plane_forward(const PlanView<S>
 // ================================================================================================
 // host-side launchers (instantiated per size in kernels_fast_group_*.cu)
 // ================================================================================================
+// Raise a kernel's dynamic shared memory limit to what is left of the opt-in maximum after its
+// static shared memory.
+template <typename K>
+cudaError_t allow_dynamic_smem(K kernel, size_t maxSmem) {
+  cudaFuncAttributes attr{};
+  cudaError_t e = cudaFuncGetAttributes(&attr, kernel);
+  if (e != cudaSuccess) return e;
+  const size_t avail = maxSmem > attr.sharedSizeBytes ? maxSmem - attr.sharedSizeBytes : 0;
+  return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(avail));
+}
 template <typename S, typename A, int NZ>
 struct ZKernels {
   using CA = typename Types<S, A>::CA;
   static size_t smem(int spb) { return (NZ + static_cast<size_t>(spb) * ZLayout<NZ>::pitch) * sizeof(CA); }
   static cudaError_t prepare(size_t maxSmem) {
-    cudaError_t e1 = cudaFuncSetAttribute(z_backward<S, A, NZ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          static_cast<int>(maxSmem));
-    cudaError_t e2 = cudaFuncSetAttribute(z_forward<S, A, NZ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          static_cast<int>(maxSmem));
+    cudaError_t e1 = allow_dynamic_smem(z_backward<S, A, NZ>, maxSmem);
+    cudaError_t e2 = allow_dynamic_smem(z_forward<S, A, NZ>, maxSmem);
     return e1 != cudaSuccess ? e1 : e2;
   }
   static void backward(const PlanView<S>& p, int spb, const S* values, cudaStream_t st) {
@@ -583,10 +591,8 @@ struct PlaneKernels {
   using CA = typename Types<S, A>::CA;
   static size_t smem(int numColumns, int rows) { return L::template bytes<CA>(numColumns, rows); }
   static cudaError_t prepare(size_t maxSmem) {
-    cudaError_t e1 = cudaFuncSetAttribute(plane_backward<S, A, NX, NY, R2C>,
-                                          cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(maxSmem));
-    cudaError_t e2 = cudaFuncSetAttribute(plane_forward<S, A, NX, NY, R2C>,
-                                          cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(maxSmem));
+    cudaError_t e1 = allow_dynamic_smem(plane_backward<S, A, NX, NY, R2C>, maxSmem);
+    cudaError_t e2 = allow_dynamic_smem(plane_forward<S, A, NX, NY, R2C>, maxSmem);
     return e1 != cudaSuccess ? e1 : e2;
   }
   static void backward(const PlanView<S>& p, int rows, S* space, cudaStream_t st) {

@@ -258,14 +258,15 @@ def test_kernel_paths_and_fallbacks(lib):
     non-cubic sizes, planes too large for shared memory, an R2C space buffer aligned to 8 bytes
     only) fall back to the generic kernels with the same results."""
     rng = np.random.default_rng(31)
-    # fast paths
-    for dims, ttype in [((64, 64, 64), 0), ((192, 192, 192), 1), ((12, 12, 12), 1), ((100, 100, 13), 0)]:
-        idx = sphere_indices(dims[0], dims[0] // 4, r2c=(ttype == 1)) if dims[2] == dims[0] else \
-            random_indices(rng, *dims, r2c=(ttype == 1))
-        tr = _transform("float64", ttype, dims, idx)
-        info = tr.path_info()
-        assert info["fused_plane"] == (dims[0] == dims[1]), (dims, info)
-        assert info["fast_z"] == (dims[2] in (12, 64, 100, 192)), (dims, info)
+    # fast paths (both precisions: a kernel that cannot be prepared silently loses its fast path)
+    for dtype in ("float64", "float32"):
+        for dims, ttype in [((64, 64, 64), 0), ((192, 192, 192), 1), ((12, 12, 12), 1), ((100, 100, 13), 0)]:
+            idx = sphere_indices(dims[0], dims[0] // 4, r2c=(ttype == 1)) if dims[2] == dims[0] else \
+                random_indices(rng, *dims, r2c=(ttype == 1))
+            tr = _transform(dtype, ttype, dims, idx)
+            info = tr.path_info()
+            assert info["fused_plane"] == (dims[0] == dims[1]), (dtype, dims, info)
+            assert info["fast_z"] == (dims[2] in (12, 64, 100, 192)), (dtype, dims, info)
     # 192^3 C2C |k| <= 48 FP64: 97 columns do not fit one block's shared memory -> generic planes
     idx = sphere_indices(192, 48)
     tr = _transform("float64", 0, (192, 192, 192), idx)
