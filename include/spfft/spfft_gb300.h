@@ -66,8 +66,10 @@ SPFFT_EXPORT SpfftError spfft_gb300_float_transform_stage_times(SpfftFloatTransf
                                                                 void* stream, float* stageMs);
 
 /* Which kernels a transform runs (no counterpart in the reference): bit 0 set = size-specialised
- * z pass, bit 1 set = fused size-specialised plane pass (y and x in one kernel); otherwise the
- * generic kernels. */
+ * z pass; bit 1 set = fused size-specialised plane pass (y and x in one kernel per plane); bit 2
+ * set = split size-specialised y and x passes over column and row groups; otherwise the generic
+ * kernels. The plane strategy can be forced at transform creation with the environment variable
+ * SPFFT_GB300_PLANE=fused|split|generic. */
 SPFFT_EXPORT SpfftError spfft_gb300_transform_path_info(SpfftTransform transform, int* flags);
 SPFFT_EXPORT SpfftError spfft_gb300_float_transform_path_info(SpfftFloatTransform transform,
                                                               int* flags);

@@ -339,10 +339,12 @@ class Transform:
 
     # ---- extensions ----------------------------------------------------------------------------
     def path_info(self) -> dict:
-        """Which kernels run: size-specialised z pass, fused plane pass (else the generic ones)."""
+        """Which kernels run: size-specialised z pass; fused plane pass or split specialised y and x
+        passes (else the generic ones)."""
         v = ctypes.c_int(0)
         _call("spfft_gb300_" + self._p[len("spfft_"):] + "transform_path_info", self._h, ctypes.byref(v))
-        return {"fast_z": bool(v.value & 1), "fused_plane": bool(v.value & 2)}
+        return {"fast_z": bool(v.value & 1), "fused_plane": bool(v.value & 2),
+                "split_plane": bool(v.value & 4)}
 
     def set_stream(self, stream: Any) -> None:
         """Run every later call on this CUDA stream (torch.cuda.Stream, cudaStream_t int or None)."""

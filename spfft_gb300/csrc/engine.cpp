@@ -3,7 +3,9 @@
 #include "engine.hpp"
 
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
+#include <string>
 #include <mutex>
 #include <vector>
 
@@ -179,6 +181,10 @@ GpuPlan<T>::GpuPlan(const IndexPlan& p, int device) {
       }
     }
     const bool r2c = p.type == SPFFT_TRANS_R2C;
+    // Candidate plane strategies. SPFFT_GB300_PLANE=fused|split|generic forces one (when it is
+    // available for this shape); otherwise split is preferred, then fused, then generic.
+    bool fusedOk = false, splitOk = false;
+    int fusedRows = 0, cpb = 0, rpb = 0;
     if (ns > 0 && p.dimX == p.dimY && fast_dispatch<T>(FastOp::Has, p.dimX, r2c, a) &&
         prepare_fast_once<T>(device, p.dimX)) {
       size_t sm = 0;
@@ -189,12 +195,56 @@ GpuPlan<T>::GpuPlan(const IndexPlan& p, int device) {
         a.param = rows;
         fast_dispatch<T>(FastOp::PlaneSmem, p.dimX, r2c, a);
         if (sm <= optin) {
-          fastPlane_ = true;
-          fastRows_ = rows;
+          fusedOk = true;
+          fusedRows = rows;
           break;
         }
       }
     }
+    if (ns > 0 && fast_dispatch<T>(FastOp::Has, p.dimX, r2c, a) &&
+        fast_dispatch<T>(FastOp::Has, p.dimY, r2c, a) && prepare_fast_once<T>(device, p.dimX) &&
+        prepare_fast_once<T>(device, p.dimY)) {
+      size_t sm = 0;
+      a.smemOut = &sm;
+      a.numColumns = ncol;
+      // Columns per y block and rows per x block: 16 and 32 (>= 256 work items per pass for the
+      // usual lengths) while a block stays within 100 KB, smaller otherwise.
+      const size_t budget = 100 * 1024;
+      for (cpb = 16; cpb > 1; cpb /= 2) {
+        a.param = cpb;
+        fast_dispatch<T>(FastOp::YSmem, p.dimY, r2c, a);
+        if (sm <= budget) break;
+      }
+      a.param = cpb;
+      fast_dispatch<T>(FastOp::YSmem, p.dimY, r2c, a);
+      const bool yFits = sm <= optin;
+      for (rpb = 32; rpb > 1; rpb /= 2) {
+        a.param = rpb;
+        fast_dispatch<T>(FastOp::XSmem, p.dimX, r2c, a);
+        if (sm <= budget) break;
+      }
+      a.param = rpb;
+      fast_dispatch<T>(FastOp::XSmem, p.dimX, r2c, a);
+      splitOk = yFits && sm <= optin;
+      cpb = std::min(cpb, std::max(1, ncol));
+      rpb = std::min(rpb, p.dimY);
+    }
+    const char* force = std::getenv("SPFFT_GB300_PLANE");
+    const std::string want = force ? force : "";
+    if (want == "generic") {
+      planePath_ = PlanePath::Generic;
+    } else if (want == "fused" && fusedOk) {
+      planePath_ = PlanePath::Fused;
+    } else if (want == "split" && splitOk) {
+      planePath_ = PlanePath::Split;
+    } else if (splitOk) {
+      planePath_ = PlanePath::Split;
+    } else if (fusedOk) {
+      planePath_ = PlanePath::Fused;
+    }
+    fastRows_ = fusedRows;
+    splitCpb_ = cpb;
+    splitRpb_ = rpb;
   }
 
   base_.fz = make_radix_plan(p.dimZ);
@@ -263,12 +313,21 @@ void GpuPlan<T>::backward(const T* values, T* space, void* scratch, cudaStream_t
   }
   check_launch(cudaGetLastError());
   mark(events, 1, stream);
-  if (fastPlane_ && aligned) {
+  if (planePath_ == PlanePath::Fused && aligned) {
     a.param = fastRows_;
     a.out = space;
     fast_dispatch<T>(FastOp::PlaneBackward, base_.dimX, base_.r2c != 0, a);
     check_launch(cudaGetLastError());
     mark(events, 2, stream);
+  } else if (planePath_ == PlanePath::Split && aligned) {
+    a.param = splitCpb_;
+    fast_dispatch<T>(FastOp::YBackward, base_.dimY, base_.r2c != 0, a);
+    check_launch(cudaGetLastError());
+    mark(events, 2, stream);
+    a.param = splitRpb_;
+    a.out = space;
+    fast_dispatch<T>(FastOp::XBackward, base_.dimX, base_.r2c != 0, a);
+    check_launch(cudaGetLastError());
   } else {
     check_launch(launch_generic<T>(GenericPass::YBackward, v, config_, nullptr, nullptr, T(0), stream));
     mark(events, 2, stream);
@@ -287,12 +346,21 @@ void GpuPlan<T>::forward(const T* space, T* values, bool scaled, void* scratch,
   a.plan = &v;
   a.stream = stream;
   mark(events, 0, stream);
-  if (fastPlane_ && aligned) {
+  if (planePath_ == PlanePath::Fused && aligned) {
     a.param = fastRows_;
     a.in = space;
     fast_dispatch<T>(FastOp::PlaneForward, base_.dimX, base_.r2c != 0, a);
     check_launch(cudaGetLastError());
     mark(events, 1, stream);
+  } else if (planePath_ == PlanePath::Split && aligned) {
+    a.param = splitRpb_;
+    a.in = space;
+    fast_dispatch<T>(FastOp::XForward, base_.dimX, base_.r2c != 0, a);
+    check_launch(cudaGetLastError());
+    mark(events, 1, stream);
+    a.param = splitCpb_;
+    fast_dispatch<T>(FastOp::YForward, base_.dimY, base_.r2c != 0, a);
+    check_launch(cudaGetLastError());
   } else {
     check_launch(launch_generic<T>(GenericPass::XForward, v, config_, space, nullptr, T(0), stream));
     mark(events, 1, stream);

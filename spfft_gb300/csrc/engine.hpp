@@ -34,8 +34,14 @@ public:
   void forward(const T* space, T* values, bool scaled, void* scratch, cudaStream_t stream,
                const StageEvents* events = nullptr) const;
 
-  // Which kernels run: bit 0 = size-specialised z pass, bit 1 = fused size-specialised plane pass.
-  int path_flags() const { return (fastZ_ ? 1 : 0) | (fastPlane_ ? 2 : 0); }
+  // How the y and x passes run: generic kernels, one fused specialised kernel per plane, or
+  // specialised y and x kernels over column / row groups with the compact plane in HBM.
+  enum class PlanePath { Generic, Fused, Split };
+  // Which kernels run: bit 0 = size-specialised z pass, bit 1 = fused plane pass, bit 2 = split
+  // specialised y and x passes.
+  int path_flags() const {
+    return (fastZ_ ? 1 : 0) | (planePath_ == PlanePath::Fused ? 2 : 0) | (planePath_ == PlanePath::Split ? 4 : 0);
+  }
 
   // Device pointer of the value staging area inside `scratch` (host input / output path).
   T* staging(void* scratch) const {
@@ -49,8 +55,9 @@ private:
 
   PlanView<T> base_{};
   LaunchConfig config_{};
-  bool fastZ_ = false, fastPlane_ = false;
-  int fastSpb_ = 0, fastRows_ = 0;
+  bool fastZ_ = false;
+  PlanePath planePath_ = PlanePath::Generic;
+  int fastSpb_ = 0, fastRows_ = 0, splitCpb_ = 0, splitRpb_ = 0;
   ScratchLayout layout_{};
   T scale_ = T(1);
   DeviceBuffer tables_;

@@ -603,6 +603,317 @@ struct PlaneKernels {
   }
 };
 
+// ================================================================================================
+// split plane passes: y kernel over column groups, x kernel over row groups, with the compact
+// plane [z][y][numColumns] in HBM between them. More traffic than the fused plane kernel but many
+// small blocks instead of one large block per plane, so every SM stays busy.
+// ================================================================================================
+// y backward: block (column group, z)
+template <typename S, typename A, int NY>
+__global__ void __launch_bounds__(kThreads) y_backward_split(const PlanView<S> p, int cpb) {
+  using TT = Types<S, A>;
+  using CS = typename TT::CS;
+  using CA = typename TT::CA;
+  constexpr int Ay = Shape<NY>::A, By = Shape<NY>::B;
+  __shared__ int sExp;
+  CA* tw = reinterpret_cast<CA*>(g_fast_smem);
+  CA* buf = tw + NY;
+  const int nc = p.numColumns;
+  const int c0 = blockIdx.x * cpb, ncb = min(cpb, nc - c0);
+  const int z = blockIdx.y;
+  load_twiddles<S, A>(tw, p.twy, NY);
+  for (int i = threadIdx.x; i < NY * ncb; i += blockDim.x) buf[i] = czero<A>();
+  __syncthreads();
+  const CS* sticks = reinterpret_cast<const CS*>(p.sticks) + static_cast<size_t>(z) * p.numSticks;
+  const int sBegin = p.columnStickStart[c0], sEnd = p.columnStickStart[c0 + ncb];
+  for (int st = sBegin + threadIdx.x; st < sEnd; st += blockDim.x) {
+    cp_async_c(buf + p.stickY[st] * ncb + (p.stickColumn[st] - c0), sticks + st);
+  }
+  cp_async_commit();
+  cp_async_wait<0>();
+  __syncthreads();
+  const int k = convert_block<S, A>(buf, NY * ncb, &sExp);
+  if (p.r2c && c0 == 0 && p.columnX[0] == 0) line_fill(buf, NY, ncb);
+  for (int i = threadIdx.x; i < ncb * By; i += blockDim.x) {
+    const int b = i / ncb, c = i - b * ncb;
+    fft_pass1<NY, +1>(buf + c, ncb, b, tw);
+  }
+  __syncthreads();
+  CS* planes = reinterpret_cast<CS*>(p.planes) + static_cast<size_t>(z) * NY * nc + c0;
+  for (int i = threadIdx.x; i < ncb * Ay; i += blockDim.x) {
+    const int k1 = i / ncb, c = i - k1 * ncb;
+    CA v[By];
+    fft_pass2<NY, +1>(buf + c, ncb, k1, v);
+#pragma unroll
+    for (int k2 = 0; k2 < By; ++k2) planes[static_cast<size_t>(k1 + Ay * k2) * nc + c] = to_storage(v[k2], k);
+  }
+}
+
+// y forward: block (column group, z)
+template <typename S, typename A, int NY>
+__global__ void __launch_bounds__(kThreads) y_forward_split(const PlanView<S> p, int cpb) {
+  using TT = Types<S, A>;
+  using CS = typename TT::CS;
+  using CA = typename TT::CA;
+  constexpr int Ay = Shape<NY>::A, By = Shape<NY>::B;
+  __shared__ int sExp;
+  CA* tw = reinterpret_cast<CA*>(g_fast_smem);
+  CA* buf = tw + NY;
+  const int nc = p.numColumns;
+  const int c0 = blockIdx.x * cpb, ncb = min(cpb, nc - c0);
+  const int z = blockIdx.y;
+  load_twiddles<S, A>(tw, p.twy, NY);
+  const CS* planes = reinterpret_cast<const CS*>(p.planes) + static_cast<size_t>(z) * NY * nc + c0;
+  for (int i = threadIdx.x; i < NY * ncb; i += blockDim.x) {
+    const int y = i / ncb, c = i - y * ncb;
+    cp_async_c(buf + i, planes + static_cast<size_t>(y) * nc + c);
+  }
+  cp_async_commit();
+  cp_async_wait<0>();
+  __syncthreads();
+  const int k = convert_block<S, A>(buf, NY * ncb, &sExp);
+  for (int i = threadIdx.x; i < ncb * By; i += blockDim.x) {
+    const int b = i / ncb, c = i - b * ncb;
+    fft_pass1<NY, -1>(buf + c, ncb, b, tw);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < ncb * Ay; i += blockDim.x) {
+    const int k1 = i / ncb, c = i - k1 * ncb;
+    CA v[By];
+    fft_pass2<NY, -1>(buf + c, ncb, k1, v);
+#pragma unroll
+    for (int k2 = 0; k2 < By; ++k2) buf[(k1 * By + k2) * ncb + c] = v[k2];
+  }
+  __syncthreads();
+  CS* sticks = reinterpret_cast<CS*>(p.sticks) + static_cast<size_t>(z) * p.numSticks;
+  const int sBegin = p.columnStickStart[c0], sEnd = p.columnStickStart[c0 + ncb];
+  for (int st = sBegin + threadIdx.x; st < sEnd; st += blockDim.x) {
+    sticks[st] = to_storage(buf[transposed_pos<NY>(p.stickY[st]) * ncb + (p.stickColumn[st] - c0)], k);
+  }
+}
+
+// Shared memory of the x kernels: twx[NX] | (R2C) twm[M] | colOf[NXF] | P[rows][numColumns] |
+// W[rows][WP].
+template <typename CA, int NX, bool R2C>
+struct RowSmem {
+  using L = PlaneLayout<NX, 2, R2C>;
+  CA* twx;
+  CA* twm;
+  int* colOf;
+  CA* P;
+  CA* W;
+  __device__ __forceinline__ RowSmem(int numColumns, int rows) {
+    const size_t c = sizeof(CA);
+    twx = reinterpret_cast<CA*>(g_fast_smem);
+    twm = twx + NX;
+    colOf = reinterpret_cast<int*>(twm + (R2C ? L::M : 0));
+    P = reinterpret_cast<CA*>(reinterpret_cast<unsigned char*>(colOf) + ((L::NXF * sizeof(int) + c - 1) / c) * c);
+    W = P + rows * numColumns;
+  }
+  template <typename CAT>
+  static size_t bytes(int numColumns, int rows) {
+    const size_t c = sizeof(CAT);
+    return (NX + (R2C ? L::M : 0)) * c + ((L::NXF * sizeof(int) + c - 1) / c) * c +
+           static_cast<size_t>(rows) * numColumns * c + static_cast<size_t>(rows) * L::WP * c;
+  }
+};
+
+template <typename S, typename A, int NX, bool R2C>
+__device__ __forceinline__ void row_load_tables(const PlanView<S>& p, RowSmem<typename Types<S, A>::CA, NX, R2C>& s) {
+  using L = PlaneLayout<NX, 2, R2C>;
+  using CS = typename Types<S, A>::CS;
+  load_twiddles<S, A>(s.twx, p.twx, NX);
+  if (R2C) {
+    const CS* tx = reinterpret_cast<const CS*>(p.twx);
+    for (int i = threadIdx.x; i < L::M; i += blockDim.x) s.twm[i] = tw_arith(tx[2 * i]);
+  }
+  for (int i = threadIdx.x; i < L::NXF; i += blockDim.x) s.colOf[i] = -1;
+  __syncthreads();
+  for (int c = threadIdx.x; c < p.numColumns; c += blockDim.x) s.colOf[p.columnX[c]] = c;
+}
+
+// x backward: block (row group, z); compact rows from HBM -> x-FFT -> space rows
+template <typename S, typename A, int NX, bool R2C>
+__global__ void __launch_bounds__(kThreads) x_backward_split(const PlanView<S> p, S* __restrict__ space,
+                                                             int rpb) {
+  using TT = Types<S, A>;
+  using CS = typename TT::CS;
+  using CA = typename TT::CA;
+  using L = PlaneLayout<NX, 2, R2C>;
+  constexpr int Ax = L::Ax, Bx = L::Bx;
+  __shared__ int sExp;
+  const int nc = p.numColumns, ny = p.dimY;
+  const int y0 = blockIdx.x * rpb, nr = min(rpb, ny - y0);
+  const int z = blockIdx.y;
+  RowSmem<CA, NX, R2C> s(nc, rpb);
+  row_load_tables<S, A, NX, R2C>(p, s);
+  const CS* planes = reinterpret_cast<const CS*>(p.planes) + (static_cast<size_t>(z) * ny + y0) * nc;
+  for (int i = threadIdx.x; i < nr * nc; i += blockDim.x) cp_async_c(s.P + i, planes + i);
+  cp_async_commit();
+  cp_async_wait<0>();
+  __syncthreads();
+  const int k = convert_block<S, A>(s.P, nr * nc, &sExp);
+  const CA* twl = R2C ? s.twm : s.twx;
+  for (int i = threadIdx.x; i < nr * Bx; i += blockDim.x) {
+    const int rl = i / Bx, b = i - rl * Bx;
+    const CA* prow = s.P + rl * nc;
+    CA v[Ax];
+#pragma unroll
+    for (int a = 0; a < Ax; ++a) {
+      const int kk = a * Bx + b;
+      if (!R2C) {
+        const int col = s.colOf[kk];
+        v[a] = col >= 0 ? prow[col] : czero<A>();
+      } else {
+        const int ck = s.colOf[kk], cm = s.colOf[L::M - kk];
+        const CA xk = ck >= 0 ? prow[ck] : czero<A>();
+        const CA xm = cm >= 0 ? prow[cm] : czero<A>();
+        if (kk == 0) {
+          v[a] = make_c(xk.x + xm.x, xk.x - xm.x);
+        } else {
+          const CA sum = make_c(xk.x + xm.x, xk.y - xm.y);
+          const CA dif = make_c(xk.x - xm.x, xk.y + xm.y);
+          const CA u = cmulc(dif, s.twx[kk]);
+          v[a] = make_c(sum.x - u.y, sum.y + u.x);
+        }
+      }
+    }
+    fft_pass1_regs<L::LX, +1>(v, b, twl);
+    CA* wrow = s.W + rl * L::WP;
+#pragma unroll
+    for (int k1 = 0; k1 < Ax; ++k1) wrow[L::wpos(k1 * Bx + b)] = v[k1];
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < nr * Ax; i += blockDim.x) {
+    const int rl = i / Ax, k1 = i - rl * Ax;
+    CA v[Bx];
+    fft_pass2<L::LX, +1>(s.W + rl * L::WP + k1 * L::PAD, 1, k1, v);
+    CS* out = reinterpret_cast<CS*>(space + (static_cast<size_t>(z) * ny + y0 + rl) * NX * (R2C ? 1 : 2));
+#pragma unroll
+    for (int k2 = 0; k2 < Bx; ++k2) out[k1 + Ax * k2] = to_storage(v[k2], k);
+  }
+}
+
+// x forward: block (row group, z); space rows -> x-FFT -> compact rows to HBM
+template <typename S, typename A, int NX, bool R2C>
+__global__ void __launch_bounds__(kThreads) x_forward_split(const PlanView<S> p, const S* __restrict__ space,
+                                                            int rpb) {
+  using TT = Types<S, A>;
+  using CS = typename TT::CS;
+  using CA = typename TT::CA;
+  using L = PlaneLayout<NX, 2, R2C>;
+  constexpr int Ax = L::Ax, Bx = L::Bx;
+  __shared__ int sExp;
+  const int nc = p.numColumns, ny = p.dimY;
+  const int y0 = blockIdx.x * rpb, nr = min(rpb, ny - y0);
+  const int z = blockIdx.y;
+  RowSmem<CA, NX, R2C> s(nc, rpb);
+  row_load_tables<S, A, NX, R2C>(p, s);
+  const CS* rows = reinterpret_cast<const CS*>(space + (static_cast<size_t>(z) * ny + y0) * NX * (R2C ? 1 : 2));
+  for (int i = threadIdx.x; i < nr * L::LX; i += blockDim.x) {
+    const int rl = i / L::LX, e = i - rl * L::LX;
+    cp_async_c(s.W + rl * L::WP + L::wpos(e), rows + i);
+  }
+  cp_async_commit();
+  int k = 0;
+  if (TT::kScaled) {
+    if (threadIdx.x == 0) sExp = 0;
+    __syncthreads();
+    int e = 0;
+    for (int i = threadIdx.x; i < nr * L::LX; i += blockDim.x) e = max(e, max_exponent(rows[i]));
+    atomicMax(&sExp, e);
+  }
+  cp_async_wait<0>();
+  __syncthreads();
+  if (TT::kScaled) k = block_scale(sExp);
+  const CA* twl = R2C ? s.twm : s.twx;
+  for (int i = threadIdx.x; i < nr * Bx; i += blockDim.x) {
+    const int rl = i / Bx, b = i - rl * Bx;
+    CA* wrow = s.W + rl * L::WP;
+    CA v[Ax];
+#pragma unroll
+    for (int a = 0; a < Ax; ++a) v[a] = to_arith(reinterpret_cast<const CS*>(wrow)[a * (Bx + L::PAD) + b], k);
+    fft_pass1_regs<L::LX, -1>(v, b, twl);
+#pragma unroll
+    for (int k1 = 0; k1 < Ax; ++k1) wrow[k1 * (Bx + L::PAD) + b] = v[k1];
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < nr * Ax; i += blockDim.x) {
+    const int rl = i / Ax, k1 = i - rl * Ax;
+    CA v[Bx];
+    CA* wrow = s.W + rl * L::WP + k1 * L::PAD;
+    fft_pass2<L::LX, -1>(wrow, 1, k1, v);
+    if (!R2C) {
+      CA* prow = s.P + rl * nc;
+#pragma unroll
+      for (int k2 = 0; k2 < Bx; ++k2) {
+        const int col = s.colOf[k1 + Ax * k2];
+        if (col >= 0) prow[col] = v[k2];
+      }
+    } else {
+#pragma unroll
+      for (int k2 = 0; k2 < Bx; ++k2) wrow[k1 * Bx + k2] = v[k2];
+    }
+  }
+  __syncthreads();
+  if (R2C) {
+    const A half = A(0.5);
+    for (int i = threadIdx.x; i < nr * nc; i += blockDim.x) {
+      const int rl = i / nc, c = i - rl * nc;
+      const int kk = p.columnX[c];
+      const CA* wrow = s.W + rl * L::WP;
+      const CA zk = wrow[L::wpos(transposed_pos<L::LX>(kk % L::M))];
+      const CA zm = wrow[L::wpos(transposed_pos<L::LX>((L::M - kk) % L::M))];
+      const CA dif = make_c(zk.x - zm.x, zk.y + zm.y);
+      const CA u = cmul(dif, s.twx[kk]);
+      s.P[rl * nc + c] = make_c(half * (zk.x + zm.x + u.y), half * (zk.y - zm.y - u.x));
+    }
+    __syncthreads();
+  }
+  CS* planes = reinterpret_cast<CS*>(p.planes) + (static_cast<size_t>(z) * ny + y0) * nc;
+  for (int i = threadIdx.x; i < nr * nc; i += blockDim.x) planes[i] = to_storage(s.P[i], k);
+}
+
+template <typename S, typename A, int NY>
+struct YSplitKernels {
+  using CA = typename Types<S, A>::CA;
+  static size_t smem(int cpb) { return (NY + static_cast<size_t>(NY) * cpb) * sizeof(CA); }
+  static cudaError_t prepare(size_t maxSmem) {
+    cudaError_t e1 = allow_dynamic_smem(y_backward_split<S, A, NY>, maxSmem);
+    cudaError_t e2 = allow_dynamic_smem(y_forward_split<S, A, NY>, maxSmem);
+    return e1 != cudaSuccess ? e1 : e2;
+  }
+  static void backward(const PlanView<S>& p, int cpb, cudaStream_t st) {
+    const dim3 g((p.numColumns + cpb - 1) / cpb, p.dimZ);
+    y_backward_split<S, A, NY><<<g, kThreads, smem(cpb), st>>>(p, cpb);
+  }
+  static void forward(const PlanView<S>& p, int cpb, cudaStream_t st) {
+    const dim3 g((p.numColumns + cpb - 1) / cpb, p.dimZ);
+    y_forward_split<S, A, NY><<<g, kThreads, smem(cpb), st>>>(p, cpb);
+  }
+};
+
+template <typename S, typename A, int NX, bool R2C>
+struct XSplitKernels {
+  using CA = typename Types<S, A>::CA;
+  static size_t smem(int numColumns, int rpb) {
+    return RowSmem<CA, NX, R2C>::template bytes<CA>(numColumns, rpb);
+  }
+  static cudaError_t prepare(size_t maxSmem) {
+    cudaError_t e1 = allow_dynamic_smem(x_backward_split<S, A, NX, R2C>, maxSmem);
+    cudaError_t e2 = allow_dynamic_smem(x_forward_split<S, A, NX, R2C>, maxSmem);
+    return e1 != cudaSuccess ? e1 : e2;
+  }
+  static void backward(const PlanView<S>& p, int rpb, S* space, cudaStream_t st) {
+    const dim3 g((p.dimY + rpb - 1) / rpb, p.dimZ);
+    x_backward_split<S, A, NX, R2C><<<g, kThreads, smem(p.numColumns, rpb), st>>>(p, space, rpb);
+  }
+  static void forward(const PlanView<S>& p, int rpb, const S* space, cudaStream_t st) {
+    const dim3 g((p.dimY + rpb - 1) / rpb, p.dimZ);
+    x_forward_split<S, A, NX, R2C><<<g, kThreads, smem(p.numColumns, rpb), st>>>(p, space, rpb);
+  }
+};
+
 // Arithmetic type of the specialised kernels for a storage type: float for FP32, double-float
 // for FP64.
 template <typename S>

@@ -9,7 +9,22 @@
 namespace spfft {
 namespace gb300 {
 
-enum class FastOp { Has, Prepare, ZBackward, ZForward, PlaneBackward, PlaneForward, PlaneSmem, ZSmem };
+enum class FastOp {
+  Has,
+  Prepare,
+  ZBackward,
+  ZForward,
+  PlaneBackward,
+  PlaneForward,
+  PlaneSmem,
+  ZSmem,
+  YBackward,  // split y pass (n = dimY), param = columns per block
+  YForward,
+  YSmem,
+  XBackward,  // split x pass (n = dimX), param = rows per block
+  XForward,
+  XSmem
+};
 
 template <typename T>
 struct FastArgs {

@@ -265,12 +265,12 @@ def test_kernel_paths_and_fallbacks(lib):
                 random_indices(rng, *dims, r2c=(ttype == 1))
             tr = _transform(dtype, ttype, dims, idx)
             info = tr.path_info()
-            assert info["fused_plane"] == (dims[0] == dims[1]), (dtype, dims, info)
+            assert info["split_plane"], (dtype, dims, info)
             assert info["fast_z"] == (dims[2] in (12, 64, 100, 192)), (dtype, dims, info)
     # 192^3 C2C |k| <= 48 FP64: 97 columns do not fit one block's shared memory -> generic planes
     idx = sphere_indices(192, 48)
     tr = _transform("float64", 0, (192, 192, 192), idx)
-    assert tr.path_info() == {"fast_z": True, "fused_plane": False}
+    assert tr.path_info()["fast_z"] and not tr.path_info()["fused_plane"]
     vals = _values(rng, len(idx))
     oracle = pipeline.HostPipeline(0, 192, 192, 192, idx)
     out = torch.empty((192, 192, 192), dtype=torch.complex128, device="cuda")
@@ -281,7 +281,7 @@ def test_kernel_paths_and_fallbacks(lib):
     dims = (48, 48, 48)
     idx = sphere_indices(48, 12, r2c=True)
     tr = _transform("float64", 1, dims, idx)
-    assert tr.path_info()["fused_plane"]
+    assert tr.path_info()["split_plane"]
     vals = _values(rng, len(idx))
     oracle = pipeline.HostPipeline(1, *dims, idx)
     big = torch.zeros(48 ** 3 + 1, dtype=torch.float64, device="cuda")
@@ -297,3 +297,27 @@ def test_kernel_paths_and_fallbacks(lib):
     with pytest.raises(sp.SpfftError) as e:
         tr.backward(vbig[1:], torch.empty((48, 48, 48), dtype=torch.float64, device="cuda"))
     assert e.value.code == sp.ErrorCode.SPFFT_INVALID_PARAMETER_ERROR
+
+
+@pytest.mark.parametrize("plane", ["generic", "fused", "split"])
+@pytest.mark.parametrize("dtype", ["float64", "float32"])
+def test_plane_strategies_agree(lib, plane, dtype, monkeypatch):
+    """Every plane strategy (generic kernels, one fused kernel per plane, split y / x kernels) gives
+    the oracle's result, for C2C and R2C, backward and forward."""
+    monkeypatch.setenv("SPFFT_GB300_PLANE", plane)
+    rng = np.random.default_rng(17)
+    for n, radius, ttype in [(64, 16, 0), (96, 24, 1), (48, 20, 1), (60, 13, 0)]:
+        idx = sphere_indices(n, radius, r2c=(ttype == 1))
+        tr = _transform(dtype, ttype, (n, n, n), idx)
+        info = tr.path_info()
+        assert info["fused_plane"] == (plane == "fused") and info["split_plane"] == (plane == "split"), info
+        vals = _values(rng, len(idx))
+        oracle = pipeline.HostPipeline(ttype, n, n, n, idx)
+        want = oracle.backward(vals)
+        st = CT[dtype] if ttype == 0 else RT[dtype]
+        out = torch.empty((n, n, n), dtype=st, device="cuda")
+        tr.backward(torch.from_numpy(vals).to(CT[dtype]).cuda(), out)
+        assert rel_l2(out.cpu().numpy(), want) <= TOL[dtype], (n, ttype, plane)
+        f = torch.empty(len(idx), dtype=CT[dtype], device="cuda")
+        tr.forward(out, f)
+        assert rel_l2(f.cpu().numpy(), oracle.forward(out.cpu().numpy().astype(np.complex128 if ttype == 0 else np.float64))) <= TOL[dtype]
