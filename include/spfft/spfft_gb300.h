@@ -74,6 +74,33 @@ SPFFT_EXPORT SpfftError spfft_gb300_transform_path_info(SpfftTransform transform
 SPFFT_EXPORT SpfftError spfft_gb300_float_transform_path_info(SpfftFloatTransform transform,
                                                               int* flags);
 
+/* ---- batched execution (no counterpart in the reference; the GB300 form of its multi-transform)
+ * A batch holds many transforms (all double or all float, on distinct grids, same device). Each
+ * pass of each group of equally shaped transforms runs as ONE kernel launch over all of them, so
+ * small transforms fill the GPU. Buffers are bound once; a backward + forward pair can be captured
+ * into a CUDA graph on first use and replayed. Transforms whose lengths have no specialised
+ * kernels run one by one inside the same calls. */
+typedef void* SpfftGb300Batch;
+SPFFT_EXPORT SpfftError spfft_gb300_batch_create(SpfftGb300Batch* batch, int numTransforms,
+                                                 const SpfftTransform* transforms);
+SPFFT_EXPORT SpfftError spfft_gb300_float_batch_create(SpfftGb300Batch* batch, int numTransforms,
+                                                       const SpfftFloatTransform* transforms);
+SPFFT_EXPORT SpfftError spfft_gb300_batch_destroy(SpfftGb300Batch batch);
+/* values[i]: device interleaved-complex frequency values of transform i; spaces[i]: its device
+ * space domain. Pointers must be aligned to the complex size (16 bytes double, 8 bytes float). */
+SPFFT_EXPORT SpfftError spfft_gb300_batch_bind(SpfftGb300Batch batch, void* const* values,
+                                               void* const* spaces);
+SPFFT_EXPORT SpfftError spfft_gb300_batch_backward(SpfftGb300Batch batch, void* stream);
+SPFFT_EXPORT SpfftError spfft_gb300_batch_forward(SpfftGb300Batch batch, SpfftScalingType scaling,
+                                                  void* stream);
+/* Backward then forward of every transform as one CUDA graph on `stream` (not the default
+ * stream). The graph is captured on the first call for each scaling and replayed afterwards;
+ * rebinding buffers drops it. */
+SPFFT_EXPORT SpfftError spfft_gb300_batch_pair_graph(SpfftGb300Batch batch, SpfftScalingType scaling,
+                                                     void* stream);
+SPFFT_EXPORT SpfftError spfft_gb300_batch_info(SpfftGb300Batch batch, int* numGroups,
+                                               int* numUnbatched, int* launchesPerPair);
+
 /* Allocation-free backward transform (no counterpart in the reference). Runs the backward transform
  * of an existing double-precision transform on device pointers (values: interleaved complex
  * frequency values; space: the space domain in the transform's layout) on `stream` (a

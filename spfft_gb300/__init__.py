@@ -134,6 +134,15 @@ def _declare(lib: ctypes.CDLL) -> None:
         getattr(lib, prefix + "transform_stage_times").argtypes = [_vp, _i, _vp, _vp, _i, _vp,
                                                                    ctypes.POINTER(ctypes.c_float)]
     lib.spfft_gb300_plan_indices.argtypes = [_i, _i, _i, _i, _i, _vp, _vp, _vp, _i, _ip, _ip]
+    lib.spfft_gb300_batch_create.argtypes = [ctypes.POINTER(_vp), _i, ctypes.POINTER(_vp)]
+    lib.spfft_gb300_float_batch_create.argtypes = [ctypes.POINTER(_vp), _i, ctypes.POINTER(_vp)]
+    lib.spfft_gb300_batch_destroy.argtypes = [_vp]
+    lib.spfft_gb300_batch_bind.argtypes = [_vp, ctypes.POINTER(_vp), ctypes.POINTER(_vp)]
+    lib.spfft_gb300_batch_backward.argtypes = [_vp, _vp]
+    lib.spfft_gb300_batch_forward.argtypes = [_vp, _i, _vp]
+    lib.spfft_gb300_batch_pair_graph.argtypes = [_vp, _i, _vp]
+    lib.spfft_gb300_batch_info.argtypes = [_vp, _ip, _ip, _ip]
+    lib.spfft_gb300_transform_backward_noalloc.argtypes = [_vp, _vp, _vp, _vp]
 
 
 def _check(code: int, func: str) -> None:
@@ -405,3 +414,54 @@ def multi_transform_forward(transforms, inputs, outputs, scalings=None) -> None:
     else:
         ins = (_vp * n)(*[address(x) for x in inputs])
         _call(p + "multi_transform_forward_ptr", n, _handles(transforms), ins, outs, sc)
+
+
+def _stream_handle(stream: Any):
+    return None if stream is None else int(getattr(stream, "cuda_stream", stream))
+
+
+class Batch:
+    """Many transforms executed together: each pass of each group of equally shaped transforms is
+    one kernel launch, and a backward + forward pair can run as a captured CUDA graph
+    (``spfft_gb300_batch_*`` in include/spfft/spfft_gb300.h)."""
+
+    def __init__(self, transforms):
+        if not transforms:
+            raise ValueError("empty batch")
+        dtypes = {t.dtype for t in transforms}
+        if len(dtypes) != 1:
+            raise ValueError("a batch holds transforms of one precision")
+        self.dtype = dtypes.pop()
+        self._transforms = list(transforms)
+        h = _vp()
+        fn = "spfft_gb300_float_batch_create" if _prefix(self.dtype) == "spfft_float_" else "spfft_gb300_batch_create"
+        _call(fn, ctypes.byref(h), len(transforms), _handles(transforms))
+        self._h = h
+        self._bound = None
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value and _lib is not None:
+            _lib.spfft_gb300_batch_destroy(h)
+            self._h = None
+
+    def bind(self, values, spaces) -> None:
+        n = len(self._transforms)
+        v = (_vp * n)(*[address(x) for x in values])
+        s = (_vp * n)(*[address(x) for x in spaces])
+        _call("spfft_gb300_batch_bind", self._h, v, s)
+        self._bound = (list(values), list(spaces))  # keep the buffers alive
+
+    def backward(self, stream: Any = None) -> None:
+        _call("spfft_gb300_batch_backward", self._h, _stream_handle(stream))
+
+    def forward(self, scaling: int = SPFFT_NO_SCALING, stream: Any = None) -> None:
+        _call("spfft_gb300_batch_forward", self._h, scaling, _stream_handle(stream))
+
+    def pair_graph(self, scaling: int = SPFFT_NO_SCALING, stream: Any = None) -> None:
+        _call("spfft_gb300_batch_pair_graph", self._h, scaling, _stream_handle(stream))
+
+    def info(self) -> dict:
+        g, u, l = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        _call("spfft_gb300_batch_info", self._h, ctypes.byref(g), ctypes.byref(u), ctypes.byref(l))
+        return {"groups": g.value, "unbatched": u.value, "launches_per_pair": l.value}

@@ -12,5 +12,7 @@ struct TransformAccess {
   static TransformInternal<float>& get(TransformFloat& t) { return *t.transform_; }
   static const TransformInternal<double>& get(const Transform& t) { return *t.transform_; }
   static const TransformInternal<float>& get(const TransformFloat& t) { return *t.transform_; }
+  static std::shared_ptr<TransformInternal<double>> share(Transform& t) { return t.transform_; }
+  static std::shared_ptr<TransformInternal<float>> share(TransformFloat& t) { return t.transform_; }
 };
 }  // namespace spfft

@@ -1,0 +1,344 @@
+// BatchPlan: groups transforms by shape, uploads their plan views and bound buffer pointers, and
+// runs each pass of each group as one batched launch.
+#include "batch.hpp"
+
+#include <algorithm>
+#include <cstring>
+#include <map>
+#include <tuple>
+
+#include "engine.hpp"
+#include "kernels_fast.hpp"
+
+namespace spfft {
+namespace gb300 {
+
+namespace {
+constexpr size_t kAlign = 256;
+inline size_t align_up(size_t v) { return (v + kAlign - 1) / kAlign * kAlign; }
+constexpr size_t kZBudget = 56 * 1024, kPlaneBudget = 100 * 1024;
+}  // namespace
+
+template <typename T>
+struct BatchPlan<T>::Group {
+  int nx = 0, ny = 0, nz = 0;
+  bool r2c = false;
+  std::vector<int> members;
+  int spb = 0, cpb = 0, rpb = 0;
+  size_t smemZ = 0, smemY = 0, smemX = 0;
+  int blocksZ = 0, blocksY = 0, blocksX = 0;
+  T scale = T(0);
+  DeviceBuffer dev;
+  size_t offViews = 0, offStartsZ = 0, offStartsY = 0, offStartsX = 0, offValues = 0, offSpaces = 0;
+  BatchView<T> view(size_t startsOff, T scaleValue) const {
+    char* d = static_cast<char*>(dev.get());
+    BatchView<T> v;
+    v.views = reinterpret_cast<const PlanView<T>*>(d + offViews);
+    v.starts = reinterpret_cast<const int*>(d + startsOff);
+    v.count = static_cast<int>(members.size());
+    v.in = nullptr;
+    v.out = nullptr;
+    v.scale = scaleValue;
+    return v;
+  }
+};
+
+template <typename T>
+BatchPlan<T>::BatchPlan(std::vector<std::shared_ptr<TransformInternal<T>>> transforms)
+    : transforms_(std::move(transforms)) {
+  const int n = static_cast<int>(transforms_.size());
+  if (n == 0) throw InvalidParameterError();
+  for (auto& t : transforms_) {
+    if (!t) throw InvalidParameterError();
+  }
+  device_ = transforms_[0]->device_id();
+  for (int a = 0; a < n; ++a) {
+    if (transforms_[a]->device_id() != device_) throw InvalidParameterError();
+    for (int b = a + 1; b < n; ++b) {
+      if (transforms_[a]->shared_grid(*transforms_[b])) throw InvalidParameterError();
+    }
+  }
+  DeviceGuard guard(device_);
+  const size_t optin = smem_optin(device_) - 1024;
+
+  // group by shape; transforms without specialised kernels for every length run one by one
+  std::map<std::tuple<int, int, int, bool>, int> index;
+  for (int t = 0; t < n; ++t) {
+    const IndexPlan& ip = transforms_[t]->index_plan();
+    const bool r2c = ip.type == SPFFT_TRANS_R2C;
+    const bool ok = ip.num_sticks() > 0 && fast_prepare<T>(device_, ip.dimX) &&
+                    fast_prepare<T>(device_, ip.dimY) && fast_prepare<T>(device_, ip.dimZ);
+    if (!ok) {
+      fallback_.push_back(t);
+      continue;
+    }
+    const auto key = std::make_tuple(ip.dimX, ip.dimY, ip.dimZ, r2c);
+    auto it = index.find(key);
+    if (it == index.end()) {
+      it = index.emplace(key, static_cast<int>(groups_.size())).first;
+      groups_.emplace_back(new Group());
+      Group& g = *groups_.back();
+      g.nx = ip.dimX;
+      g.ny = ip.dimY;
+      g.nz = ip.dimZ;
+      g.r2c = r2c;
+      g.scale = static_cast<T>(1.0 / (static_cast<double>(ip.dimX) * ip.dimY * ip.dimZ));
+    }
+    groups_[it->second]->members.push_back(t);
+  }
+
+  // tile shapes per group (sized for the group's widest plane) and device tables
+  std::vector<std::unique_ptr<Group>> kept;
+  for (auto& gp : groups_) {
+    Group& g = *gp;
+    int maxCols = 1;
+    for (int t : g.members) maxCols = std::max(maxCols, transforms_[t]->index_plan().num_columns());
+    FastArgs<T> a;
+    size_t sm = 0;
+    a.smemOut = &sm;
+    for (g.spb = 32; g.spb > 1; g.spb /= 2) {
+      a.param = g.spb;
+      fast_dispatch<T>(FastOp::ZSmem, g.nz, g.r2c, a);
+      if (sm <= kZBudget) break;
+    }
+    a.param = g.spb;
+    fast_dispatch<T>(FastOp::ZSmem, g.nz, g.r2c, a);
+    g.smemZ = sm;
+    for (g.cpb = 16; g.cpb > 1; g.cpb /= 2) {
+      a.param = g.cpb;
+      fast_dispatch<T>(FastOp::YSmem, g.ny, g.r2c, a);
+      if (sm <= kPlaneBudget) break;
+    }
+    a.param = g.cpb;
+    fast_dispatch<T>(FastOp::YSmem, g.ny, g.r2c, a);
+    g.smemY = sm;
+    a.numColumns = maxCols;
+    for (g.rpb = 32; g.rpb > 1; g.rpb /= 2) {
+      a.param = g.rpb;
+      fast_dispatch<T>(FastOp::XSmem, g.nx, g.r2c, a);
+      if (sm <= kPlaneBudget) break;
+    }
+    a.param = g.rpb;
+    fast_dispatch<T>(FastOp::XSmem, g.nx, g.r2c, a);
+    g.smemX = sm;
+    g.rpb = std::min(g.rpb, g.ny);
+    if (g.smemZ > optin || g.smemY > optin || g.smemX > optin) {
+      for (int t : g.members) fallback_.push_back(t);
+      continue;
+    }
+    const size_t m = g.members.size();
+    g.offViews = 0;
+    g.offStartsZ = align_up(m * sizeof(PlanView<T>));
+    g.offStartsY = g.offStartsZ + align_up((m + 1) * sizeof(int));
+    g.offStartsX = g.offStartsY + align_up((m + 1) * sizeof(int));
+    g.offValues = g.offStartsX + align_up((m + 1) * sizeof(int));
+    g.offSpaces = g.offValues + align_up(m * sizeof(T*));
+    g.dev = DeviceBuffer(g.offSpaces + align_up(m * sizeof(T*)));
+    std::vector<int> sz(m + 1, 0), sy(m + 1, 0), sx(m + 1, 0);
+    for (size_t i = 0; i < m; ++i) {
+      const IndexPlan& ip = transforms_[g.members[i]]->index_plan();
+      sz[i + 1] = sz[i] + (ip.num_sticks() + g.spb - 1) / g.spb;
+      sy[i + 1] = sy[i] + ((ip.num_columns() + g.cpb - 1) / g.cpb) * ip.dimZ;
+      sx[i + 1] = sx[i] + ((ip.dimY + g.rpb - 1) / g.rpb) * ip.dimZ;
+    }
+    g.blocksZ = sz[m];
+    g.blocksY = sy[m];
+    g.blocksX = sx[m];
+    char* d = static_cast<char*>(g.dev.get());
+    check_cuda(cudaMemcpy(d + g.offStartsZ, sz.data(), (m + 1) * sizeof(int), cudaMemcpyHostToDevice));
+    check_cuda(cudaMemcpy(d + g.offStartsY, sy.data(), (m + 1) * sizeof(int), cudaMemcpyHostToDevice));
+    check_cuda(cudaMemcpy(d + g.offStartsX, sx.data(), (m + 1) * sizeof(int), cudaMemcpyHostToDevice));
+    kept.push_back(std::move(gp));
+  }
+  groups_ = std::move(kept);
+  std::sort(fallback_.begin(), fallback_.end());
+  scratchSeen_.assign(n, nullptr);
+  values_.assign(n, nullptr);
+  spaces_.assign(n, nullptr);
+  upload_views();
+}
+
+template <typename T>
+BatchPlan<T>::~BatchPlan() {
+  for (auto& g : graphs_) {
+    if (g) (void)cudaGraphExecDestroy(g);
+  }
+}
+
+template <typename T>
+int BatchPlan<T>::launches_per_pair() const {
+  return 6 * static_cast<int>(groups_.size()) + 6 * static_cast<int>(fallback_.size());
+}
+
+// Plan views embed the grids' scratch pointers; refresh them if a grid's scratch moved (a grid
+// grows its scratch when another transform is created on it).
+template <typename T>
+void BatchPlan<T>::upload_views() {
+  bool changed = false;
+  for (size_t t = 0; t < transforms_.size(); ++t) {
+    void* sc = transforms_[t]->grid().scratch();
+    if (sc != scratchSeen_[t]) changed = true;
+    scratchSeen_[t] = sc;
+  }
+  if (!changed) return;
+  DeviceGuard guard(device_);
+  for (auto& gp : groups_) {
+    Group& g = *gp;
+    std::vector<PlanView<T>> views;
+    for (int t : g.members) {
+      views.push_back(transforms_[t]->gpu_plan().device_view(transforms_[t]->grid().scratch()));
+    }
+    check_cuda(cudaMemcpy(static_cast<char*>(g.dev.get()) + g.offViews, views.data(),
+                          views.size() * sizeof(PlanView<T>), cudaMemcpyHostToDevice));
+  }
+}
+
+template <typename T>
+void BatchPlan<T>::bind(const T* const* values, T* const* spaces) {
+  if (!values || !spaces) throw InvalidParameterError();
+  const uintptr_t c = 2 * sizeof(T);
+  for (size_t t = 0; t < transforms_.size(); ++t) {
+    if (!spaces[t] || reinterpret_cast<uintptr_t>(spaces[t]) % c) throw InvalidParameterError();
+    if (transforms_[t]->num_local_elements() > 0 &&
+        (!values[t] || reinterpret_cast<uintptr_t>(values[t]) % c)) {
+      throw InvalidParameterError();
+    }
+    values_[t] = values[t];
+    spaces_[t] = spaces[t];
+  }
+  DeviceGuard guard(device_);
+  for (auto& gp : groups_) {
+    Group& g = *gp;
+    std::vector<T*> vp, sp;
+    for (int t : g.members) {
+      vp.push_back(const_cast<T*>(values_[t]));
+      sp.push_back(spaces_[t]);
+    }
+    char* d = static_cast<char*>(g.dev.get());
+    check_cuda(cudaMemcpy(d + g.offValues, vp.data(), vp.size() * sizeof(T*), cudaMemcpyHostToDevice));
+    check_cuda(cudaMemcpy(d + g.offSpaces, sp.data(), sp.size() * sizeof(T*), cudaMemcpyHostToDevice));
+  }
+  for (auto& g : graphs_) {
+    if (g) (void)cudaGraphExecDestroy(g);
+    g = nullptr;
+  }
+  bound_ = true;
+}
+
+template <typename T>
+void BatchPlan<T>::check_bound() const {
+  if (!bound_) throw InvalidParameterError();
+}
+
+namespace {
+template <typename T>
+void launch(FastOp op, int n, bool r2c, const BatchView<T>& bv, int blocks, size_t smem, int param,
+            cudaStream_t s) {
+  if (blocks == 0) return;
+  FastArgs<T> a;
+  a.batch = &bv;
+  a.blocks = blocks;
+  a.smem = smem;
+  a.param = param;
+  a.stream = s;
+  fast_dispatch<T>(op, n, r2c, a);
+  check_launch(cudaGetLastError());
+}
+}  // namespace
+
+template <typename T>
+void BatchPlan<T>::backward(cudaStream_t stream) {
+  check_bound();
+  DeviceGuard guard(device_);
+  upload_views();
+  for (auto& gp : groups_) {
+    Group& g = *gp;
+    BatchView<T> bv = g.view(g.offStartsZ, T(0));
+    bv.in = reinterpret_cast<const T* const*>(static_cast<char*>(g.dev.get()) + g.offValues);
+    launch(FastOp::BatchZBackward, g.nz, g.r2c, bv, g.blocksZ, g.smemZ, g.spb, stream);
+  }
+  for (auto& gp : groups_) {
+    Group& g = *gp;
+    BatchView<T> bv = g.view(g.offStartsY, T(0));
+    launch(FastOp::BatchYBackward, g.ny, g.r2c, bv, g.blocksY, g.smemY, g.cpb, stream);
+  }
+  for (auto& gp : groups_) {
+    Group& g = *gp;
+    BatchView<T> bv = g.view(g.offStartsX, T(0));
+    bv.out = reinterpret_cast<T* const*>(static_cast<char*>(g.dev.get()) + g.offSpaces);
+    launch(FastOp::BatchXBackward, g.nx, g.r2c, bv, g.blocksX, g.smemX, g.rpb, stream);
+  }
+  for (int t : fallback_) {
+    transforms_[t]->gpu_plan().backward(values_[t], spaces_[t], transforms_[t]->grid().scratch(), stream);
+  }
+}
+
+template <typename T>
+void BatchPlan<T>::forward(bool scaled, cudaStream_t stream) {
+  check_bound();
+  DeviceGuard guard(device_);
+  upload_views();
+  for (auto& gp : groups_) {
+    Group& g = *gp;
+    BatchView<T> bv = g.view(g.offStartsX, T(0));
+    bv.in = reinterpret_cast<const T* const*>(static_cast<char*>(g.dev.get()) + g.offSpaces);
+    launch(FastOp::BatchXForward, g.nx, g.r2c, bv, g.blocksX, g.smemX, g.rpb, stream);
+  }
+  for (auto& gp : groups_) {
+    Group& g = *gp;
+    BatchView<T> bv = g.view(g.offStartsY, T(0));
+    launch(FastOp::BatchYForward, g.ny, g.r2c, bv, g.blocksY, g.smemY, g.cpb, stream);
+  }
+  for (auto& gp : groups_) {
+    Group& g = *gp;
+    BatchView<T> bv = g.view(g.offStartsZ, scaled ? g.scale : T(0));
+    bv.out = reinterpret_cast<T* const*>(static_cast<char*>(g.dev.get()) + g.offValues);
+    launch(FastOp::BatchZForward, g.nz, g.r2c, bv, g.blocksZ, g.smemZ, g.spb, stream);
+  }
+  for (int t : fallback_) {
+    transforms_[t]->gpu_plan().forward(spaces_[t], const_cast<T*>(values_[t]), scaled,
+                                       transforms_[t]->grid().scratch(), stream);
+  }
+}
+
+template <typename T>
+void BatchPlan<T>::pair_graph(bool scaled, cudaStream_t stream) {
+  check_bound();
+  if (stream == nullptr || stream == cudaStreamLegacy || stream == cudaStreamPerThread) {
+    throw InvalidParameterError();
+  }
+  DeviceGuard guard(device_);
+  // refresh views outside the capture (a synchronous copy cannot be captured)
+  std::vector<void*> seen = scratchSeen_;
+  upload_views();
+  if (seen != scratchSeen_) {
+    for (auto& g : graphs_) {
+      if (g) (void)cudaGraphExecDestroy(g);
+      g = nullptr;
+    }
+  }
+  cudaGraphExec_t& exec = graphs_[scaled ? 1 : 0];
+  if (!exec) {
+    cudaGraph_t graph = nullptr;
+    check_cuda(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+    try {
+      backward(stream);
+      forward(scaled, stream);
+    } catch (...) {
+      (void)cudaStreamEndCapture(stream, &graph);
+      if (graph) (void)cudaGraphDestroy(graph);
+      throw;
+    }
+    check_cuda(cudaStreamEndCapture(stream, &graph));
+    const cudaError_t st = cudaGraphInstantiate(&exec, graph, 0);
+    (void)cudaGraphDestroy(graph);
+    check_cuda(st);
+  }
+  check_cuda(cudaGraphLaunch(exec, stream));
+}
+
+template class BatchPlan<double>;
+template class BatchPlan<float>;
+
+}  // namespace gb300
+}  // namespace spfft

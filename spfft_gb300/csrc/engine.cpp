@@ -380,6 +380,15 @@ void GpuPlan<T>::forward(const T* space, T* values, bool scaled, void* scratch,
   mark(events, 3, stream);
 }
 
+size_t smem_optin(int device) { return static_cast<size_t>(max_smem_optin(device)); }
+template <typename T>
+bool fast_prepare(int device, int n) {
+  FastArgs<T> a;
+  return fast_dispatch<T>(FastOp::Has, n, false, a) && prepare_fast_once<T>(device, n);
+}
+template bool fast_prepare<double>(int, int);
+template bool fast_prepare<float>(int, int);
+
 template class GpuPlan<double>;
 template class GpuPlan<float>;
 

@@ -43,6 +43,10 @@ public:
     return (fastZ_ ? 1 : 0) | (planePath_ == PlanePath::Fused ? 2 : 0) | (planePath_ == PlanePath::Split ? 4 : 0);
   }
 
+  // Device view of this plan with its intermediates in `scratch` (used by batched execution).
+  PlanView<T> device_view(void* scratch) const { return view(scratch); }
+  T forward_scale() const { return scale_; }
+
   // Device pointer of the value staging area inside `scratch` (host input / output path).
   T* staging(void* scratch) const {
     return reinterpret_cast<T*>(static_cast<char*>(scratch) + layout_.valuesOffset);
@@ -62,6 +66,12 @@ private:
   T scale_ = T(1);
   DeviceBuffer tables_;
 };
+
+// Opt-in shared memory per block of `device`, and one-time attribute setup of the specialised
+// kernels of length n (false if n has no specialised kernels).
+size_t smem_optin(int device);
+template <typename T>
+bool fast_prepare(int device, int n);
 
 extern template class GpuPlan<double>;
 extern template class GpuPlan<float>;

@@ -37,6 +37,18 @@ struct PlanView {
   T* planes;
 };
 
+// Device tables of one shape group of a batch for one pass (all device pointers); read by the
+// batched kernels (kernels_batch.cuh).
+template <typename S>
+struct BatchView {
+  const PlanView<S>* views;  // [count]
+  const int* starts;         // [count + 1] first block of each transform in this pass
+  int count;
+  const S* const* in;   // per transform: values (backward z) or space (forward x)
+  S* const* out;        // per transform: space (backward x) or values (forward z)
+  S scale;              // forward scaling factor, 0 = none
+};
+
 // Tile shapes of the generic kernels, chosen by the host (engine.cpp: choose_launch_config).
 struct LaunchConfig {
   int threads;            // threads per block (all kernels)

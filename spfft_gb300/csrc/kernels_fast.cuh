@@ -154,17 +154,19 @@ struct ZLayout {
   static constexpr int pitch = NZ | 1;  // odd: conflict-free column access across sticks
 };
 
+// Kernel bodies take their block coordinates as arguments, so the single-transform kernels and the
+// batched kernels (kernels_batch.cuh) share them.
 template <typename S, typename A, int NZ>
-__global__ void __launch_bounds__(kThreads) z_backward(const PlanView<S> p,
-                                                       const S* __restrict__ values, int spb) {
+__device__ __forceinline__ void z_backward_body(const PlanView<S>& p, const S* __restrict__ values,
+                                                int spb, int bx, int* sExpPtr) {
   using TT = Types<S, A>;
   using CS = typename TT::CS;
   using CA = typename TT::CA;
   constexpr int Az = Shape<NZ>::A, Bz = Shape<NZ>::B, PZ = ZLayout<NZ>::pitch;
-  __shared__ int sExp;
+  int& sExp = *sExpPtr;
   CA* tw = reinterpret_cast<CA*>(g_fast_smem);
   CA* buf = tw + NZ;
-  const int s0 = blockIdx.x * spb;
+  const int s0 = bx * spb;
   const int nsb = min(spb, p.numSticks - s0);
 
   load_twiddles<S, A>(tw, p.twz, NZ);
@@ -217,16 +219,23 @@ __global__ void __launch_bounds__(kThreads) z_backward(const PlanView<S> p,
 }
 
 template <typename S, typename A, int NZ>
-__global__ void __launch_bounds__(kThreads) z_forward(const PlanView<S> p, S* __restrict__ values,
-                                                      S scale, int spb) {
+__global__ void __launch_bounds__(kThreads) z_backward(const PlanView<S> p,
+                                                       const S* __restrict__ values, int spb) {
+  __shared__ int sExp;
+  z_backward_body<S, A, NZ>(p, values, spb, blockIdx.x, &sExp);
+}
+
+template <typename S, typename A, int NZ>
+__device__ __forceinline__ void z_forward_body(const PlanView<S>& p, S* __restrict__ values, S scale,
+                                               int spb, int bx, int* sExpPtr) {
   using TT = Types<S, A>;
   using CS = typename TT::CS;
   using CA = typename TT::CA;
   constexpr int Az = Shape<NZ>::A, Bz = Shape<NZ>::B, PZ = ZLayout<NZ>::pitch;
-  __shared__ int sExp;
+  int& sExp = *sExpPtr;
   CA* tw = reinterpret_cast<CA*>(g_fast_smem);
   CA* buf = tw + NZ;
-  const int s0 = blockIdx.x * spb;
+  const int s0 = bx * spb;
   const int nsb = min(spb, p.numSticks - s0);
 
   load_twiddles<S, A>(tw, p.twz, NZ);
@@ -268,6 +277,13 @@ __global__ void __launch_bounds__(kThreads) z_forward(const PlanView<S> p, S* __
     if (scale != S(0)) v = cscale(v, scale);
     out[p.entryUser[e]] = v;
   }
+}
+
+template <typename S, typename A, int NZ>
+__global__ void __launch_bounds__(kThreads) z_forward(const PlanView<S> p, S* __restrict__ values,
+                                                      S scale, int spb) {
+  __shared__ int sExp;
+  z_forward_body<S, A, NZ>(p, values, scale, spb, blockIdx.x, &sExp);
 }
 
 // ================================================================================================
@@ -610,17 +626,16 @@ struct PlaneKernels {
 // ================================================================================================
 // y backward: block (column group, z)
 template <typename S, typename A, int NY>
-__global__ void __launch_bounds__(kThreads) y_backward_split(const PlanView<S> p, int cpb) {
+__device__ __forceinline__ void y_backward_body(const PlanView<S>& p, int cpb, int bx, int z, int* sExpPtr) {
   using TT = Types<S, A>;
   using CS = typename TT::CS;
   using CA = typename TT::CA;
   constexpr int Ay = Shape<NY>::A, By = Shape<NY>::B;
-  __shared__ int sExp;
+  int& sExp = *sExpPtr;
   CA* tw = reinterpret_cast<CA*>(g_fast_smem);
   CA* buf = tw + NY;
   const int nc = p.numColumns;
-  const int c0 = blockIdx.x * cpb, ncb = min(cpb, nc - c0);
-  const int z = blockIdx.y;
+  const int c0 = bx * cpb, ncb = min(cpb, nc - c0);
   load_twiddles<S, A>(tw, p.twy, NY);
   for (int i = threadIdx.x; i < NY * ncb; i += blockDim.x) buf[i] = czero<A>();
   __syncthreads();
@@ -649,19 +664,24 @@ __global__ void __launch_bounds__(kThreads) y_backward_split(const PlanView<S> p
   }
 }
 
+template <typename S, typename A, int NY>
+__global__ void __launch_bounds__(kThreads) y_backward_split(const PlanView<S> p, int cpb) {
+  __shared__ int sExp;
+  y_backward_body<S, A, NY>(p, cpb, blockIdx.x, blockIdx.y, &sExp);
+}
+
 // y forward: block (column group, z)
 template <typename S, typename A, int NY>
-__global__ void __launch_bounds__(kThreads) y_forward_split(const PlanView<S> p, int cpb) {
+__device__ __forceinline__ void y_forward_body(const PlanView<S>& p, int cpb, int bx, int z, int* sExpPtr) {
   using TT = Types<S, A>;
   using CS = typename TT::CS;
   using CA = typename TT::CA;
   constexpr int Ay = Shape<NY>::A, By = Shape<NY>::B;
-  __shared__ int sExp;
+  int& sExp = *sExpPtr;
   CA* tw = reinterpret_cast<CA*>(g_fast_smem);
   CA* buf = tw + NY;
   const int nc = p.numColumns;
-  const int c0 = blockIdx.x * cpb, ncb = min(cpb, nc - c0);
-  const int z = blockIdx.y;
+  const int c0 = bx * cpb, ncb = min(cpb, nc - c0);
   load_twiddles<S, A>(tw, p.twy, NY);
   const CS* planes = reinterpret_cast<const CS*>(p.planes) + static_cast<size_t>(z) * NY * nc + c0;
   for (int i = threadIdx.x; i < NY * ncb; i += blockDim.x) {
@@ -690,6 +710,12 @@ __global__ void __launch_bounds__(kThreads) y_forward_split(const PlanView<S> p,
   for (int st = sBegin + threadIdx.x; st < sEnd; st += blockDim.x) {
     sticks[st] = to_storage(buf[transposed_pos<NY>(p.stickY[st]) * ncb + (p.stickColumn[st] - c0)], k);
   }
+}
+
+template <typename S, typename A, int NY>
+__global__ void __launch_bounds__(kThreads) y_forward_split(const PlanView<S> p, int cpb) {
+  __shared__ int sExp;
+  y_forward_body<S, A, NY>(p, cpb, blockIdx.x, blockIdx.y, &sExp);
 }
 
 // Shared memory of the x kernels: twx[NX] | (R2C) twm[M] | colOf[NXF] | P[rows][numColumns] |
@@ -734,17 +760,16 @@ __device__ __forceinline__ void row_load_tables(const PlanView<S>& p, RowSmem<ty
 
 // x backward: block (row group, z); compact rows from HBM -> x-FFT -> space rows
 template <typename S, typename A, int NX, bool R2C>
-__global__ void __launch_bounds__(kThreads) x_backward_split(const PlanView<S> p, S* __restrict__ space,
-                                                             int rpb) {
+__device__ __forceinline__ void x_backward_body(const PlanView<S>& p, S* __restrict__ space, int rpb,
+                                                int bx, int z, int* sExpPtr) {
   using TT = Types<S, A>;
   using CS = typename TT::CS;
   using CA = typename TT::CA;
   using L = PlaneLayout<NX, 2, R2C>;
   constexpr int Ax = L::Ax, Bx = L::Bx;
-  __shared__ int sExp;
+  int& sExp = *sExpPtr;
   const int nc = p.numColumns, ny = p.dimY;
-  const int y0 = blockIdx.x * rpb, nr = min(rpb, ny - y0);
-  const int z = blockIdx.y;
+  const int y0 = bx * rpb, nr = min(rpb, ny - y0);
   RowSmem<CA, NX, R2C> s(nc, rpb);
   row_load_tables<S, A, NX, R2C>(p, s);
   const CS* planes = reinterpret_cast<const CS*>(p.planes) + (static_cast<size_t>(z) * ny + y0) * nc;
@@ -794,19 +819,25 @@ __global__ void __launch_bounds__(kThreads) x_backward_split(const PlanView<S> p
   }
 }
 
+template <typename S, typename A, int NX, bool R2C>
+__global__ void __launch_bounds__(kThreads) x_backward_split(const PlanView<S> p, S* __restrict__ space,
+                                                             int rpb) {
+  __shared__ int sExp;
+  x_backward_body<S, A, NX, R2C>(p, space, rpb, blockIdx.x, blockIdx.y, &sExp);
+}
+
 // x forward: block (row group, z); space rows -> x-FFT -> compact rows to HBM
 template <typename S, typename A, int NX, bool R2C>
-__global__ void __launch_bounds__(kThreads) x_forward_split(const PlanView<S> p, const S* __restrict__ space,
-                                                            int rpb) {
+__device__ __forceinline__ void x_forward_body(const PlanView<S>& p, const S* __restrict__ space, int rpb,
+                                               int bx, int z, int* sExpPtr) {
   using TT = Types<S, A>;
   using CS = typename TT::CS;
   using CA = typename TT::CA;
   using L = PlaneLayout<NX, 2, R2C>;
   constexpr int Ax = L::Ax, Bx = L::Bx;
-  __shared__ int sExp;
+  int& sExp = *sExpPtr;
   const int nc = p.numColumns, ny = p.dimY;
-  const int y0 = blockIdx.x * rpb, nr = min(rpb, ny - y0);
-  const int z = blockIdx.y;
+  const int y0 = bx * rpb, nr = min(rpb, ny - y0);
   RowSmem<CA, NX, R2C> s(nc, rpb);
   row_load_tables<S, A, NX, R2C>(p, s);
   const CS* rows = reinterpret_cast<const CS*>(space + (static_cast<size_t>(z) * ny + y0) * NX * (R2C ? 1 : 2));
@@ -872,6 +903,13 @@ __global__ void __launch_bounds__(kThreads) x_forward_split(const PlanView<S> p,
   }
   CS* planes = reinterpret_cast<CS*>(p.planes) + (static_cast<size_t>(z) * ny + y0) * nc;
   for (int i = threadIdx.x; i < nr * nc; i += blockDim.x) planes[i] = to_storage(s.P[i], k);
+}
+
+template <typename S, typename A, int NX, bool R2C>
+__global__ void __launch_bounds__(kThreads) x_forward_split(const PlanView<S> p, const S* __restrict__ space,
+                                                            int rpb) {
+  __shared__ int sExp;
+  x_forward_body<S, A, NX, R2C>(p, space, rpb, blockIdx.x, blockIdx.y, &sExp);
 }
 
 template <typename S, typename A, int NY>

@@ -23,7 +23,15 @@ enum class FastOp {
   YSmem,
   XBackward,  // split x pass (n = dimX), param = rows per block
   XForward,
-  XSmem
+  XSmem,
+  // batched passes over a shape group (args.batch, args.blocks, args.smem): n is the z length for
+  // BatchZ*, the y length for BatchY*, the x length for BatchX*
+  BatchZBackward,
+  BatchZForward,
+  BatchYBackward,
+  BatchYForward,
+  BatchXBackward,
+  BatchXForward
 };
 
 template <typename T>
@@ -37,6 +45,9 @@ struct FastArgs {
   size_t maxSmem = 0;
   int numColumns = 0;
   size_t* smemOut = nullptr;
+  const BatchView<T>* batch = nullptr;
+  int blocks = 0;
+  size_t smem = 0;
 };
 
 // Each group handles its own sizes: returns true if `n` (the z length for z ops, the cubic plane
