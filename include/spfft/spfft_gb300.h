@@ -51,6 +51,32 @@ SPFFT_EXPORT SpfftError spfft_gb300_float_transform_forward_device(SpfftFloatTra
                                                                    SpfftScalingType scaling,
                                                                    void* stream);
 
+/* Adjoints for differentiation (no counterpart in the reference), on device pointers and `stream`,
+ * without synchronisation. Gradients follow the convention dL/dRe + i dL/dIm for complex
+ * quantities. adjoint_backward maps the gradient of the space domain to the gradient of the
+ * frequency values: for C2C the unnormalised forward transform and its gather (the transpose of
+ * the backward scatter); for R2C the same times each value's hermitian multiplicity (2, or 1 for
+ * self-conjugate frequencies, the x Nyquist plane and the y Nyquist row of the x = 0 plane).
+ * adjoint_forward maps the gradient of the frequency values to the gradient of the space domain
+ * (the backward transform of the value gradient divided by those multiplicities, scaled like the
+ * forward). The R2C adjoints assume each hermitian pair is given once, as the reference's R2C
+ * index rules describe. */
+SPFFT_EXPORT SpfftError spfft_gb300_transform_adjoint_backward(SpfftTransform transform,
+                                                               const double* gradSpace,
+                                                               double* gradValues, void* stream);
+SPFFT_EXPORT SpfftError spfft_gb300_transform_adjoint_forward(SpfftTransform transform,
+                                                              const double* gradValues,
+                                                              double* gradSpace,
+                                                              SpfftScalingType scaling, void* stream);
+SPFFT_EXPORT SpfftError spfft_gb300_float_transform_adjoint_backward(SpfftFloatTransform transform,
+                                                                     const float* gradSpace,
+                                                                     float* gradValues, void* stream);
+SPFFT_EXPORT SpfftError spfft_gb300_float_transform_adjoint_forward(SpfftFloatTransform transform,
+                                                                    const float* gradValues,
+                                                                    float* gradSpace,
+                                                                    SpfftScalingType scaling,
+                                                                    void* stream);
+
 /* Profiling aid: run one backward (direction 0: input = values, output = space) or forward
  * (direction 1: input = space, output = values) on device pointers and `stream`, with CUDA events
  * around each of the three kernels of the pass; waits and writes the three kernel times (ms) to

@@ -131,6 +131,8 @@ def _declare(lib: ctypes.CDLL) -> None:
         getattr(lib, prefix + "transform_backward_device").argtypes = [_vp, _vp, _vp, _vp]
         getattr(lib, prefix + "transform_forward_device").argtypes = [_vp, _vp, _vp, _i, _vp]
         getattr(lib, prefix + "transform_path_info").argtypes = [_vp, _ip]
+        getattr(lib, prefix + "transform_adjoint_backward").argtypes = [_vp, _vp, _vp, _vp]
+        getattr(lib, prefix + "transform_adjoint_forward").argtypes = [_vp, _vp, _vp, _i, _vp]
         getattr(lib, prefix + "transform_stage_times").argtypes = [_vp, _i, _vp, _vp, _i, _vp,
                                                                    ctypes.POINTER(ctypes.c_float)]
     lib.spfft_gb300_plan_indices.argtypes = [_i, _i, _i, _i, _i, _vp, _vp, _vp, _i, _ip, _ip]
@@ -359,6 +361,17 @@ class Transform:
         """Run every later call on this CUDA stream (torch.cuda.Stream, cudaStream_t int or None)."""
         ptr = None if stream is None else int(getattr(stream, "cuda_stream", stream))
         _call("spfft_gb300_" + self._p[len("spfft_"):] + "transform_set_stream", self._h, ptr)
+
+    def adjoint_backward(self, grad_space: Any, grad_values: Any, stream: Any = None) -> None:
+        """Gradient of the frequency values from the gradient of the space domain."""
+        _call("spfft_gb300_" + self._p[len("spfft_"):] + "transform_adjoint_backward", self._h,
+              address(grad_space), address(grad_values), _stream_handle(stream))
+
+    def adjoint_forward(self, grad_values: Any, grad_space: Any, scaling: int = SPFFT_NO_SCALING,
+                        stream: Any = None) -> None:
+        """Gradient of the space domain from the gradient of the frequency values."""
+        _call("spfft_gb300_" + self._p[len("spfft_"):] + "transform_adjoint_forward", self._h,
+              address(grad_values), address(grad_space), scaling, _stream_handle(stream))
 
     def backward_device(self, values: Any, space: Any, stream: Any = None) -> None:
         s = None if stream is None else int(getattr(stream, "cuda_stream", stream))

@@ -220,6 +220,21 @@ SPFFT_GB300_GRID_C_API(spfft_float_grid_, GridFloat)
                                                  static_cast<cudaStream_t>(stream), stageMs);     \
     });                                                                                           \
   }                                                                                               \
+  SpfftError GPREFIX##adjoint_backward(void* transform, const T* gradSpace, T* gradValues,        \
+                                       void* stream) {                                            \
+    return with_handle<spfft::TRANSFORM>(transform, [&](spfft::TRANSFORM& t) {                    \
+      spfft::TransformAccess::get(t).adjoint_backward_device(gradSpace, gradValues,               \
+                                                             static_cast<cudaStream_t>(stream));  \
+    });                                                                                           \
+  }                                                                                               \
+  SpfftError GPREFIX##adjoint_forward(void* transform, const T* gradValues, T* gradSpace,         \
+                                      SpfftScalingType scaling, void* stream) {                   \
+    return with_handle<spfft::TRANSFORM>(transform, [&](spfft::TRANSFORM& t) {                    \
+      spfft::TransformAccess::get(t).adjoint_forward_device(gradValues, gradSpace,                \
+                                                            scaling == SPFFT_FULL_SCALING,        \
+                                                            static_cast<cudaStream_t>(stream));   \
+    });                                                                                           \
+  }                                                                                               \
   SpfftError GPREFIX##path_info(void* transform, int* flags) {                                    \
     return with_handle<spfft::TRANSFORM>(transform, [&](spfft::TRANSFORM& t) {                    \
       *flags = spfft::TransformAccess::get(t).path_flags();                                       \

@@ -134,6 +134,7 @@ GpuPlan<T>::GpuPlan(const IndexPlan& p, int device) {
       {p.entryPos.data(), p.entryPos.size() * sizeof(int), 0},
       {p.entryUser.data(), p.entryUser.size() * sizeof(int), 0},
       {p.stickEntryStart.data(), p.stickEntryStart.size() * sizeof(int), 0},
+      {p.hermitianWeight.data(), p.hermitianWeight.size(), 0},
   };
   size_t total = 0;
   for (auto& part : parts) {
@@ -260,6 +261,9 @@ GpuPlan<T>::GpuPlan(const IndexPlan& p, int device) {
   base_.entryPos = reinterpret_cast<const int*>(d + parts[7].offset);
   base_.entryUser = reinterpret_cast<const int*>(d + parts[8].offset);
   base_.stickEntryStart = reinterpret_cast<const int*>(d + parts[9].offset);
+  base_.hermitianWeight =
+      p.hermitianWeight.empty() ? nullptr : reinterpret_cast<const unsigned char*>(d + parts[10].offset);
+  numValues_ = nv;
 
   // Forward scaling factor T(1 / (Nx Ny Nz)) computed in double (execution_gpu.cpp:58-59).
   scale_ = static_cast<T>(1.0 / (static_cast<double>(p.dimX) * p.dimY * p.dimZ));
@@ -334,6 +338,33 @@ void GpuPlan<T>::backward(const T* values, T* space, void* scratch, cudaStream_t
     check_launch(launch_generic<T>(GenericPass::XBackward, v, config_, nullptr, space, T(0), stream));
   }
   mark(events, 3, stream);
+}
+
+// Adjoint of backward: the unnormalised forward transform with its gather (the transpose of the
+// backward's scatter), times the hermitian multiplicity of each R2C value.
+template <typename T>
+void GpuPlan<T>::adjoint_backward(const T* gradSpace, T* gradValues, void* scratch, cudaStream_t stream) const {
+  forward(gradSpace, gradValues, false, scratch, stream);
+  if (base_.hermitianWeight) {
+    check_launch(launch_weight_values<T>(gradValues, gradValues, base_.hermitianWeight, numValues_, T(1), 0,
+                                         stream));
+  }
+}
+
+// Adjoint of forward: the backward transform of the value gradient, divided by the R2C
+// multiplicities (the backward's implied mirror terms must not be counted twice) and scaled like
+// the forward.
+template <typename T>
+void GpuPlan<T>::adjoint_forward(const T* gradValues, T* gradSpace, bool scaled, void* scratch,
+                                 cudaStream_t stream) const {
+  const T* in = gradValues;
+  if (base_.hermitianWeight || scaled) {
+    T* st = staging(scratch);
+    check_launch(launch_weight_values<T>(gradValues, st, base_.hermitianWeight, numValues_,
+                                         scaled ? scale_ : T(1), 1, stream));
+    in = st;
+  }
+  backward(in, gradSpace, scratch, stream);
 }
 
 template <typename T>

@@ -34,6 +34,12 @@ public:
   void forward(const T* space, T* values, bool scaled, void* scratch, cudaStream_t stream,
                const StageEvents* events = nullptr) const;
 
+  // Adjoints (with respect to the real inner product Re <a, b>): of backward (space gradient ->
+  // value gradient) and of forward (value gradient -> space gradient).
+  void adjoint_backward(const T* gradSpace, T* gradValues, void* scratch, cudaStream_t stream) const;
+  void adjoint_forward(const T* gradValues, T* gradSpace, bool scaled, void* scratch,
+                       cudaStream_t stream) const;
+
   // How the y and x passes run: generic kernels, one fused specialised kernel per plane, or
   // specialised y and x kernels over column / row groups with the compact plane in HBM.
   enum class PlanePath { Generic, Fused, Split };
@@ -64,6 +70,7 @@ private:
   int fastSpb_ = 0, fastRows_ = 0, splitCpb_ = 0, splitRpb_ = 0;
   ScratchLayout layout_{};
   T scale_ = T(1);
+  int numValues_ = 0;
   DeviceBuffer tables_;
 };
 

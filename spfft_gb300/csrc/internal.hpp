@@ -104,6 +104,15 @@ public:
   // Kernel-only entry points on device pointers, on the stream the caller gives.
   void backward_device(const T* values, T* space, cudaStream_t stream);
   void forward_device(const T* space, T* values, bool scaled, cudaStream_t stream);
+  // Adjoint passes on device pointers (see GpuPlan::adjoint_backward / adjoint_forward).
+  void adjoint_backward_device(const T* gradSpace, T* gradValues, cudaStream_t stream) {
+    gb300::DeviceGuard guard(grid_->device_id());
+    gpu_->adjoint_backward(gradSpace, gradValues, grid_->scratch(), stream);
+  }
+  void adjoint_forward_device(const T* gradValues, T* gradSpace, bool scaled, cudaStream_t stream) {
+    gb300::DeviceGuard guard(grid_->device_id());
+    gpu_->adjoint_forward(gradValues, gradSpace, scaled, grid_->scratch(), stream);
+  }
   // One pass in `direction` (0 backward, 1 forward) on device pointers with events between the
   // three kernels; waits for completion and returns the kernel times in milliseconds.
   void stage_times(int direction, const T* in, T* out, bool scaled, cudaStream_t stream,

@@ -33,6 +33,7 @@ struct PlanView {
   const int* entryPos;
   const int* entryUser;
   const int* stickEntryStart;
+  const unsigned char* hermitianWeight;  // R2C: per user value, 1 or 2; null for C2C
   T* sticks;
   T* planes;
 };
@@ -73,6 +74,12 @@ enum class GenericPass { ZBackward, YBackward, XBackward, XForward, YForward, ZF
 template <typename T>
 cudaError_t launch_generic(GenericPass pass, const PlanView<T>& p, const LaunchConfig& c,
                            const T* in, T* out, T scale, cudaStream_t stream);
+// out[i] = in[i] * factor * w_i (divide = 0) or in[i] * factor / w_i (divide = 1) for the n complex
+// values, with w_i = weight[i] (1 when weight is null). In place allowed.
+template <typename T>
+cudaError_t launch_weight_values(const T* in, T* out, const unsigned char* weight, int n, T factor,
+                                 int divide, cudaStream_t stream);
+
 // One-time per-process attribute setup (dynamic shared memory limits).
 template <typename T>
 cudaError_t prepare_kernels(size_t maxSmem);

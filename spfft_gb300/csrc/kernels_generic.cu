@@ -296,7 +296,31 @@ __global__ void z_forward_kernel(const PlanView<T> p, T* __restrict__ values, T 
   }
 }
 
+template <typename T>
+__global__ void weight_values_kernel(const T* __restrict__ in, T* out, const unsigned char* __restrict__ w,
+                                     int n, T factor, int divide) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    T f = factor;
+    if (w) f = divide ? factor / T(w[i]) : factor * T(w[i]);
+    out[2 * i] = in[2 * i] * f;
+    out[2 * i + 1] = in[2 * i + 1] * f;
+  }
+}
+
 }  // namespace
+
+template <typename T>
+cudaError_t launch_weight_values(const T* in, T* out, const unsigned char* weight, int n, T factor,
+                                 int divide, cudaStream_t stream) {
+  if (n <= 0) return cudaSuccess;
+  const int blocks = (n + 255) / 256 < 4 * 152 ? (n + 255) / 256 : 4 * 152;
+  weight_values_kernel<T><<<blocks, 256, 0, stream>>>(in, out, weight, n, factor, divide);
+  return cudaGetLastError();
+}
+template cudaError_t launch_weight_values<double>(const double*, double*, const unsigned char*, int,
+                                                  double, int, cudaStream_t);
+template cudaError_t launch_weight_values<float>(const float*, float*, const unsigned char*, int, float,
+                                                 int, cudaStream_t);
 
 template <typename T>
 cudaError_t prepare_kernels(size_t maxSmem) {

@@ -118,6 +118,20 @@ IndexPlan make_index_plan(SpfftTransformType type, int dimX, int dimY, int dimZ,
     p.entryPos[e] = p.valueIndices[order[e]];
     if (order[e] != e) p.identityOrder = false;
   }
+  if (hermitian) {
+    auto nyquist = [](int n, int v) { return n % 2 == 0 && v == n / 2; };
+    p.hermitianWeight.resize(numValues);
+    for (int i = 0; i < numValues; ++i) {
+      const int x = storage_index(dimX, triplets[3 * i]), y = storage_index(dimY, triplets[3 * i + 1]),
+                z = storage_index(dimZ, triplets[3 * i + 2]);
+      unsigned char m;
+      if (x != 0) m = nyquist(dimX, x) ? 1 : 2;
+      else if (y != 0) m = nyquist(dimY, y) ? 1 : 2;
+      else m = (z != 0 && !nyquist(dimZ, z)) ? 2 : 1;
+      p.hermitianWeight[i] = m;
+    }
+  }
+
   p.stickEntryStart.assign(numSticks + 1, 0);
   for (int e = 0; e < numValues; ++e) ++p.stickEntryStart[p.entryPos[e] / dimZ + 1];
   for (int s = 0; s < numSticks; ++s) p.stickEntryStart[s + 1] += p.stickEntryStart[s];

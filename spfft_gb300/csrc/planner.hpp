@@ -48,6 +48,11 @@ struct IndexPlan {
   std::vector<int> stickEntryStart;
   // True when entryUser[e] == e for every e (values already in stick order).
   bool identityOrder = true;
+  // R2C only, per user value: how many times the value enters the real space field (1 or 2),
+  // counting the hermitian mirror that the C2R convention and the stick / plane symmetry fills
+  // imply. 2 unless the frequency is self-conjugate, on the x Nyquist plane, or on the y Nyquist
+  // row of the x = 0 plane (where the plane fill conjugates in place). Used by the adjoints.
+  std::vector<unsigned char> hermitianWeight;
 
   int num_sticks() const { return static_cast<int>(stickKeys.size()); }
   int num_columns() const { return static_cast<int>(columnX.size()); }
