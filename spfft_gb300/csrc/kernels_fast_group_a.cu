@@ -1,5 +1,5 @@
-// Specialised kernels for one group of FFT lengths (cubic grids; every length is even so the
-// R2C/C2R half-length path applies).
+// Specialised kernels (single, split and batched) for one group of FFT lengths; every length is
+// even, so the R2C/C2R half-length path applies.
 #define SPFFT_GB300_GROUP fast_group_a
-#define SPFFT_GB300_SIZES(X) X(12) X(48) X(60) X(64) X(72)
+#define SPFFT_GB300_SIZES(X) X(12) X(48)
 #include "kernels_fast_group.inc"

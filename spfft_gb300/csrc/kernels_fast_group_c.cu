@@ -1,5 +1,5 @@
-// Specialised kernels for one group of FFT lengths (cubic grids; every length is even so the
-// R2C/C2R half-length path applies).
+// Specialised kernels (single, split and batched) for one group of FFT lengths; every length is
+// even, so the R2C/C2R half-length path applies.
 #define SPFFT_GB300_GROUP fast_group_c
-#define SPFFT_GB300_SIZES(X) X(120) X(128) X(150)
+#define SPFFT_GB300_SIZES(X) X(72) X(90)
 #include "kernels_fast_group.inc"
