@@ -290,7 +290,25 @@ def measure_gpu(args, rank: int, world: int) -> dict:
     e2e_s = time.perf_counter() - t0
     e2e = {"value": round(e2e_steps / e2e_s * world, 3), "unit": UNIT,
            "h2d_bytes_per_step": int(hv.numel() * hv.element_size() + hspace.numel() * hspace.element_size()),
-           "d2h_bytes_per_step": int(hspace.numel() * hspace.element_size() + hout.numel() * hout.element_size())}
+           "d2h_bytes_per_step": int(hspace.numel() * hspace.element_size() + hout.numel() * hout.element_size()),
+           "host_access": os.environ.get("SPFFT_GB300_HOST_ACCESS", "direct"),
+           "buffers": "pinned host (torch pin_memory), synchronous calls"}
+    # the same pair with the reference's staged copies, for comparison
+    if os.environ.get("SPFFT_GB300_HOST_ACCESS", "direct") != "copy":
+        os.environ["SPFFT_GB300_HOST_ACCESS"] = "copy"
+        tr2 = sp.Transform(1, sp.SPFFT_PU_GPU, ttype, n, n, n, npts, sp.SPFFT_INDEX_TRIPLETS, idx, dtype=dtype)
+        del os.environ["SPFFT_GB300_HOST_ACCESS"]
+        for _ in range(max(1, args.warmup)):
+            tr2.backward(hv, hspace)
+            tr2.forward(hspace, hout)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            tr2.backward(hv, hspace)
+            tr2.forward(hspace, hout)
+        torch.cuda.synchronize()
+        e2e["staged_copies_value"] = round(e2e_steps / (time.perf_counter() - t0) * world, 3)
+        del tr2
 
     # correctness guard on the timed output: forward(backward(v)) = N * v on C2C, and on R2C for
     # the values that are not on the x = 0 plane (those are folded by the hermitian fill)

@@ -1,6 +1,8 @@
 // GridInternal / TransformInternal implementation.
 #include "internal.hpp"
 
+#include <cstdlib>
+#include <cstring>
 #include <thread>
 
 namespace spfft {
@@ -97,6 +99,10 @@ TransformInternal<T>::TransformInternal(SpfftProcessingUnitType processingUnit,
   stream_.reset(new gb300::Stream());
   startEvent_.reset(new gb300::Event());
   endEvent_.reset(new gb300::Event());
+  // SPFFT_GB300_HOST_ACCESS=copy restores the reference's staged host <-> device copies for pinned
+  // host buffers; by default kernels read and write them directly.
+  const char* access = std::getenv("SPFFT_GB300_HOST_ACCESS");
+  directHost_ = !(access && std::strcmp(access, "copy") == 0);
 }
 
 template <typename T>
@@ -150,6 +156,15 @@ void TransformInternal<T>::backward_enqueue(const T* input, T* output) {
   cudaStream_t s = begin();
   auto in = gb300::split_pointer(input);
   auto out = gb300::split_pointer(output);
+  if (directHost_) {
+    // pinned host buffers: let the kernels read / write them over the coherent host link
+    if (in.first) {
+      if (const T* d = gb300::mapped_host_alias(in.first)) in = {nullptr, d};
+    }
+    if (out.first) {
+      if (T* d = gb300::mapped_host_alias(out.first)) out = {nullptr, d};
+    }
+  }
   void* scratch = grid_->scratch();
   const T* values = in.second;
   if (in.first) {
@@ -173,6 +188,14 @@ void TransformInternal<T>::forward_enqueue(const T* input, T* output, SpfftScali
   cudaStream_t s = begin();
   auto in = gb300::split_pointer(input);
   auto out = gb300::split_pointer(output);
+  if (directHost_) {
+    if (in.first) {
+      if (const T* d = gb300::mapped_host_alias(in.first)) in = {nullptr, d};
+    }
+    if (out.first) {
+      if (T* d = gb300::mapped_host_alias(out.first)) out = {nullptr, d};
+    }
+  }
   void* scratch = grid_->scratch();
   const T* space = in.second;
   if (in.first) {

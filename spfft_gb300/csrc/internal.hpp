@@ -132,6 +132,7 @@ private:
   std::unique_ptr<gb300::Event> startEvent_, endEvent_;
   cudaStream_t userStream_ = nullptr;
   bool hasUserStream_ = false;
+  bool directHost_ = true;  // kernels access pinned host buffers directly (else: staged copies)
 };
 
 extern template class GridInternal<double>;

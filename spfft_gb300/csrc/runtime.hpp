@@ -170,5 +170,20 @@ inline std::pair<T*, T*> split_pointer(T* p) {
   return {attr.hostPointer ? static_cast<T*>(attr.hostPointer) : p, nullptr};
 }
 
+// Device-accessible alias of pinned (page-locked, mapped) host memory, or nullptr for any other
+// pointer. On GB300 the Grace host memory sits behind the coherent NVLink-C2C link, so kernels can
+// read and write such buffers directly instead of staging them through device memory.
+template <typename T>
+inline T* mapped_host_alias(T* p) {
+  if (!p) return nullptr;
+  cudaPointerAttributes attr{};
+  if (cudaPointerGetAttributes(&attr, static_cast<const void*>(p)) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return nullptr;
+  }
+  if (attr.type != cudaMemoryTypeHost || !attr.devicePointer) return nullptr;
+  return static_cast<T*>(attr.devicePointer);
+}
+
 }  // namespace gb300
 }  // namespace spfft

@@ -321,3 +321,35 @@ def test_plane_strategies_agree(lib, plane, dtype, monkeypatch):
         f = torch.empty(len(idx), dtype=CT[dtype], device="cuda")
         tr.forward(out, f)
         assert rel_l2(f.cpu().numpy(), oracle.forward(out.cpu().numpy().astype(np.complex128 if ttype == 0 else np.float64))) <= TOL[dtype]
+
+
+@pytest.mark.parametrize("access", ["direct", "copy"])
+@pytest.mark.parametrize("dtype", ["float64", "float32"])
+def test_pinned_host_buffers(lib, access, dtype, monkeypatch):
+    """Pinned host buffers: kernels read / write them directly over the host link (default) or
+    through staged copies (SPFFT_GB300_HOST_ACCESS=copy); same results either way, including
+    in-place calls."""
+    monkeypatch.setenv("SPFFT_GB300_HOST_ACCESS", access)
+    rng = np.random.default_rng(21)
+    for n, radius, ttype in [(48, 12, 1), (64, 16, 0), (13, 4, 0)]:
+        idx = sphere_indices(n, radius, r2c=(ttype == 1))
+        tr = _transform(dtype, ttype, (n, n, n), idx)
+        oracle = pipeline.HostPipeline(ttype, n, n, n, idx)
+        vals = _values(rng, len(idx))
+        if ttype == 1:
+            vals[(idx == 0).all(axis=1)] = vals[(idx == 0).all(axis=1)].real
+        hv = torch.from_numpy(vals).to(CT[dtype]).pin_memory()
+        st = CT[dtype] if ttype == 0 else RT[dtype]
+        hs = torch.empty((n, n, n), dtype=st).pin_memory()
+        tr.backward(hv, hs)
+        want = oracle.backward(vals)
+        assert rel_l2(hs.numpy(), want) <= TOL[dtype], (n, access)
+        hf = torch.empty_like(hv)
+        tr.forward(hs, hf, sp.SPFFT_FULL_SCALING)
+        assert rel_l2(hf.numpy(), oracle.forward(hs.numpy().astype(np.float64 if ttype else np.complex128),
+                                                   scaled=True)) <= TOL[dtype]
+        if ttype == 0:  # in place through one pinned buffer
+            buf = torch.zeros((n, n, n), dtype=st).pin_memory()
+            buf.view(-1)[: len(idx)] = torch.from_numpy(vals).to(st)
+            tr.backward(buf, buf)
+            assert rel_l2(buf.numpy(), want) <= TOL[dtype]
