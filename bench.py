@@ -38,13 +38,34 @@ UNIT = "pairs/s"
 # workload
 # ---------------------------------------------------------------------------------------------
 def sphere_indices(n: int, radius: float, r2c: bool) -> np.ndarray:
+    """Centered triplets with x^2 + y^2 + z^2 <= radius^2 on an n^3 grid, in z-stick order (x, y, z
+    ascending). R2C keeps x > 0, plus x = 0 with y > 0 or (y = 0, z >= 0). Built column by column:
+    the z range of each (x, y) column comes from an integer-corrected square root."""
     lo, hi = n // 2 - n + 1, n // 2
-    r = np.arange(lo, hi + 1)
-    x, y, z = np.meshgrid(r, r, r, indexing="ij")
-    m = x * x + y * y + z * z <= radius * radius
+    r = np.arange(lo, hi + 1, dtype=np.int64)
+    x, y = np.meshgrid(r, r, indexing="ij")
+    x, y = x.ravel(), y.ravel()
+    r2 = radius * radius
+    rest = r2 - (x * x + y * y)
+    keep = rest >= 0
     if r2c:
-        m &= (x > 0) | ((x == 0) & ((y > 0) | ((y == 0) & (z >= 0))))
-    return np.ascontiguousarray(np.stack([x[m], y[m], z[m]], axis=1).astype(np.int32))
+        keep &= x >= 0
+    x, y, rest = x[keep], y[keep], rest[keep]
+    zm = np.floor(np.sqrt(np.maximum(rest, 0))).astype(np.int64)
+    zm += ((zm + 1) ** 2 <= rest)  # correct the rounding of the square root both ways
+    zm -= (zm * zm > rest)
+    zlo = np.maximum(-zm, lo)
+    zhi = np.minimum(zm, hi)
+    if r2c:
+        zlo = np.where((x == 0) & (y == 0), 0, zlo)
+        drop = (x == 0) & (y < 0)
+        zhi = np.where(drop, zlo - 1, zhi)
+    cnt = np.maximum(zhi - zlo + 1, 0)
+    total = int(cnt.sum())
+    col = np.repeat(np.arange(len(x)), cnt)
+    start = np.cumsum(cnt) - cnt
+    z = zlo[col] + (np.arange(total) - start[col])
+    return np.ascontiguousarray(np.stack([x[col], y[col], z], axis=1).astype(np.int32))
 
 
 WORKLOADS = {
@@ -53,6 +74,33 @@ WORKLOADS = {
     "c2c_64_sphere16": (64, 16, False),
     "c2c_96_sphere24": (96, 24, False),
 }
+
+
+# Batches of independent transforms: name -> (seed, builder). A builder returns one
+# (n, radius, r2c) triple per transform.
+def _uneven_128(rng):
+    # 256 C2C transforms on 128^3, cutoff radius R ~ U[24, 40] each
+    return [(128, float(r), False) for r in rng.uniform(24.0, 40.0, 256)]
+
+
+def _mixed_512(rng):
+    # 512 transforms on cubic grids from {48, 60, 72, 90, 108, 120, 150, 160}, half C2C and half
+    # R2C, cutoff radius R = U(0.2, 0.3) * n
+    sizes = np.array([48, 60, 72, 90, 108, 120, 150, 160])
+    ns = rng.choice(sizes, 512)
+    fr = rng.uniform(0.2, 0.3, 512)
+    return [(int(n), float(f * n), bool(i % 2)) for i, (n, f) in enumerate(zip(ns, fr))]
+
+
+BATCH_WORKLOADS = {
+    "c2c_128_uneven256": (3, _uneven_128),
+    "mixed_512": (5, _mixed_512),
+}
+
+
+def batch_specs(name: str) -> list:
+    seed, builder = BATCH_WORKLOADS[name]
+    return builder(np.random.default_rng(seed))
 
 
 def make_values(idx: np.ndarray, r2c: bool, seed: int = 1) -> np.ndarray:
@@ -387,13 +435,228 @@ def measure_batched(args, workload: str, batch: int, dtype: str, radii=None) -> 
             "workload": workload, "l2": "batch working set > L2 (no flush)"}
 
 
+def batch_values(idx: np.ndarray, r2c: bool, seed: int) -> np.ndarray:
+    """complex N(0, 1) / sqrt(npts); real at k = 0 for R2C."""
+    rng = np.random.default_rng(seed)
+    v = (rng.standard_normal(len(idx)) + 1j * rng.standard_normal(len(idx))) / np.sqrt(max(1, len(idx)))
+    if r2c:
+        k0 = (idx == 0).all(axis=1)
+        v[k0] = v[k0].real
+    return v
+
+
+def measure_batch_workload(args, rank: int, world: int) -> dict:
+    """A batch of independent transforms (sharded over the ranks, no collective): FP32 pairs/s as
+    one captured graph per step, the FP64 plain drop-in path over the same transforms one by one,
+    the FP32 error against that FP64 path, per-pass roofline, and an end-to-end leg with the
+    frequency values in pinned host memory."""
+    import torch
+
+    import spfft_gb300 as sp
+
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    specs_all = batch_specs(args.workload)
+    mine = list(range(rank, len(specs_all), world))
+    idxs, hosts, geo = [], [], []
+    for j in mine:
+        n, radius, r2c = specs_all[j]
+        idx = sphere_indices(n, radius, r2c)
+        idxs.append(idx)
+        hosts.append(batch_values(idx, r2c, seed=1000 + j))
+        geo.append((n, len(idx), int(np.unique((idx[:, 0] % n) * n + idx[:, 1] % n).size),
+                    int(np.unique(idx[:, 0] % n).size), r2c))
+
+    def make(dtype):
+        ct = torch.complex128 if dtype == "float64" else torch.complex64
+        rt = torch.float64 if dtype == "float64" else torch.float32
+        trs, vals, spaces = [], [], []
+        for j, idx, v in zip(mine, idxs, hosts):
+            n, _, r2c = specs_all[j]
+            ttype = sp.SPFFT_TRANS_R2C if r2c else sp.SPFFT_TRANS_C2C
+            trs.append(sp.Transform(1, sp.SPFFT_PU_GPU, ttype, n, n, n, len(idx), sp.SPFFT_INDEX_TRIPLETS,
+                                    idx, dtype=dtype))
+            vals.append(torch.from_numpy(v).to(ct).cuda())
+            spaces.append(torch.empty((n, n, n), dtype=rt if r2c else ct, device="cuda"))
+        return trs, vals, spaces, ct
+
+    stream = torch.cuda.Stream()
+    # ---- FP32 batched -------------------------------------------------------------------------
+    trs32, vals32, spaces32, ct32 = make("float32")
+    bt = sp.Batch(trs32)
+    bt.bind(vals32, spaces32)
+    for _ in range(args.warmup):
+        bt.pair_graph(sp.SPFFT_FULL_SCALING, stream)
+    torch.cuda.synchronize()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(dev) as clocks:
+        for k in range(args.steps):
+            starts[k].record(stream)
+            bt.pair_graph(sp.SPFFT_FULL_SCALING, stream)
+            ends[k].record(stream)
+        torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    total_ms = sum(a.elapsed_time(b) for a, b in zip(starts, ends))
+    if world > 1:
+        t = torch.tensor([total_ms], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = len(specs_all) * args.steps / (total_ms / 1e3)
+
+    # per-pass roofline (groups run pass by pass for the events)
+    names_b = ["z_backward", "y_backward", "x_backward"]
+    names_f = ["x_forward", "y_forward", "z_forward"]
+    acc = {k: [] for k in names_b + names_f}
+    for _ in range(5):
+        for nm, ms in zip(names_b, bt.stage_times(0, sp.SPFFT_NO_SCALING, stream)):
+            acc[nm].append(ms)
+        for nm, ms in zip(names_f, bt.stage_times(1, sp.SPFFT_FULL_SCALING, stream)):
+            acc[nm].append(ms)
+    pass_ms = {k: statistics.median(v) for k, v in acc.items()}
+    pass_bytes = {k: 0 for k in acc}
+    pair_bytes = 0
+    for (n, npts, nsticks, ncols, r2c) in geo:
+        ab = algorithmic_bytes(n, npts, nsticks, ncols, r2c, 4)
+        for k in pass_bytes:
+            pass_bytes[k] += ab["kernels"][k]
+        pair_bytes += ab["pair"]
+    dominant = max(pass_ms, key=pass_ms.get)
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    achieved = pass_bytes[dominant] / (pass_ms[dominant] * 1e-3) / 1e9
+    roofline = {"bound": "hbm", "kernel": dominant + "_batch", "achieved": round(achieved, 1), "peak": peak,
+                "unit": "GB/s", "frac": round(achieved / peak, 4),
+                "peak_source": "measured" if "hbm_gbs" in peaks else "fallback",
+                "traffic": load_traffic_table().get((dominant + "_batch", args.workload, "float32")),
+                "algorithmic_bytes": pass_bytes[dominant],
+                "pass_ms": {k: round(v, 4) for k, v in pass_ms.items()},
+                "pass_gbs": {k: round(pass_bytes[k] / (pass_ms[k] * 1e-3) / 1e9, 1) for k in pass_ms}}
+
+    # ---- end to end: values from / to pinned host memory around the captured pair ---------------
+    hv = [torch.from_numpy(v).to(ct32).pin_memory() for v in hosts]
+    ho = [torch.empty_like(h).pin_memory() for h in hv]
+    e2e_steps = max(3, args.steps)
+
+    def e2e_step():
+        with torch.cuda.stream(stream):
+            for d, h in zip(vals32, hv):
+                d.copy_(h, non_blocking=True)
+            bt.pair_graph(sp.SPFFT_FULL_SCALING, stream)
+            for h, d in zip(ho, vals32):
+                h.copy_(d, non_blocking=True)
+        stream.synchronize()
+
+    for _ in range(2):
+        e2e_step()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        e2e_step()
+    e2e_s = time.perf_counter() - t0
+    vbytes = int(sum(h.numel() * h.element_size() for h in hv))
+    e2e = {"value": round(len(specs_all) * e2e_steps / e2e_s, 2), "unit": UNIT,
+           "h2d_bytes_per_step": vbytes * world, "d2h_bytes_per_step": vbytes * world,
+           "buffers": "frequency values in pinned host memory, space domains on the device"}
+
+    # ---- FP32 error against the FP64 drop-in path on a sample ----------------------------------
+    trs64, vals64, spaces64, ct64 = make("float64")
+    for d, h in zip(vals32, hosts):
+        d.copy_(torch.from_numpy(h).to(ct32))
+    bt.backward(stream)
+    stream.synchronize()
+    sample = sorted(set(list(range(min(4, len(mine)))) + list(range(max(0, len(mine) - 4), len(mine)))))
+    errs_b, errs_f = [], []
+    out32 = [torch.empty_like(vals32[i]) for i in range(len(mine))]
+    for i in sample:
+        trs64[i].backward(vals64[i], spaces64[i])
+        errs_b.append(float(torch.linalg.vector_norm((spaces32[i].to(spaces64[i].dtype) - spaces64[i]).flatten())
+                            / torch.linalg.vector_norm(spaces64[i].flatten())))
+        f64 = torch.empty_like(vals64[i])
+        trs64[i].forward(spaces64[i], f64, sp.SPFFT_FULL_SCALING)
+        trs32[i].forward(spaces32[i], out32[i], sp.SPFFT_FULL_SCALING)
+        errs_f.append(float(torch.linalg.vector_norm((out32[i].to(ct64) - f64).flatten())
+                            / torch.linalg.vector_norm(f64.flatten())))
+
+    # ---- FP64 plain: the drop-in API, one transform after another ------------------------------
+    for t in trs64:
+        t.set_stream(stream)
+        t.set_execution_mode(sp.SPFFT_EXEC_ASYNCHRONOUS)
+
+    def plain_step():
+        for t, v, sp_ in zip(trs64, vals64, spaces64):
+            t.backward(v, sp_)
+            t.forward(sp_, v, sp.SPFFT_FULL_SCALING)
+
+    with torch.cuda.stream(stream):
+        plain_step()
+    torch.cuda.synchronize()
+    psteps = max(3, min(args.steps, 10))
+    a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a0.record(stream)
+    with torch.cuda.stream(stream):
+        for _ in range(psteps):
+            plain_step()
+    a1.record(stream)
+    torch.cuda.synchronize()
+    plain = len(mine) * psteps / (a0.elapsed_time(a1) / 1e3) * world
+    info = bt.info()
+    del trs64, vals64, spaces64
+    return {"value": value, "ms_per_step": total_ms / args.steps, "clocks": clocks.summary(),
+            "roofline": roofline, "e2e": e2e, "pair_bytes": pair_bytes,
+            "launches_per_step": info["launches_per_pair"], "groups": info["groups"],
+            "unbatched": info["unbatched"], "fp64_plain": plain,
+            "err_backward": max(errs_b), "err_forward": max(errs_f), "sampled": len(sample),
+            "transforms": len(specs_all)}
+
+
+def cpu_batch_pairs_per_s(workload: str, min_seconds: float, max_pairs: int, exact: bool = False,
+                          warmup: int = 1) -> dict:
+    """Pairs/s of the oracle port over the batch's transforms in order (cycling), all host threads."""
+    from oracle import pipeline
+
+    specs = batch_specs(workload)
+    cores = os.cpu_count() or 1
+    cache = {}
+
+    def get(j):
+        if j not in cache:
+            n, radius, r2c = specs[j]
+            idx = sphere_indices(n, radius, r2c)
+            cache[j] = (pipeline.HostPipeline(1 if r2c else 0, n, n, n, idx), batch_values(idx, r2c, 1000 + j))
+        return cache[j]
+
+    # size the sample from one timed pair, then plan every transform of it before timing
+    p, v = get(0)
+    for _ in range(max(1, warmup)):
+        t0 = time.perf_counter()
+        p.forward(p.backward(v, workers=cores), workers=cores)
+        one = time.perf_counter() - t0
+    count = max_pairs if exact else int(max(1, min(max_pairs, min_seconds / max(one, 1e-6))))
+    for j in range(min(count, len(specs))):
+        get(j)
+    t0 = time.perf_counter()
+    for k in range(count):
+        p, v = get(k % len(specs))
+        p.forward(p.backward(v, workers=cores), workers=cores)
+    dt = time.perf_counter() - t0
+    return {"value": count / dt, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"the first {count} FP64 backward+forward pairs of {workload} (numpy/scipy.fft port "
+                      f"of the reference host pipeline, {cores} threads, plans built before timing), {dt:.2f} s"}
+
+
 def main() -> int:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="r2c_192_sphere48")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS) + sorted(BATCH_WORKLOADS),
+                    default="r2c_192_sphere48")
     ap.add_argument("--dtype", choices=["float64", "float32"], default="float64")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -404,6 +667,8 @@ def main() -> int:
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
+    if args.workload in BATCH_WORKLOADS:
+        return batch_main(args, rank, world)
     n, radius, r2c = WORKLOADS[args.workload]
     config = {"workload": args.workload, "grid": [n, n, n], "cutoff_radius": radius,
               "transform": "R2C" if r2c else "C2C", "precision": args.dtype,
@@ -456,6 +721,62 @@ def main() -> int:
         line["fp32_batched"]["ratio_vs_value"] = round(res["batched"]["value"] / res["pairs_per_s"], 2)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_pairs_per_s(args.workload, args.cpu_seconds, 400)
+        line["cpu_baseline"]["value"] = round(line["cpu_baseline"]["value"], 3)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(line))
+    return 0
+
+
+def batch_main(args, rank: int, world: int) -> int:
+    specs = batch_specs(args.workload)
+    sizes = sorted({n for n, _, _ in specs})
+    config = {"workload": args.workload, "transforms": len(specs), "grids": [f"{n}^3" for n in sizes],
+              "transform": "C2C" if not any(r for _, _, r in specs) else "C2C and R2C",
+              "cutoff_radii": [round(min(r for _, r, _ in specs), 2), round(max(r for _, r, _ in specs), 2)],
+              "precision": "float32 batched (one CUDA graph per step); float64 plain alongside",
+              "space_buffer": "external out-of-place, one per transform",
+              "l2": "batch working set > L2 (no flush)", "parallelism": f"transforms sharded x{world}"}
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        res = cpu_batch_pairs_per_s(args.workload, 0.0, args.steps, exact=True, warmup=args.warmup)
+        value = res["value"]
+        print(json.dumps({
+            "impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": UNIT,
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(1e3 / value, 3), "higher_is_better": True, "scaling": "strong",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config,
+            "cpu_baseline": {**res, "value": round(value, 3)},
+            "e2e": {"value": round(value, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "reference CPU path: the oracle port, one transform of the batch per step"}))
+        return 0
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        dist.init_process_group("nccl")
+    from spfft_gb300 import build as _b
+    _b.build()
+    res = measure_batch_workload(args, rank, world)
+    line = {
+        "metric": METRIC, "value": round(res["value"], 2), "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(res["ms_per_step"], 4),
+        "higher_is_better": True, "scaling": "strong", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic", "config": config, "roofline": res["roofline"],
+        "hbm_gbs_per_pair_accounting": round(res["pair_bytes"] * res["value"] / world / 1e9, 1),
+        "e2e": res["e2e"], "clocks": res["clocks"],
+        "gpu_launches": res["launches_per_step"] * args.steps,
+        "shape_groups": res["groups"], "unbatched_transforms": res["unbatched"],
+        "fp64_plain": {"value": round(res["fp64_plain"], 2), "unit": UNIT,
+                       "ratio_fp32_batched_vs_fp64_plain": round(res["value"] / res["fp64_plain"], 2)},
+        "fp32_vs_fp64_rel_l2_max": {"backward_space": res["err_backward"], "forward_values": res["err_forward"],
+                                    "transforms_checked": res["sampled"]},
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_batch_pairs_per_s(args.workload, args.cpu_seconds, 2000)
         line["cpu_baseline"]["value"] = round(line["cpu_baseline"]["value"], 3)
     if world > 1:
         import torch.distributed as dist

@@ -103,9 +103,10 @@ SPFFT_EXPORT SpfftError spfft_gb300_float_transform_path_info(SpfftFloatTransfor
 /* ---- batched execution (no counterpart in the reference; the GB300 form of its multi-transform)
  * A batch holds many transforms (all double or all float, on distinct grids, same device). Each
  * pass of each group of equally shaped transforms runs as ONE kernel launch over all of them, so
- * small transforms fill the GPU. Buffers are bound once; a backward + forward pair can be captured
- * into a CUDA graph on first use and replayed. Transforms whose lengths have no specialised
- * kernels run one by one inside the same calls. */
+ * small transforms fill the GPU; different groups run concurrently on forked streams. Buffers are
+ * bound once; a backward + forward pair can be captured into a CUDA graph on first use and
+ * replayed. Transforms whose lengths have no specialised kernels run one by one inside the same
+ * calls. */
 typedef void* SpfftGb300Batch;
 SPFFT_EXPORT SpfftError spfft_gb300_batch_create(SpfftGb300Batch* batch, int numTransforms,
                                                  const SpfftTransform* transforms);
@@ -113,19 +114,34 @@ SPFFT_EXPORT SpfftError spfft_gb300_float_batch_create(SpfftGb300Batch* batch, i
                                                        const SpfftFloatTransform* transforms);
 SPFFT_EXPORT SpfftError spfft_gb300_batch_destroy(SpfftGb300Batch batch);
 /* values[i]: device interleaved-complex frequency values of transform i; spaces[i]: its device
- * space domain. Pointers must be aligned to the complex size (16 bytes double, 8 bytes float). */
+ * space domain. Pointers must be aligned to the complex size (16 bytes double, 8 bytes float).
+ * Synchronous: call it while no work of the batch is in flight. Captured graphs stay valid. */
 SPFFT_EXPORT SpfftError spfft_gb300_batch_bind(SpfftGb300Batch batch, void* const* values,
                                                void* const* spaces);
 SPFFT_EXPORT SpfftError spfft_gb300_batch_backward(SpfftGb300Batch batch, void* stream);
 SPFFT_EXPORT SpfftError spfft_gb300_batch_forward(SpfftGb300Batch batch, SpfftScalingType scaling,
                                                   void* stream);
 /* Backward then forward of every transform as one CUDA graph on `stream` (not the default
- * stream). The graph is captured on the first call for each scaling and replayed afterwards;
- * rebinding buffers drops it. */
+ * stream). The graph is captured on the first call for each scaling and replayed afterwards; it
+ * reads the bound pointers from a device table, so it follows later rebinds. */
 SPFFT_EXPORT SpfftError spfft_gb300_batch_pair_graph(SpfftGb300Batch batch, SpfftScalingType scaling,
                                                      void* stream);
 SPFFT_EXPORT SpfftError spfft_gb300_batch_info(SpfftGb300Batch batch, int* numGroups,
                                                int* numUnbatched, int* launchesPerPair);
+/* One direction (0 backward, 1 forward) of the bound batch with the groups run pass by pass on
+ * `stream` and events between the three passes (z, y, x in backward order); waits and writes the
+ * pass times in milliseconds to stageMs[3]. For profiling: ordinary calls run groups concurrently. */
+SPFFT_EXPORT SpfftError spfft_gb300_batch_stage_times(SpfftGb300Batch batch, int direction,
+                                                      SpfftScalingType scaling, void* stream,
+                                                      float* stageMs);
+
+/* Multi-transform calls (spfft_multi_transform_* and spfft_float_multi_transform_*) run as one
+ * batched execution (the batch above, built and cached by the library, its graphs replayed) when
+ * the call has at least two transforms, all on one device, none with a stream set by
+ * spfft_gb300_*transform_set_stream, every buffer device memory or pinned host memory, complex-
+ * aligned, and one scaling for all forwards. Otherwise the transforms run one by one. This counts
+ * the calls so far that ran batched (process-wide). */
+SPFFT_EXPORT SpfftError spfft_gb300_multi_batched_calls(long long* count);
 
 /* Allocation-free backward transform (no counterpart in the reference). Runs the backward transform
  * of an existing double-precision transform on device pointers (values: interleaved complex

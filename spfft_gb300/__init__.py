@@ -144,6 +144,8 @@ def _declare(lib: ctypes.CDLL) -> None:
     lib.spfft_gb300_batch_forward.argtypes = [_vp, _i, _vp]
     lib.spfft_gb300_batch_pair_graph.argtypes = [_vp, _i, _vp]
     lib.spfft_gb300_batch_info.argtypes = [_vp, _ip, _ip, _ip]
+    lib.spfft_gb300_multi_batched_calls.argtypes = [ctypes.POINTER(ctypes.c_longlong)]
+    lib.spfft_gb300_batch_stage_times.argtypes = [_vp, _i, _i, _vp, ctypes.POINTER(ctypes.c_float)]
     lib.spfft_gb300_transform_backward_noalloc.argtypes = [_vp, _vp, _vp, _vp]
 
 
@@ -429,6 +431,13 @@ def multi_transform_forward(transforms, inputs, outputs, scalings=None) -> None:
         _call(p + "multi_transform_forward_ptr", n, _handles(transforms), ins, outs, sc)
 
 
+def multi_batched_calls() -> int:
+    """How many multi-transform calls so far ran as one batched execution."""
+    c = ctypes.c_longlong()
+    _call("spfft_gb300_multi_batched_calls", ctypes.byref(c))
+    return int(c.value)
+
+
 def _stream_handle(stream: Any):
     return None if stream is None else int(getattr(stream, "cuda_stream", stream))
 
@@ -473,6 +482,12 @@ class Batch:
 
     def pair_graph(self, scaling: int = SPFFT_NO_SCALING, stream: Any = None) -> None:
         _call("spfft_gb300_batch_pair_graph", self._h, scaling, _stream_handle(stream))
+
+    def stage_times(self, direction: int, scaling: int = SPFFT_NO_SCALING, stream: Any = None) -> list:
+        """Pass times (ms) of one direction, the groups run pass by pass (z, y, x backward order)."""
+        ms = (ctypes.c_float * 3)()
+        _call("spfft_gb300_batch_stage_times", self._h, direction, scaling, _stream_handle(stream), ms)
+        return [float(m) for m in ms]
 
     def info(self) -> dict:
         g, u, l = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()

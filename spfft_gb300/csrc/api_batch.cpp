@@ -4,6 +4,7 @@
 
 #include "access.hpp"
 #include "batch.hpp"
+#include "multi_batch.hpp"
 #include "spfft/spfft_gb300.h"
 #include "spfft/transform.hpp"
 #include "spfft/transform_float.hpp"
@@ -121,6 +122,22 @@ SpfftError spfft_gb300_batch_info(SpfftGb300Batch batch, int* numGroups, int* nu
       if (numUnbatched) *numUnbatched = h.f->num_unbatched();
       if (launchesPerPair) *launchesPerPair = h.f->launches_per_pair();
     }
+  });
+}
+
+SpfftError spfft_gb300_multi_batched_calls(long long* count) {
+  if (!count) return SPFFT_INVALID_PARAMETER_ERROR;
+  *count = spfft::gb300::multi_batched_calls();
+  return SPFFT_SUCCESS;
+}
+
+SpfftError spfft_gb300_batch_stage_times(SpfftGb300Batch batch, int direction, SpfftScalingType scaling,
+                                         void* stream, float* stageMs) {
+  if (!stageMs || (direction != 0 && direction != 1)) return SPFFT_INVALID_PARAMETER_ERROR;
+  return with_batch(batch, [&](BatchHandle& h) {
+    const bool s = scaling == SPFFT_FULL_SCALING;
+    if (h.d) h.d->stage_times(direction, s, static_cast<cudaStream_t>(stream), stageMs);
+    else h.f->stage_times(direction, s, static_cast<cudaStream_t>(stream), stageMs);
   });
 }
 

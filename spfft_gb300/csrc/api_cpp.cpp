@@ -6,6 +6,7 @@
 
 #include "access.hpp"
 #include "internal.hpp"
+#include "multi_batch.hpp"
 #include "planner.hpp"
 #include "spfft/grid.hpp"
 #include "spfft/grid_float.hpp"
@@ -48,7 +49,11 @@ void multi_forward(int n, TransformType* transforms, const ValueType* const* inp
     for (int b = a + 1; b < n; ++b)
       if (TransformAccess::get(transforms[a]).shared_grid(TransformAccess::get(transforms[b])))
         throw InvalidParameterError();
-  // Enqueue every transform before waiting on any (multi_transform_internal.hpp:78-111).
+  // One batched execution when the call qualifies (multi_batch.hpp).
+  std::vector<decltype(TransformAccess::share(transforms[0]))> shared;
+  for (int t = 0; t < n; ++t) shared.push_back(TransformAccess::share(transforms[t]));
+  if (gb300::multi_forward_batched(shared, inputs, outputs, scalings)) return;
+  // Otherwise enqueue every transform before waiting on any (multi_transform_internal.hpp:78-111).
   for (int t = 0; t < n; ++t) {
     auto& ti = TransformAccess::get(transforms[t]);
     gb300::DeviceGuard guard(ti.device_id());
@@ -65,6 +70,9 @@ void multi_backward(int n, TransformType* transforms, const ValueType* const* in
     for (int b = a + 1; b < n; ++b)
       if (TransformAccess::get(transforms[a]).shared_grid(TransformAccess::get(transforms[b])))
         throw InvalidParameterError();
+  std::vector<decltype(TransformAccess::share(transforms[0]))> shared;
+  for (int t = 0; t < n; ++t) shared.push_back(TransformAccess::share(transforms[t]));
+  if (gb300::multi_backward_batched(shared, inputs, outputs)) return;
   for (int t = 0; t < n; ++t) {
     auto& ti = TransformAccess::get(transforms[t]);
     gb300::DeviceGuard guard(ti.device_id());

@@ -46,16 +46,17 @@ struct BatchPlan<T>::Group {
 template <typename T>
 BatchPlan<T>::BatchPlan(std::vector<std::shared_ptr<TransformInternal<T>>> transforms)
     : transforms_(std::move(transforms)) {
-  const int n = static_cast<int>(transforms_.size());
+  const int n = static_cast<int>(tp_.size());
   if (n == 0) throw InvalidParameterError();
   for (auto& t : transforms_) {
     if (!t) throw InvalidParameterError();
+    tp_.push_back(t.get());
   }
-  device_ = transforms_[0]->device_id();
+  device_ = tp_[0]->device_id();
   for (int a = 0; a < n; ++a) {
-    if (transforms_[a]->device_id() != device_) throw InvalidParameterError();
+    if (tp_[a]->device_id() != device_) throw InvalidParameterError();
     for (int b = a + 1; b < n; ++b) {
-      if (transforms_[a]->shared_grid(*transforms_[b])) throw InvalidParameterError();
+      if (tp_[a]->shared_grid(*tp_[b])) throw InvalidParameterError();
     }
   }
   DeviceGuard guard(device_);
@@ -64,7 +65,7 @@ BatchPlan<T>::BatchPlan(std::vector<std::shared_ptr<TransformInternal<T>>> trans
   // group by shape; transforms without specialised kernels for every length run one by one
   std::map<std::tuple<int, int, int, bool>, int> index;
   for (int t = 0; t < n; ++t) {
-    const IndexPlan& ip = transforms_[t]->index_plan();
+    const IndexPlan& ip = tp_[t]->index_plan();
     const bool r2c = ip.type == SPFFT_TRANS_R2C;
     const bool ok = ip.num_sticks() > 0 && fast_prepare<T>(device_, ip.dimX) &&
                     fast_prepare<T>(device_, ip.dimY) && fast_prepare<T>(device_, ip.dimZ);
@@ -92,7 +93,7 @@ BatchPlan<T>::BatchPlan(std::vector<std::shared_ptr<TransformInternal<T>>> trans
   for (auto& gp : groups_) {
     Group& g = *gp;
     int maxCols = 1;
-    for (int t : g.members) maxCols = std::max(maxCols, transforms_[t]->index_plan().num_columns());
+    for (int t : g.members) maxCols = std::max(maxCols, tp_[t]->index_plan().num_columns());
     FastArgs<T> a;
     size_t sm = 0;
     a.smemOut = &sm;
@@ -136,7 +137,7 @@ BatchPlan<T>::BatchPlan(std::vector<std::shared_ptr<TransformInternal<T>>> trans
     g.dev = DeviceBuffer(g.offSpaces + align_up(m * sizeof(T*)));
     std::vector<int> sz(m + 1, 0), sy(m + 1, 0), sx(m + 1, 0);
     for (size_t i = 0; i < m; ++i) {
-      const IndexPlan& ip = transforms_[g.members[i]]->index_plan();
+      const IndexPlan& ip = tp_[g.members[i]]->index_plan();
       sz[i + 1] = sz[i] + (ip.num_sticks() + g.spb - 1) / g.spb;
       sy[i + 1] = sy[i] + ((ip.num_columns() + g.cpb - 1) / g.cpb) * ip.dimZ;
       sx[i + 1] = sx[i] + ((ip.dimY + g.rpb - 1) / g.rpb) * ip.dimZ;
@@ -152,6 +153,14 @@ BatchPlan<T>::BatchPlan(std::vector<std::shared_ptr<TransformInternal<T>>> trans
   }
   groups_ = std::move(kept);
   std::sort(fallback_.begin(), fallback_.end());
+  const size_t branches = groups_.size() + (fallback_.empty() ? 0 : 1);
+  if (branches > 1) {
+    fork_.reset(new Event());
+    for (size_t b = 0; b < branches; ++b) {
+      branchStreams_.emplace_back(new Stream());
+      branchDone_.emplace_back(new Event());
+    }
+  }
   scratchSeen_.assign(n, nullptr);
   values_.assign(n, nullptr);
   spaces_.assign(n, nullptr);
@@ -175,8 +184,8 @@ int BatchPlan<T>::launches_per_pair() const {
 template <typename T>
 void BatchPlan<T>::upload_views() {
   bool changed = false;
-  for (size_t t = 0; t < transforms_.size(); ++t) {
-    void* sc = transforms_[t]->grid().scratch();
+  for (size_t t = 0; t < tp_.size(); ++t) {
+    void* sc = tp_[t]->grid().scratch();
     if (sc != scratchSeen_[t]) changed = true;
     scratchSeen_[t] = sc;
   }
@@ -186,7 +195,7 @@ void BatchPlan<T>::upload_views() {
     Group& g = *gp;
     std::vector<PlanView<T>> views;
     for (int t : g.members) {
-      views.push_back(transforms_[t]->gpu_plan().device_view(transforms_[t]->grid().scratch()));
+      views.push_back(tp_[t]->gpu_plan().device_view(tp_[t]->grid().scratch()));
     }
     check_cuda(cudaMemcpy(static_cast<char*>(g.dev.get()) + g.offViews, views.data(),
                           views.size() * sizeof(PlanView<T>), cudaMemcpyHostToDevice));
@@ -194,15 +203,17 @@ void BatchPlan<T>::upload_views() {
 }
 
 template <typename T>
-void BatchPlan<T>::bind(const T* const* values, T* const* spaces) {
+void BatchPlan<T>::bind(const T* const* values, T* const* spaces, cudaStream_t stream, bool async) {
   if (!values || !spaces) throw InvalidParameterError();
   const uintptr_t c = 2 * sizeof(T);
-  for (size_t t = 0; t < transforms_.size(); ++t) {
+  for (size_t t = 0; t < tp_.size(); ++t) {
     if (!spaces[t] || reinterpret_cast<uintptr_t>(spaces[t]) % c) throw InvalidParameterError();
-    if (transforms_[t]->num_local_elements() > 0 &&
+    if (tp_[t]->num_local_elements() > 0 &&
         (!values[t] || reinterpret_cast<uintptr_t>(values[t]) % c)) {
       throw InvalidParameterError();
     }
+  }
+  for (size_t t = 0; t < tp_.size(); ++t) {
     values_[t] = values[t];
     spaces_[t] = spaces[t];
   }
@@ -215,12 +226,16 @@ void BatchPlan<T>::bind(const T* const* values, T* const* spaces) {
       sp.push_back(spaces_[t]);
     }
     char* d = static_cast<char*>(g.dev.get());
-    check_cuda(cudaMemcpy(d + g.offValues, vp.data(), vp.size() * sizeof(T*), cudaMemcpyHostToDevice));
-    check_cuda(cudaMemcpy(d + g.offSpaces, sp.data(), sp.size() * sizeof(T*), cudaMemcpyHostToDevice));
-  }
-  for (auto& g : graphs_) {
-    if (g) (void)cudaGraphExecDestroy(g);
-    g = nullptr;
+    if (async) {
+      // pageable source: staged by the driver before the call returns, written in stream order
+      check_cuda(cudaMemcpyAsync(d + g.offValues, vp.data(), vp.size() * sizeof(T*), cudaMemcpyHostToDevice,
+                                 stream));
+      check_cuda(cudaMemcpyAsync(d + g.offSpaces, sp.data(), sp.size() * sizeof(T*), cudaMemcpyHostToDevice,
+                                 stream));
+    } else {
+      check_cuda(cudaMemcpy(d + g.offValues, vp.data(), vp.size() * sizeof(T*), cudaMemcpyHostToDevice));
+      check_cuda(cudaMemcpy(d + g.offSpaces, sp.data(), sp.size() * sizeof(T*), cudaMemcpyHostToDevice));
+    }
   }
   bound_ = true;
 }
@@ -247,30 +262,74 @@ void launch(FastOp op, int n, bool r2c, const BatchView<T>& bv, int blocks, size
 }  // namespace
 
 template <typename T>
+void BatchPlan<T>::run_group(Group& g, int what, bool scaled, cudaStream_t s) {
+  char* d = static_cast<char*>(g.dev.get());
+  if (what & 1) {
+    BatchView<T> bz = g.view(g.offStartsZ, T(0));
+    bz.in = reinterpret_cast<const T* const*>(d + g.offValues);
+    launch(FastOp::BatchZBackward, g.nz, g.r2c, bz, g.blocksZ, g.smemZ, g.spb, s);
+    const BatchView<T> by = g.view(g.offStartsY, T(0));
+    launch(FastOp::BatchYBackward, g.ny, g.r2c, by, g.blocksY, g.smemY, g.cpb, s);
+    BatchView<T> bx = g.view(g.offStartsX, T(0));
+    bx.out = reinterpret_cast<T* const*>(d + g.offSpaces);
+    launch(FastOp::BatchXBackward, g.nx, g.r2c, bx, g.blocksX, g.smemX, g.rpb, s);
+  }
+  if (what & 2) {
+    BatchView<T> bx = g.view(g.offStartsX, T(0));
+    bx.in = reinterpret_cast<const T* const*>(d + g.offSpaces);
+    launch(FastOp::BatchXForward, g.nx, g.r2c, bx, g.blocksX, g.smemX, g.rpb, s);
+    const BatchView<T> by = g.view(g.offStartsY, T(0));
+    launch(FastOp::BatchYForward, g.ny, g.r2c, by, g.blocksY, g.smemY, g.cpb, s);
+    BatchView<T> bz = g.view(g.offStartsZ, scaled ? g.scale : T(0));
+    bz.out = reinterpret_cast<T* const*>(d + g.offValues);
+    launch(FastOp::BatchZForward, g.nz, g.r2c, bz, g.blocksZ, g.smemZ, g.spb, s);
+  }
+}
+
+template <typename T>
+void BatchPlan<T>::run_fallback(int what, bool scaled, cudaStream_t s) {
+  for (int t : fallback_) {
+    const GpuPlan<T>& plan = tp_[t]->gpu_plan();
+    void* scratch = tp_[t]->grid().scratch();
+    if (what & 1) plan.backward(values_[t], spaces_[t], scratch, s);
+    if (what & 2) plan.forward(spaces_[t], const_cast<T*>(values_[t]), scaled, scratch, s);
+  }
+}
+
+template <typename T>
+void BatchPlan<T>::run(int what, bool scaled, cudaStream_t stream) {
+  if (!fork_) {
+    for (auto& gp : groups_) run_group(*gp, what, scaled, stream);
+    run_fallback(what, scaled, stream);
+    return;
+  }
+  // fork: every branch starts after the work already on `stream`; join: `stream` continues after
+  // every branch (also while `stream` is being captured into a graph)
+  fork_->record(stream);
+  size_t b = 0;
+  for (auto& gp : groups_) {
+    cudaStream_t s = branchStreams_[b]->get();
+    fork_->wait_on(s);
+    run_group(*gp, what, scaled, s);
+    branchDone_[b]->record(s);
+    ++b;
+  }
+  if (!fallback_.empty()) {
+    cudaStream_t s = branchStreams_[b]->get();
+    fork_->wait_on(s);
+    run_fallback(what, scaled, s);
+    branchDone_[b]->record(s);
+    ++b;
+  }
+  for (size_t i = 0; i < b; ++i) branchDone_[i]->wait_on(stream);
+}
+
+template <typename T>
 void BatchPlan<T>::backward(cudaStream_t stream) {
   check_bound();
   DeviceGuard guard(device_);
   upload_views();
-  for (auto& gp : groups_) {
-    Group& g = *gp;
-    BatchView<T> bv = g.view(g.offStartsZ, T(0));
-    bv.in = reinterpret_cast<const T* const*>(static_cast<char*>(g.dev.get()) + g.offValues);
-    launch(FastOp::BatchZBackward, g.nz, g.r2c, bv, g.blocksZ, g.smemZ, g.spb, stream);
-  }
-  for (auto& gp : groups_) {
-    Group& g = *gp;
-    BatchView<T> bv = g.view(g.offStartsY, T(0));
-    launch(FastOp::BatchYBackward, g.ny, g.r2c, bv, g.blocksY, g.smemY, g.cpb, stream);
-  }
-  for (auto& gp : groups_) {
-    Group& g = *gp;
-    BatchView<T> bv = g.view(g.offStartsX, T(0));
-    bv.out = reinterpret_cast<T* const*>(static_cast<char*>(g.dev.get()) + g.offSpaces);
-    launch(FastOp::BatchXBackward, g.nx, g.r2c, bv, g.blocksX, g.smemX, g.rpb, stream);
-  }
-  for (int t : fallback_) {
-    transforms_[t]->gpu_plan().backward(values_[t], spaces_[t], transforms_[t]->grid().scratch(), stream);
-  }
+  run(1, false, stream);
 }
 
 template <typename T>
@@ -278,60 +337,92 @@ void BatchPlan<T>::forward(bool scaled, cudaStream_t stream) {
   check_bound();
   DeviceGuard guard(device_);
   upload_views();
-  for (auto& gp : groups_) {
-    Group& g = *gp;
-    BatchView<T> bv = g.view(g.offStartsX, T(0));
-    bv.in = reinterpret_cast<const T* const*>(static_cast<char*>(g.dev.get()) + g.offSpaces);
-    launch(FastOp::BatchXForward, g.nx, g.r2c, bv, g.blocksX, g.smemX, g.rpb, stream);
+  run(2, scaled, stream);
+}
+
+template <typename T>
+void BatchPlan<T>::stage_times(int direction, bool scaled, cudaStream_t stream, float ms[3]) {
+  check_bound();
+  DeviceGuard guard(device_);
+  upload_views();
+  StageEvents ev{};
+  for (auto& e : ev.ev) check_cuda(cudaEventCreate(&e));
+  auto pass = [&](FastOp op, int which) {
+    for (auto& gp : groups_) {
+      Group& g = *gp;
+      char* d = static_cast<char*>(g.dev.get());
+      if (which == 0) {
+        BatchView<T> bz = g.view(g.offStartsZ, scaled ? g.scale : T(0));
+        if (op == FastOp::BatchZBackward) bz.in = reinterpret_cast<const T* const*>(d + g.offValues);
+        else bz.out = reinterpret_cast<T* const*>(d + g.offValues);
+        launch(op, g.nz, g.r2c, bz, g.blocksZ, g.smemZ, g.spb, stream);
+      } else if (which == 1) {
+        launch(op, g.ny, g.r2c, g.view(g.offStartsY, T(0)), g.blocksY, g.smemY, g.cpb, stream);
+      } else {
+        BatchView<T> bx = g.view(g.offStartsX, T(0));
+        if (op == FastOp::BatchXBackward) bx.out = reinterpret_cast<T* const*>(d + g.offSpaces);
+        else bx.in = reinterpret_cast<const T* const*>(d + g.offSpaces);
+        launch(op, g.nx, g.r2c, bx, g.blocksX, g.smemX, g.rpb, stream);
+      }
+    }
+  };
+  try {
+    check_cuda(cudaEventRecord(ev.ev[0], stream));
+    if (direction == 0) {
+      pass(FastOp::BatchZBackward, 0);
+      check_cuda(cudaEventRecord(ev.ev[1], stream));
+      pass(FastOp::BatchYBackward, 1);
+      check_cuda(cudaEventRecord(ev.ev[2], stream));
+      pass(FastOp::BatchXBackward, 2);
+      run_fallback(1, scaled, stream);
+    } else {
+      pass(FastOp::BatchXForward, 2);
+      check_cuda(cudaEventRecord(ev.ev[1], stream));
+      pass(FastOp::BatchYForward, 1);
+      check_cuda(cudaEventRecord(ev.ev[2], stream));
+      pass(FastOp::BatchZForward, 0);
+      run_fallback(2, scaled, stream);
+    }
+    check_cuda(cudaEventRecord(ev.ev[3], stream));
+    check_cuda(cudaEventSynchronize(ev.ev[3]));
+    for (int i = 0; i < 3; ++i) check_cuda(cudaEventElapsedTime(&ms[i], ev.ev[i], ev.ev[i + 1]));
+  } catch (...) {
+    for (auto& e : ev.ev) (void)cudaEventDestroy(e);
+    throw;
   }
-  for (auto& gp : groups_) {
-    Group& g = *gp;
-    BatchView<T> bv = g.view(g.offStartsY, T(0));
-    launch(FastOp::BatchYForward, g.ny, g.r2c, bv, g.blocksY, g.smemY, g.cpb, stream);
-  }
-  for (auto& gp : groups_) {
-    Group& g = *gp;
-    BatchView<T> bv = g.view(g.offStartsZ, scaled ? g.scale : T(0));
-    bv.out = reinterpret_cast<T* const*>(static_cast<char*>(g.dev.get()) + g.offValues);
-    launch(FastOp::BatchZForward, g.nz, g.r2c, bv, g.blocksZ, g.smemZ, g.spb, stream);
-  }
-  for (int t : fallback_) {
-    transforms_[t]->gpu_plan().forward(spaces_[t], const_cast<T*>(values_[t]), scaled,
-                                       transforms_[t]->grid().scratch(), stream);
-  }
+  for (auto& e : ev.ev) (void)cudaEventDestroy(e);
 }
 
 template <typename T>
 void BatchPlan<T>::pair_graph(bool scaled, cudaStream_t stream) {
+  graph(3, scaled, stream);
+}
+
+template <typename T>
+void BatchPlan<T>::graph(int what, bool scaled, cudaStream_t stream) {
   check_bound();
   if (stream == nullptr || stream == cudaStreamLegacy || stream == cudaStreamPerThread) {
     throw InvalidParameterError();
   }
   DeviceGuard guard(device_);
-  // refresh views outside the capture (a synchronous copy cannot be captured)
-  std::vector<void*> seen = scratchSeen_;
+  // refresh views outside the capture (a synchronous copy cannot be captured); the graphs read
+  // the views and the bound pointers from device tables at fixed addresses, so neither a refresh
+  // nor a rebind invalidates them
   upload_views();
-  if (seen != scratchSeen_) {
-    for (auto& g : graphs_) {
-      if (g) (void)cudaGraphExecDestroy(g);
-      g = nullptr;
-    }
-  }
-  cudaGraphExec_t& exec = graphs_[scaled ? 1 : 0];
+  cudaGraphExec_t& exec = graphs_[2 * what + (scaled ? 1 : 0)];
   if (!exec) {
-    cudaGraph_t graph = nullptr;
+    cudaGraph_t g = nullptr;
     check_cuda(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
     try {
-      backward(stream);
-      forward(scaled, stream);
+      run(what, scaled, stream);
     } catch (...) {
-      (void)cudaStreamEndCapture(stream, &graph);
-      if (graph) (void)cudaGraphDestroy(graph);
+      (void)cudaStreamEndCapture(stream, &g);
+      if (g) (void)cudaGraphDestroy(g);
       throw;
     }
-    check_cuda(cudaStreamEndCapture(stream, &graph));
-    const cudaError_t st = cudaGraphInstantiate(&exec, graph, 0);
-    (void)cudaGraphDestroy(graph);
+    check_cuda(cudaStreamEndCapture(stream, &g));
+    const cudaError_t st = cudaGraphInstantiate(&exec, g, 0);
+    (void)cudaGraphDestroy(g);
     check_cuda(st);
   }
   check_cuda(cudaGraphLaunch(exec, stream));

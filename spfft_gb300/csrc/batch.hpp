@@ -27,17 +27,33 @@ public:
   BatchPlan& operator=(const BatchPlan&) = delete;
 
   // Device buffers of every transform: values[i] (interleaved complex) and spaces[i] (the space
-  // domain). Both must be aligned to the complex size. Replaces earlier bindings and drops any
-  // captured graph.
-  void bind(const T* const* values, T* const* spaces);
+  // domain). Both must be aligned to the complex size. Replaces earlier bindings; captured graphs
+  // stay valid (they read the bound pointers from a device table). Synchronous by default, so no
+  // work of this batch may be in flight; with `async` the table is written in the order of
+  // `stream` instead, which then must be the stream the batch runs on.
+  void bind(const T* const* values, T* const* spaces, cudaStream_t stream = nullptr, bool async = false);
 
+  // With more than one shape group (or unbatched transforms), the groups run as concurrent
+  // branches: each on its own stream, forked from and joined back into `stream`.
   void backward(cudaStream_t stream);
   void forward(bool scaled, cudaStream_t stream);
   // backward then forward as one CUDA graph, captured on the first call for this scaling (on
-  // `stream`, which must not be the legacy default stream) and replayed afterwards.
+  // `stream`, which must not be the legacy default stream) and replayed afterwards. Each group's
+  // six launches form one chain of the graph; the chains of different groups run concurrently.
   void pair_graph(bool scaled, cudaStream_t stream);
+  // The same for one direction (what: 1 backward, 2 forward, 3 backward then forward).
+  void graph(int what, bool scaled, cudaStream_t stream);
+  // One direction (0 backward, 1 forward) with the groups run pass by pass on `stream` and events
+  // between the passes; waits and returns the three pass times in milliseconds.
+  void stage_times(int direction, bool scaled, cudaStream_t stream, float ms[3]);
 
-  int num_transforms() const { return static_cast<int>(transforms_.size()); }
+  int num_transforms() const { return static_cast<int>(tp_.size()); }
+  // Stop keeping the transforms alive (for an owner that tracks their lifetime itself and drops
+  // the plan before any of them goes away).
+  void release_transforms() { transforms_.clear(); }
+  // Pointers currently bound (nullptr before the first bind).
+  const T* bound_values(int t) const { return bound_ ? values_[t] : nullptr; }
+  const T* bound_space(int t) const { return bound_ ? spaces_[t] : nullptr; }
   int num_groups() const { return static_cast<int>(groups_.size()); }
   int num_unbatched() const { return static_cast<int>(fallback_.size()); }
   // Kernel launches of one backward + forward pair.
@@ -47,16 +63,26 @@ private:
   struct Group;
   void upload_views();
   void check_bound() const;
+  // Passes of one group on `s`: bit 0 backward, bit 1 forward (after the backward).
+  void run_group(Group& g, int what, bool scaled, cudaStream_t s);
+  void run_fallback(int what, bool scaled, cudaStream_t s);
+  // Every group (and the unbatched transforms) as concurrent branches of `stream`.
+  void run(int what, bool scaled, cudaStream_t stream);
 
-  std::vector<std::shared_ptr<TransformInternal<T>>> transforms_;
+  std::vector<std::shared_ptr<TransformInternal<T>>> transforms_;  // ownership (may be released)
+  std::vector<TransformInternal<T>*> tp_;
   std::vector<std::unique_ptr<Group>> groups_;
   std::vector<int> fallback_;
   std::vector<const T*> values_;
   std::vector<T*> spaces_;
   std::vector<void*> scratchSeen_;
   bool bound_ = false;
-  cudaGraphExec_t graphs_[2] = {nullptr, nullptr};
+  cudaGraphExec_t graphs_[8] = {};  // index 2 * what + scaled
   int device_ = 0;
+  // fork / join of the concurrent branches (created with the plan when there is more than one)
+  std::vector<std::unique_ptr<Stream>> branchStreams_;
+  std::vector<std::unique_ptr<Event>> branchDone_;
+  std::unique_ptr<Event> fork_;
 };
 
 extern template class BatchPlan<double>;

@@ -164,10 +164,18 @@ __host__ __device__ __forceinline__ dd dd_from_double(double v, int k) {
   return dd(hi, dd_float_from_bits(sign | (static_cast<unsigned>(el + 127) << 23) | frac));
 }
 
-// (hi + lo) * 2^k as the nearest double (ties to even), for dd values with |lo| <= |hi| and both
-// binary32-normal (or lo zero). Inf / NaN in hi pass through.
+// (hi + lo) * 2^k as the nearest double (ties to even), for binary32-normal (or zero) hi and lo.
+// Inf / NaN in hi pass through. Integer and FP32 instructions only.
 __host__ __device__ __forceinline__ double dd_to_double(dd v, int k) {
-  const unsigned hb = dd_bits32(v.hi), lb = dd_bits32(v.lo);
+  unsigned hb = dd_bits32(v.hi), lb = dd_bits32(v.lo);
+  if ((lb << 1) != 0 && ((lb >> 23) & 0xff) >= ((hb >> 23) & 0xff)) {
+    // lo not below hi's binade (never produced by the arithmetic, but a zero hi is possible):
+    // renormalise exactly with two_sum on the FP32 pipe, after which lo is at most half an ulp
+    // of hi.
+    const dd n = dd_two_sum(v.hi, v.lo);
+    hb = dd_bits32(n.hi);
+    lb = dd_bits32(n.lo);
+  }
   const int eh = static_cast<int>((hb >> 23) & 0xff);
   if (eh == 0xff) {
     return dd_double_from_bits((static_cast<unsigned long long>(hb >> 31) << 63) | 0x7ff0000000000000ull |
@@ -178,11 +186,7 @@ __host__ __device__ __forceinline__ double dd_to_double(dd v, int k) {
   unsigned long long S = H;
   const int el = static_cast<int>((lb >> 23) & 0xff);
   if (el != 0) {
-    const int shift = 39 - (eh - el);
-    if (shift >= 40) {  // |lo| > |hi|: not a normalised dd; never produced by the arithmetic
-      return (static_cast<double>(v.hi) + static_cast<double>(v.lo)) * dd_double_from_bits(
-                 static_cast<unsigned long long>(1023 + k) << 52);
-    }
+    const int shift = 39 - (eh - el);  // < 39: lo lies in a lower binade than hi
     const unsigned long long L = (lb & 0x7FFFFFu) | 0x800000u;
     // Bits of lo shifted out below S's last place are kept as a sticky bit, so that the final
     // rounding (which drops >= 9 bits) sees whether the exact value lies above S.

@@ -4,11 +4,25 @@
 // constant twiddles (Cooley-Tukey), fully unrolled so that every value stays in registers.
 #pragma once
 
+#include "dd.cuh"
 #include "fft_core.cuh"
 #include "twiddle_constants.hpp"
 
 namespace spfft {
 namespace gb300 {
+
+// cos / sin of 2 pi m / R in the arithmetic type T. Double-float takes the generated float pairs,
+// so forming a constant never needs a binary64 instruction.
+template <typename T>
+struct TwConst {
+  __host__ __device__ static T cos(int r, int m) { return T(tw_cos(r, m)); }
+  __host__ __device__ static T sin(int r, int m) { return T(tw_sin(r, m)); }
+};
+template <>
+struct TwConst<dd> {
+  __host__ __device__ static dd cos(int r, int m) { return dd(tw_cos_pair_hi(r, m), tw_cos_pair_lo(r, m)); }
+  __host__ __device__ static dd sin(int r, int m) { return dd(tw_sin_pair_hi(r, m), tw_sin_pair_lo(r, m)); }
+};
 
 // Multiply by exp(SIGN * 2 pi i * m / R) with m, R compile-time constants after unrolling.
 template <int R, int SIGN, typename C>
@@ -19,8 +33,8 @@ __host__ __device__ __forceinline__ C twiddle_const(C a, int m) {
   if (2 * m == R) return make_c(-a.x, -a.y);
   if (4 * m == R) return cmul_i<SIGN>(a);
   if (4 * m == 3 * R) return cmul_i<-SIGN>(a);
-  const T c = T(tw_cos(R, m));
-  const T s = T(SIGN * tw_sin(R, m));
+  const T c = TwConst<T>::cos(R, m);
+  const T s = SIGN > 0 ? TwConst<T>::sin(R, m) : -TwConst<T>::sin(R, m);
   return make_c(a.x * c - a.y * s, a.x * s + a.y * c);
 }
 

@@ -85,10 +85,11 @@ __host__ __device__ __forceinline__ void dft2(C* v) {
 template <int SIGN, typename C>
 __host__ __device__ __forceinline__ void dft3(C* v) {
   using T = decltype(v[0].x);
-  const T h = T(0.8660254037844386467637232);  // sin(2 pi / 3)
+  constexpr T h = T(0.8660254037844386467637232);  // sin(2 pi / 3)
+  constexpr T half = T(0.5);
   C t1 = cadd(v[1], v[2]);
   C t2 = csub(v[1], v[2]);
-  C m = make_c(v[0].x - T(0.5) * t1.x, v[0].y - T(0.5) * t1.y);
+  C m = make_c(v[0].x - half * t1.x, v[0].y - half * t1.y);
   C n = cmul_i<SIGN>(cscale(t2, h));
   v[0] = cadd(v[0], t1);
   v[1] = cadd(m, n);
@@ -110,8 +111,8 @@ __host__ __device__ __forceinline__ void dft4(C* v) {
 template <int SIGN, typename C>
 __host__ __device__ __forceinline__ void dft5(C* v) {
   using T = decltype(v[0].x);
-  const T c1 = T(0.3090169943749474241022934), c2 = T(-0.8090169943749474241022934);
-  const T s1 = T(0.9510565162951535721164393), s2 = T(0.5877852522924731291687060);
+  constexpr T c1 = T(0.3090169943749474241022934), c2 = T(-0.8090169943749474241022934);
+  constexpr T s1 = T(0.9510565162951535721164393), s2 = T(0.5877852522924731291687060);
   C a = cadd(v[1], v[4]), b = cadd(v[2], v[3]);
   C c = csub(v[1], v[4]), d = csub(v[2], v[3]);
   C x0 = v[0];
@@ -129,10 +130,10 @@ __host__ __device__ __forceinline__ void dft5(C* v) {
 template <int SIGN, typename C>
 __host__ __device__ __forceinline__ void dft7(C* v) {
   using T = decltype(v[0].x);
-  const T C1 = T(0.6234898018587335305250049), C2 = T(-0.2225209339563144042889026),
-          C3 = T(-0.9009688679024191262361023);
-  const T S1 = T(0.7818314824680298087084445), S2 = T(0.9749279121818236070181317),
-          S3 = T(0.4338837391175581204757683);
+  constexpr T C1 = T(0.6234898018587335305250049), C2 = T(-0.2225209339563144042889026),
+              C3 = T(-0.9009688679024191262361023);
+  constexpr T S1 = T(0.7818314824680298087084445), S2 = T(0.9749279121818236070181317),
+              S3 = T(0.4338837391175581204757683);
   C a1 = cadd(v[1], v[6]), a2 = cadd(v[2], v[5]), a3 = cadd(v[3], v[4]);
   C d1 = csub(v[1], v[6]), d2 = csub(v[2], v[5]), d3 = csub(v[3], v[4]);
   C x0 = v[0];
@@ -157,7 +158,7 @@ __host__ __device__ __forceinline__ void dft7(C* v) {
 template <int SIGN, typename C>
 __host__ __device__ __forceinline__ void dft8(C* v) {
   using T = decltype(v[0].x);
-  const T r = T(0.7071067811865475244008444);
+  constexpr T r = T(0.7071067811865475244008444);
   C b[4], c[4];
 #pragma unroll
   for (int i = 0; i < 4; ++i) {

@@ -97,6 +97,15 @@ public:
   // Run on `stream` directly (no internal stream, no default-stream ordering); nullptr restores
   // the reference protocol.
   void set_stream(cudaStream_t stream) { userStream_ = stream; hasUserStream_ = (stream != nullptr); }
+  bool has_user_stream() const { return hasUserStream_; }
+  // Device address of a user buffer: device memory as it is, pinned host memory through its mapped
+  // alias when kernels access host buffers directly, nullptr for anything else.
+  template <typename P>
+  P* device_address(P* p) const {
+    auto split = gb300::split_pointer(p);
+    if (split.second) return split.second;
+    return directHost_ ? gb300::mapped_host_alias(split.first) : nullptr;
+  }
   const gb300::IndexPlan& index_plan() const { return *plan_; }
   const gb300::GpuPlan<T>& gpu_plan() const { return *gpu_; }
   int path_flags() const { return gpu_->path_flags(); }

@@ -535,7 +535,7 @@ __global__ void __launch_bounds__(kPlaneThreads) plane_forward(const PlanView<S>
     __syncthreads();
     if (R2C) {
       // X[k] = (Z[k] + conj Z[M-k]) / 2 - i/2 e^{-2 pi i k/N} (Z[k] - conj Z[M-k]), Z[M] = Z[0]
-      const A half = A(0.5);
+      constexpr A half = A(0.5);
       for (int i = threadIdx.x; i < nr * nc; i += blockDim.x) {
         const int rl = i / nc, c = i - rl * nc;
         const int kk = p.columnX[c];
@@ -888,7 +888,7 @@ __device__ __forceinline__ void x_forward_body(const PlanView<S>& p, const S* __
   }
   __syncthreads();
   if (R2C) {
-    const A half = A(0.5);
+    constexpr A half = A(0.5);
     for (int i = threadIdx.x; i < nr * nc; i += blockDim.x) {
       const int rl = i / nc, c = i - rl * nc;
       const int kk = p.columnX[c];

@@ -147,6 +147,8 @@ public:
     check_cuda(cudaEventRecord(e_, from));
     check_cuda(cudaStreamWaitEvent(to, e_, 0));
   }
+  void record(cudaStream_t s) { check_cuda(cudaEventRecord(e_, s)); }
+  void wait_on(cudaStream_t s) { check_cuda(cudaStreamWaitEvent(s, e_, 0)); }
 
 private:
   cudaEvent_t e_ = nullptr;

@@ -1,6 +1,6 @@
 // Host self-test of the integer-only double <-> dd conversions in spfft_gb300/csrc/dd.cuh:
 // split exactness (hi + lo within 2^-47 of v * 2^k), round trips, signs, zeros, infinities and the
-// rounding of dd_to_double on normalised dd values. Prints "ok <checks>" or the first failure.
+// rounding of dd_to_double on normalised dd values and on pairs whose lo is not below hi. Prints "ok <checks>" or the first failure.
 #include <cmath>
 #include <cstdio>
 #include <random>
@@ -39,7 +39,15 @@ int main() {
       std::printf("combine error hi=%.9g lo=%.9g got %.17g want %.17g\n", n.hi, n.lo, dd_to_double(n, 0), exact);
       return 1;
     }
-    checks += 3;
+    // pairs that are not normalised (lo in hi's binade or above, zero hi) are still summed exactly
+    const float c = (float)mant(rng) * std::ldexp(1.0f, ex(rng) / 4);
+    const float e = (i % 5 == 0) ? 0.0f : (float)mant(rng) * std::ldexp(1.0f, ex(rng) / 4 % 3) * ((i & 4) ? -1.0f : 1.0f);
+    const double sum = (double)e + (double)c;  // exact: exponents differ by at most 18
+    if (dd_to_double(dd(e, c), 0) != sum) {
+      std::printf("unnormalised error hi=%.9g lo=%.9g got %.17g want %.17g\n", e, c, dd_to_double(dd(e, c), 0), sum);
+      return 1;
+    }
+    checks += 4;
   }
   // specials
   if (dd_to_double(dd_from_double(0.0, 5), -5) != 0.0) return 2;
