@@ -766,7 +766,7 @@ def batch_main(args, rank: int, world: int) -> int:
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(res["ms_per_step"], 4),
         "higher_is_better": True, "scaling": "strong", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic", "config": config, "roofline": res["roofline"],
-        "hbm_gbs_per_pair_accounting": round(res["pair_bytes"] * res["value"] / world / 1e9, 1),
+        "hbm_gbs_per_pair_accounting": round(res["pair_bytes"] / (res["ms_per_step"] * 1e-3) / 1e9, 1),
         "e2e": res["e2e"], "clocks": res["clocks"],
         "gpu_launches": res["launches_per_step"] * args.steps,
         "shape_groups": res["groups"], "unbatched_transforms": res["unbatched"],

@@ -115,7 +115,8 @@ SPFFT_EXPORT SpfftError spfft_gb300_float_batch_create(SpfftGb300Batch* batch, i
 SPFFT_EXPORT SpfftError spfft_gb300_batch_destroy(SpfftGb300Batch batch);
 /* values[i]: device interleaved-complex frequency values of transform i; spaces[i]: its device
  * space domain. Pointers must be aligned to the complex size (16 bytes double, 8 bytes float).
- * Synchronous: call it while no work of the batch is in flight. Captured graphs stay valid. */
+ * Synchronous: call it while no work of the batch is in flight. Captured graphs stay valid, except
+ * when the buffers of a transform that runs unbatched change: those graphs are captured anew. */
 SPFFT_EXPORT SpfftError spfft_gb300_batch_bind(SpfftGb300Batch batch, void* const* values,
                                                void* const* spaces);
 SPFFT_EXPORT SpfftError spfft_gb300_batch_backward(SpfftGb300Batch batch, void* stream);

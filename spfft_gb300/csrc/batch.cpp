@@ -46,12 +46,12 @@ struct BatchPlan<T>::Group {
 template <typename T>
 BatchPlan<T>::BatchPlan(std::vector<std::shared_ptr<TransformInternal<T>>> transforms)
     : transforms_(std::move(transforms)) {
-  const int n = static_cast<int>(tp_.size());
-  if (n == 0) throw InvalidParameterError();
   for (auto& t : transforms_) {
     if (!t) throw InvalidParameterError();
     tp_.push_back(t.get());
   }
+  const int n = static_cast<int>(tp_.size());
+  if (n == 0) throw InvalidParameterError();
   device_ = tp_[0]->device_id();
   for (int a = 0; a < n; ++a) {
     if (tp_[a]->device_id() != device_) throw InvalidParameterError();
@@ -211,6 +211,19 @@ void BatchPlan<T>::bind(const T* const* values, T* const* spaces, cudaStream_t s
     if (tp_[t]->num_local_elements() > 0 &&
         (!values[t] || reinterpret_cast<uintptr_t>(values[t]) % c)) {
       throw InvalidParameterError();
+    }
+  }
+  // Unbatched transforms take their pointers as kernel arguments, so a graph that contains them
+  // holds the old pointers: drop the graphs (an in-flight graph is freed when it completes) and
+  // capture them again on their next use.
+  bool fallbackMoved = false;
+  for (int t : fallback_) {
+    fallbackMoved |= values_[t] != values[t] || spaces_[t] != spaces[t];
+  }
+  if (fallbackMoved) {
+    for (auto& g : graphs_) {
+      if (g) (void)cudaGraphExecDestroy(g);
+      g = nullptr;
     }
   }
   for (size_t t = 0; t < tp_.size(); ++t) {

@@ -28,9 +28,10 @@ public:
 
   // Device buffers of every transform: values[i] (interleaved complex) and spaces[i] (the space
   // domain). Both must be aligned to the complex size. Replaces earlier bindings; captured graphs
-  // stay valid (they read the bound pointers from a device table). Synchronous by default, so no
-  // work of this batch may be in flight; with `async` the table is written in the order of
-  // `stream` instead, which then must be the stream the batch runs on.
+  // stay valid (they read the bound pointers from a device table), unless the buffers of an
+  // unbatched transform change (those are kernel arguments; the graphs are then captured anew).
+  // Synchronous by default, so no work of this batch may be in flight; with `async` the table is
+  // written in the order of `stream` instead, which then must be the stream the batch runs on.
   void bind(const T* const* values, T* const* spaces, cudaStream_t stream = nullptr, bool async = false);
 
   // With more than one shape group (or unbatched transforms), the groups run as concurrent
