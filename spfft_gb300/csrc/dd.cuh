@@ -1,5 +1,5 @@
-// Double-float ("dd") arithmetic: a value is the unevaluated sum hi + lo of two floats with
-// |lo| <= ulp(hi)/2, giving about 48 significant bits on the FP32 pipes. GB300 issues FP32 FMA at
+// Double-float ("dd") arithmetic: a value is the unevaluated sum hi + lo of two floats, lo at most
+// a few ulps of hi, giving about 44-48 significant bits on the FP32 pipes. GB300 issues FP32 FMA at
 // 57x its FP64 rate, so FFT butterflies in dd arithmetic beat native FP64 several times while
 // staying well inside a 1e-12 relative error.
 //
@@ -7,8 +7,13 @@
 //   two_sum(a, b):      s = a + b, e = exact rounding error of the sum (6 flops, any a, b)
 //   fast_two_sum(a, b): the same for |a| >= |b| (3 flops)
 //   two_prod(a, b):     p = a * b, e = fma(a, b, -p) (exact error of the product)
-// add: two_sum of the high parts, low parts added into the error, renormalised;
-// mul: two_prod of the high parts, cross terms added into the error, renormalised.
+// add: two_sum of the high parts, low parts added into the error;
+// mul: two_prod of the high parts, cross terms added into the error.
+// Neither renormalises (no final fast_two_sum): hi + lo stays the exact value of the pair and only
+// the FP32 roundings of the low-order terms cost accuracy. Without renormalisation lo may grow to
+// a few ulps of hi within a transform, which costs a few of the ~48 bits, in exchange for 8
+// instead of 11 instructions per add and 4 instead of 7 per product. The conversion to binary64
+// (dd_to_double) accepts unnormalised pairs.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -40,9 +45,8 @@ __host__ __device__ __forceinline__ dd dd_fast_two_sum(float a, float b) {
 }
 
 __host__ __device__ __forceinline__ dd operator+(dd a, dd b) {
-  dd s = dd_two_sum(a.hi, b.hi);
-  const float e = s.lo + (a.lo + b.lo);
-  return dd_fast_two_sum(s.hi, e);
+  const dd s = dd_two_sum(a.hi, b.hi);
+  return dd(s.hi, s.lo + (a.lo + b.lo));
 }
 __host__ __device__ __forceinline__ dd operator-(dd a) { return dd(-a.hi, -a.lo); }
 __host__ __device__ __forceinline__ dd operator-(dd a, dd b) { return a + (-b); }
@@ -57,8 +61,10 @@ __host__ __device__ __forceinline__ dd operator*(dd a, dd b) {
   e = fmaf(a.hi, b.lo, e);
   e = fmaf(a.lo, b.hi, e);
 #endif
-  return dd_fast_two_sum(p, e);
+  return dd(p, e);
 }
+// Multiplication by 1/2 (exact in both parts).
+__host__ __device__ __forceinline__ dd half_of(dd a) { return dd(0.5f * a.hi, 0.5f * a.lo); }
 // Multiplication by +1 / -1 (the sign factors of the butterflies).
 __host__ __device__ __forceinline__ dd operator*(int s, dd a) { return s >= 0 ? a : -a; }
 __host__ __device__ __forceinline__ bool operator!=(dd a, int z) {
@@ -169,9 +175,9 @@ __host__ __device__ __forceinline__ dd dd_from_double(double v, int k) {
 __host__ __device__ __forceinline__ double dd_to_double(dd v, int k) {
   unsigned hb = dd_bits32(v.hi), lb = dd_bits32(v.lo);
   if ((lb << 1) != 0 && ((lb >> 23) & 0xff) >= ((hb >> 23) & 0xff)) {
-    // lo not below hi's binade (never produced by the arithmetic, but a zero hi is possible):
-    // renormalise exactly with two_sum on the FP32 pipe, after which lo is at most half an ulp
-    // of hi.
+    // lo not below hi's binade (after a cancellation in the unnormalised arithmetic, or a zero
+    // hi): renormalise exactly with two_sum on the FP32 pipe, after which lo is at most half an
+    // ulp of hi.
     const dd n = dd_two_sum(v.hi, v.lo);
     hb = dd_bits32(n.hi);
     lb = dd_bits32(n.lo);

@@ -68,6 +68,9 @@ template <int SIGN, typename C>
 __host__ __device__ __forceinline__ C ctw(C a, C tw) {
   return SIGN < 0 ? cmul(a, tw) : cmulc(a, tw);
 }
+// Multiplication by 1/2 (double-float overloads it with an exact two-part scaling).
+__host__ __device__ __forceinline__ float half_of(float a) { return 0.5f * a; }
+__host__ __device__ __forceinline__ double half_of(double a) { return 0.5 * a; }
 template <typename C>
 __host__ __device__ __forceinline__ bool cnonzero(C a) {
   return a.x != 0 || a.y != 0;
@@ -86,10 +89,9 @@ template <int SIGN, typename C>
 __host__ __device__ __forceinline__ void dft3(C* v) {
   using T = decltype(v[0].x);
   constexpr T h = T(0.8660254037844386467637232);  // sin(2 pi / 3)
-  constexpr T half = T(0.5);
   C t1 = cadd(v[1], v[2]);
   C t2 = csub(v[1], v[2]);
-  C m = make_c(v[0].x - half * t1.x, v[0].y - half * t1.y);
+  C m = make_c(v[0].x - half_of(t1.x), v[0].y - half_of(t1.y));
   C n = cmul_i<SIGN>(cscale(t2, h));
   v[0] = cadd(v[0], t1);
   v[1] = cadd(m, n);

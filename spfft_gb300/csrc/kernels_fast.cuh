@@ -535,7 +535,6 @@ __global__ void __launch_bounds__(kPlaneThreads) plane_forward(const PlanView<S>
     __syncthreads();
     if (R2C) {
       // X[k] = (Z[k] + conj Z[M-k]) / 2 - i/2 e^{-2 pi i k/N} (Z[k] - conj Z[M-k]), Z[M] = Z[0]
-      constexpr A half = A(0.5);
       for (int i = threadIdx.x; i < nr * nc; i += blockDim.x) {
         const int rl = i / nc, c = i - rl * nc;
         const int kk = p.columnX[c];
@@ -544,7 +543,7 @@ __global__ void __launch_bounds__(kPlaneThreads) plane_forward(const PlanView<S>
         const CA zm = wrow[L::wpos(transposed_pos<L::LX>((L::M - kk) % L::M))];
         const CA dif = make_c(zk.x - zm.x, zk.y + zm.y);
         const CA u = cmul(dif, s.twx[kk]);
-        s.P[(r0 + rl) * nc + c] = make_c(half * (zk.x + zm.x + u.y), half * (zk.y - zm.y - u.x));
+        s.P[(r0 + rl) * nc + c] = make_c(half_of(zk.x + zm.x + u.y), half_of(zk.y - zm.y - u.x));
       }
       __syncthreads();
     }
@@ -888,7 +887,6 @@ __device__ __forceinline__ void x_forward_body(const PlanView<S>& p, const S* __
   }
   __syncthreads();
   if (R2C) {
-    constexpr A half = A(0.5);
     for (int i = threadIdx.x; i < nr * nc; i += blockDim.x) {
       const int rl = i / nc, c = i - rl * nc;
       const int kk = p.columnX[c];
@@ -897,7 +895,7 @@ __device__ __forceinline__ void x_forward_body(const PlanView<S>& p, const S* __
       const CA zm = wrow[L::wpos(transposed_pos<L::LX>((L::M - kk) % L::M))];
       const CA dif = make_c(zk.x - zm.x, zk.y + zm.y);
       const CA u = cmul(dif, s.twx[kk]);
-      s.P[rl * nc + c] = make_c(half * (zk.x + zm.x + u.y), half * (zk.y - zm.y - u.x));
+      s.P[rl * nc + c] = make_c(half_of(zk.x + zm.x + u.y), half_of(zk.y - zm.y - u.x));
     }
     __syncthreads();
   }
