@@ -147,91 +147,68 @@ __host__ __device__ __forceinline__ int dd_exponent_field(double v) {
   return static_cast<int>((dd_bits64(v) >> 52) & 0x7ff);
 }
 
-// v * 2^k as dd: hi takes the top 24 significant bits (truncated), lo the next 24. Values whose
-// scaled magnitude leaves the binary32 normal range become signed zero (below) or infinity
-// (above); callers choose k so that the block maximum lands in [1, 2).
+// v * 2^k as dd: hi takes the top 24 significant bits of v (truncated), lo the next 23 (the last
+// 6 of binary64's 53 are dropped: relative error below 2^-46). lo is formed exactly on the FP32
+// pipe as (2^(e-23) * 1.f) - 2^(e-23) from two assembled bit patterns, so no count of leading
+// zeros or variable shift is needed. Values whose scaled exponent e is below -126 become signed
+// zero (their lo already below e = -103); above 127 they become infinity. Callers choose k so
+// that the block maximum lands in [1, 2).
 __host__ __device__ __forceinline__ dd dd_from_double(double v, int k) {
   const unsigned long long u = dd_bits64(v);
-  const unsigned sign = static_cast<unsigned>(u >> 63) << 31;
-  const int E = static_cast<int>((u >> 52) & 0x7ff);
-  const unsigned long long m = u & 0xFFFFFFFFFFFFFull;
-  if (E == 0x7ff) return dd(dd_float_from_bits(sign | 0x7f800000u | (m ? 0x400000u : 0u)), 0.0f);
+  const unsigned hw = static_cast<unsigned>(u >> 32), lw = static_cast<unsigned>(u);
+  const unsigned sign = hw & 0x80000000u;
+  const int E = static_cast<int>((hw >> 20) & 0x7ffu);
   const int e = E - 1023 + k;
-  if (E == 0 || e < -126) return dd(dd_float_from_bits(sign), 0.0f);
-  if (e > 127) return dd(dd_float_from_bits(sign | 0x7f800000u), 0.0f);
-  const float hi = dd_float_from_bits(sign | (static_cast<unsigned>(e + 127) << 23) |
-                                      static_cast<unsigned>(m >> 29));
-  const unsigned r = static_cast<unsigned>(m & 0x1FFFFFFFu);  // remaining 29 fraction bits
-  if (r == 0) return dd(hi, 0.0f);
-  const int p = 31 - dd_clz32(r);  // leading one of the remainder
-  const int el = e - 52 + p;
-  if (el < -126) return dd(hi, 0.0f);
-  const unsigned frac = p >= 23 ? (r >> (p - 23)) & 0x7FFFFFu : (r << (23 - p)) & 0x7FFFFFu;
-  return dd(hi, dd_float_from_bits(sign | (static_cast<unsigned>(el + 127) << 23) | frac));
+  if (e > 127) {  // overflow, or inf / NaN (k = 0 for blocks that hold them)
+    const bool nan = E == 0x7ff && (((hw & 0xFFFFFu) | lw) != 0u);
+    return dd(dd_float_from_bits(sign | 0x7f800000u | (nan ? 0x400000u : 0u)), 0.0f);
+  }
+  const unsigned top = ((hw & 0xFFFFFu) << 3) | (lw >> 29);  // fraction bits 1..23
+  const unsigned next = (lw >> 6) & 0x7FFFFFu;                // fraction bits 24..46
+  const bool tiny = E == 0 || e < -126;
+  const float hi = dd_float_from_bits(tiny ? sign : (sign | (static_cast<unsigned>(e + 127) << 23) | top));
+  const unsigned base = sign | (static_cast<unsigned>(e + 104) << 23);
+  const float lo = (E == 0 || e < -103) ? dd_float_from_bits(sign) : dd_float_from_bits(base | next) - dd_float_from_bits(base);
+  return dd(hi, lo);
 }
 
-// (hi + lo) * 2^k as the nearest double (ties to even), for binary32-normal (or zero) hi and lo.
-// Inf / NaN in hi pass through. Integer and FP32 instructions only.
+// (hi + lo) * 2^k as a double, faithfully rounded (error below one unit in the last place), for
+// any pair of binary32 values whose sum is finite: two_sum first makes |lo| <= ulp(hi) / 2, then
+// lo is added to hi's binary64 bit pattern as an integer count of binary64 ulps of hi (at most
+// 2^28 in magnitude, so the sum never carries into the next binade; when hi is a power of two and
+// lo pulls below it the count is doubled, since the ulps there are half as large, except at the
+// bottom of the normal range where the subnormal ulps below are not). Scaled results
+// below the binary64 normal range become signed zero, above it infinity; inf / NaN in hi pass
+// through. Integer and FP32 instructions only.
 __host__ __device__ __forceinline__ double dd_to_double(dd v, int k) {
-  unsigned hb = dd_bits32(v.hi), lb = dd_bits32(v.lo);
-  if ((lb << 1) != 0 && ((lb >> 23) & 0xff) >= ((hb >> 23) & 0xff)) {
-    // lo not below hi's binade (after a cancellation in the unnormalised arithmetic, or a zero
-    // hi): renormalise exactly with two_sum on the FP32 pipe, after which lo is at most half an
-    // ulp of hi.
-    const dd n = dd_two_sum(v.hi, v.lo);
-    hb = dd_bits32(n.hi);
-    lb = dd_bits32(n.lo);
-  }
-  const int eh = static_cast<int>((hb >> 23) & 0xff);
+  const dd n = dd_two_sum(v.hi, v.lo);
+  const unsigned hb = dd_bits32(n.hi), lb = dd_bits32(n.lo);
+  const unsigned sign = hb & 0x80000000u;
+  const int eh = static_cast<int>((hb >> 23) & 0xffu);
   if (eh == 0xff) {
-    return dd_double_from_bits((static_cast<unsigned long long>(hb >> 31) << 63) | 0x7ff0000000000000ull |
-                               ((hb & 0x7fffff) ? 0x8000000000000ull : 0ull));
+    return dd_double_from_bits((static_cast<unsigned long long>(sign) << 32) | 0x7ff0000000000000ull |
+                               ((hb & 0x7fffffu) ? 0x8000000000000ull : 0ull));
   }
-  if (eh == 0) return dd_double_from_bits(static_cast<unsigned long long>(hb >> 31) << 63);
-  const unsigned long long H = static_cast<unsigned long long>((hb & 0x7FFFFFu) | 0x800000u) << 39;
-  unsigned long long S = H;
-  const int el = static_cast<int>((lb >> 23) & 0xff);
-  if (el != 0) {
-    const int shift = 39 - (eh - el);  // < 39: lo lies in a lower binade than hi
-    const unsigned long long L = (lb & 0x7FFFFFu) | 0x800000u;
-    // Bits of lo shifted out below S's last place are kept as a sticky bit, so that the final
-    // rounding (which drops >= 9 bits) sees whether the exact value lies above S.
-    unsigned long long Y = 0;
-    bool sticky = false;
-    if (shift >= 0) {
-      Y = L << shift;
-    } else if (shift > -24) {
-      Y = L >> (-shift);
-      sticky = (L & ((1ull << (-shift)) - 1)) != 0;
-    } else {
-      sticky = true;
-    }
-    if ((hb ^ lb) >> 31) {
-      S = S - Y - (sticky ? 1 : 0);
-    } else {
-      S = S + Y;
-    }
-    if (sticky) S |= 1;
-  }
-  // value = S * 2^(eh - 127 - 23 - 39 + k); normalise S to 53 bits with round-to-nearest-even
-  const int lead = 63 - dd_clz64(S);
-  int expo = eh - 127 - 62 + lead + k;  // unbiased exponent of the leading bit
-  unsigned long long mant;
-  const int drop = lead - 52;
-  if (drop > 0) {
-    mant = S >> drop;
-    const unsigned long long rem = S & ((1ull << drop) - 1), half = 1ull << (drop - 1);
-    if (rem > half || (rem == half && (mant & 1))) ++mant;
+  const int E = eh - 127 + k + 1023;  // biased binary64 exponent of hi * 2^k
+  if (eh == 0 || E <= 0) return dd_double_from_bits(static_cast<unsigned long long>(sign) << 32);
+  if (E >= 2047) return dd_double_from_bits((static_cast<unsigned long long>(sign) << 32) | 0x7ff0000000000000ull);
+  const unsigned long long H =
+      (static_cast<unsigned long long>(sign | (static_cast<unsigned>(E) << 20) | ((hb >> 3) & 0xFFFFFu)) << 32) |
+      static_cast<unsigned long long>(hb << 29);
+  const int el = static_cast<int>((lb >> 23) & 0xffu);
+  const unsigned ml = el ? ((lb & 0x7FFFFFu) | 0x800000u) : 0u;
+  const bool opposite = ((hb ^ lb) >> 31) != 0u;
+  const int s = 29 + el - eh + ((opposite && (hb & 0x7FFFFFu) == 0u && E > 1) ? 1 : 0);  // <= 6
+  unsigned y;
+  if (s >= 0) {
+    y = ml << s;
+  } else if (s > -25) {
+    y = (ml + (1u << (-s - 1))) >> (-s);
   } else {
-    mant = S << (-drop);
+    y = 0u;
   }
-  if (expo + 1023 <= 0) return dd_double_from_bits(static_cast<unsigned long long>(hb >> 31) << 63);
-  if (expo + 1023 >= 2047) {
-    return dd_double_from_bits((static_cast<unsigned long long>(hb >> 31) << 63) | 0x7ff0000000000000ull);
-  }
-  // mant has its leading one at bit 52 (or 53 after a rounding carry, which the add propagates)
-  const unsigned long long bits = (static_cast<unsigned long long>(expo + 1022) << 52) + mant;
-  return dd_double_from_bits((static_cast<unsigned long long>(hb >> 31) << 63) | bits);
+  const unsigned long long Y = static_cast<unsigned long long>(y);
+  return dd_double_from_bits(opposite ? H - Y : H + Y);
 }
 
 }  // namespace gb300
