@@ -112,6 +112,25 @@ def make_values(idx: np.ndarray, r2c: bool, seed: int = 1) -> np.ndarray:
     return v
 
 
+def batch_pass_bytes(bt, geo: list) -> dict:
+    """Algorithmic bytes of each pass slot of a batch (z, y, x per direction), summed over its
+    transforms: a fused plane pass (path 2) moves sticks + space in the y slot and nothing in the x
+    slot; split passes (path 1) and unbatched transforms (path 0) as in algorithmic_bytes."""
+    out = {k: 0 for k in ("z_backward", "y_backward", "x_backward", "x_forward", "y_forward", "z_forward")}
+    pair = 0
+    for t, (n, npts, nsticks, ncols, r2c, tsize) in enumerate(geo):
+        ab = algorithmic_bytes(n, npts, nsticks, ncols, r2c, tsize)
+        k = ab["kernels"]
+        pair += ab["pair"]
+        if bt.transform_path(t) == 2:
+            c = 2 * tsize
+            fused = nsticks * n * c + n * n * n * (tsize if r2c else c)
+            k = dict(k, y_backward=fused, y_forward=fused, x_backward=0, x_forward=0)
+        for name in out:
+            out[name] += k[name]
+    return {"passes": out, "pair": pair}
+
+
 def algorithmic_bytes(n: int, npts: int, nsticks: int, ncols: int, r2c: bool, tsize: int) -> dict:
     """Compulsory HBM bytes per launch of each kernel and per pair (SURVEY-style accounting:
     sparse values + int32 value map + intermediates + dense space grid, each read or written once)."""
@@ -421,6 +440,24 @@ def measure_batched(args, workload: str, batch: int, dtype: str, radii=None) -> 
         ends[k].record(stream)
     torch.cuda.synchronize()
     ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
+    # per-pass times and GB/s (events between the passes of a backward and of a forward)
+    geo = []
+    for idx in idxs:
+        geo.append((n, len(idx), int(np.unique((idx[:, 0] % n) * n + idx[:, 1] % n).size),
+                    int(np.unique(idx[:, 0] % n).size), r2c, 8 if dtype == "float64" else 4))
+    pb = batch_pass_bytes(bt, geo)
+    acc = {k: [] for k in pb["passes"]}
+    for _ in range(5):
+        for nm, t in zip(("z_backward", "y_backward", "x_backward"), bt.stage_times(0, sp.SPFFT_NO_SCALING, stream)):
+            acc[nm].append(t)
+        for nm, t in zip(("x_forward", "y_forward", "z_forward"), bt.stage_times(1, sp.SPFFT_FULL_SCALING, stream)):
+            acc[nm].append(t)
+    pass_ms = {k: statistics.median(v) for k, v in acc.items()}
+    pass_gbs = {k: round(pb["passes"][k] / (pass_ms[k] * 1e-3) / 1e9, 1) for k in pass_ms if pb["passes"][k]}
+    for b in range(batch):  # the stage-timed passes changed the values: restore them
+        vals[b].copy_(torch.from_numpy(hosts[b]).to(ct))
+    bt.pair_graph(sp.SPFFT_FULL_SCALING, stream)
+    torch.cuda.synchronize()
     # scaled backward+forward is the identity on C2C values and on R2C values off the x = 0 plane
     errs = []
     for b in (0, batch - 1):
@@ -432,6 +469,9 @@ def measure_batched(args, workload: str, batch: int, dtype: str, radii=None) -> 
             "transforms_per_step": batch, "ms_per_step": round(ms / args.steps, 4),
             "graph_launches_per_step": 1, "kernel_launches_per_step": info["launches_per_pair"],
             "shape_groups": info["groups"], "roundtrip_rel_l2_max": max(errs),
+            "plane_pass": "fused" if bt.transform_path(0) == 2 else "split",
+            "pass_ms": {k: round(v, 4) for k, v in pass_ms.items()}, "pass_gbs": pass_gbs,
+            "hbm_gbs_per_pair_accounting": round(pb["pair"] / (ms / args.steps * 1e-3) / 1e9, 1),
             "workload": workload, "l2": "batch working set > L2 (no flush)"}
 
 
@@ -465,7 +505,7 @@ def measure_batch_workload(args, rank: int, world: int) -> dict:
         idxs.append(idx)
         hosts.append(batch_values(idx, r2c, seed=1000 + j))
         geo.append((n, len(idx), int(np.unique((idx[:, 0] % n) * n + idx[:, 1] % n).size),
-                    int(np.unique(idx[:, 0] % n).size), r2c))
+                    int(np.unique(idx[:, 0] % n).size), r2c, 4))
 
     def make(dtype):
         ct = torch.complex128 if dtype == "float64" else torch.complex64
@@ -519,13 +559,8 @@ def measure_batch_workload(args, rank: int, world: int) -> dict:
         for nm, ms in zip(names_f, bt.stage_times(1, sp.SPFFT_FULL_SCALING, stream)):
             acc[nm].append(ms)
     pass_ms = {k: statistics.median(v) for k, v in acc.items()}
-    pass_bytes = {k: 0 for k in acc}
-    pair_bytes = 0
-    for (n, npts, nsticks, ncols, r2c) in geo:
-        ab = algorithmic_bytes(n, npts, nsticks, ncols, r2c, 4)
-        for k in pass_bytes:
-            pass_bytes[k] += ab["kernels"][k]
-        pair_bytes += ab["pair"]
+    pb = batch_pass_bytes(bt, geo)
+    pass_bytes, pair_bytes = pb["passes"], pb["pair"]
     dominant = max(pass_ms, key=pass_ms.get)
     peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
     peak = float(peaks.get("hbm_gbs", 6800.0))
@@ -536,7 +571,8 @@ def measure_batch_workload(args, rank: int, world: int) -> dict:
                 "traffic": load_traffic_table().get((dominant + "_batch", args.workload, "float32")),
                 "algorithmic_bytes": pass_bytes[dominant],
                 "pass_ms": {k: round(v, 4) for k, v in pass_ms.items()},
-                "pass_gbs": {k: round(pass_bytes[k] / (pass_ms[k] * 1e-3) / 1e9, 1) for k in pass_ms}}
+                "pass_gbs": {k: round(pass_bytes[k] / (pass_ms[k] * 1e-3) / 1e9, 1) for k in pass_ms
+                             if pass_bytes[k]}}
 
     # ---- end to end: values from / to pinned host memory around the captured pair ---------------
     hv = [torch.from_numpy(v).to(ct32).pin_memory() for v in hosts]

@@ -129,9 +129,15 @@ SPFFT_EXPORT SpfftError spfft_gb300_batch_pair_graph(SpfftGb300Batch batch, Spff
                                                      void* stream);
 SPFFT_EXPORT SpfftError spfft_gb300_batch_info(SpfftGb300Batch batch, int* numGroups,
                                                int* numUnbatched, int* launchesPerPair);
+/* How transform `index` (its position at creation) runs: 0 one by one (no batched kernels for its
+ * lengths), 1 batched with split y and x passes, 2 batched with one fused plane pass (y and x per
+ * plane with the compact plane on chip; chosen for cubic planes that fit two blocks per SM, or
+ * forced with SPFFT_GB300_BATCH_PLANE=fused|split at batch creation). */
+SPFFT_EXPORT SpfftError spfft_gb300_batch_transform_path(SpfftGb300Batch batch, int index, int* path);
 /* One direction (0 backward, 1 forward) of the bound batch with the groups run pass by pass on
- * `stream` and events between the three passes (z, y, x in backward order); waits and writes the
- * pass times in milliseconds to stageMs[3]. For profiling: ordinary calls run groups concurrently. */
+ * `stream` and events between the three passes (z, y, x in backward order; a fused group runs its
+ * plane pass in the y slot and nothing in the x slot); waits and writes the pass times in
+ * milliseconds to stageMs[3]. For profiling: ordinary calls run groups concurrently. */
 SPFFT_EXPORT SpfftError spfft_gb300_batch_stage_times(SpfftGb300Batch batch, int direction,
                                                       SpfftScalingType scaling, void* stream,
                                                       float* stageMs);

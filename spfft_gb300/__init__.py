@@ -144,6 +144,7 @@ def _declare(lib: ctypes.CDLL) -> None:
     lib.spfft_gb300_batch_forward.argtypes = [_vp, _i, _vp]
     lib.spfft_gb300_batch_pair_graph.argtypes = [_vp, _i, _vp]
     lib.spfft_gb300_batch_info.argtypes = [_vp, _ip, _ip, _ip]
+    lib.spfft_gb300_batch_transform_path.argtypes = [_vp, _i, _ip]
     lib.spfft_gb300_multi_batched_calls.argtypes = [ctypes.POINTER(ctypes.c_longlong)]
     lib.spfft_gb300_batch_stage_times.argtypes = [_vp, _i, _i, _vp, ctypes.POINTER(ctypes.c_float)]
     lib.spfft_gb300_transform_backward_noalloc.argtypes = [_vp, _vp, _vp, _vp]
@@ -493,3 +494,9 @@ class Batch:
         g, u, l = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
         _call("spfft_gb300_batch_info", self._h, ctypes.byref(g), ctypes.byref(u), ctypes.byref(l))
         return {"groups": g.value, "unbatched": u.value, "launches_per_pair": l.value}
+
+    def transform_path(self, index: int) -> int:
+        """0 unbatched, 1 batched with split y and x passes, 2 batched with the fused plane pass."""
+        v = ctypes.c_int()
+        _call("spfft_gb300_batch_transform_path", self._h, int(index), ctypes.byref(v))
+        return v.value

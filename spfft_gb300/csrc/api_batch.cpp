@@ -125,6 +125,13 @@ SpfftError spfft_gb300_batch_info(SpfftGb300Batch batch, int* numGroups, int* nu
   });
 }
 
+SpfftError spfft_gb300_batch_transform_path(SpfftGb300Batch batch, int index, int* path) {
+  if (!path) return SPFFT_INVALID_PARAMETER_ERROR;
+  return with_batch(batch, [&](BatchHandle& h) {
+    *path = h.d ? h.d->transform_path(index) : h.f->transform_path(index);
+  });
+}
+
 SpfftError spfft_gb300_multi_batched_calls(long long* count) {
   if (!count) return SPFFT_INVALID_PARAMETER_ERROR;
   *count = spfft::gb300::multi_batched_calls();

@@ -3,8 +3,10 @@
 #include "batch.hpp"
 
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 #include <map>
+#include <string>
 #include <tuple>
 
 #include "engine.hpp"
@@ -17,6 +19,9 @@ namespace {
 constexpr size_t kAlign = 256;
 inline size_t align_up(size_t v) { return (v + kAlign - 1) / kAlign * kAlign; }
 constexpr size_t kZBudget = 56 * 1024, kPlaneBudget = 100 * 1024;
+// A fused plane block (y and x passes of one plane with the compact plane on chip) within this
+// budget runs two per SM (228 KB of shared memory per SM, 1 KB of it reserved per block).
+constexpr size_t kFusedBudget = 112 * 1024;
 }  // namespace
 
 template <typename T>
@@ -27,9 +32,15 @@ struct BatchPlan<T>::Group {
   int spb = 0, cpb = 0, rpb = 0;
   size_t smemZ = 0, smemY = 0, smemX = 0;
   int blocksZ = 0, blocksY = 0, blocksX = 0;
+  // fused plane passes: one block per plane, rows per x chunk (backward uses both halves of the
+  // forward's double buffer, so twice the rows)
+  bool fused = false;
+  int rowsF = 0, rowsB = 0, blocksP = 0;
+  size_t smemP = 0;
   T scale = T(0);
   DeviceBuffer dev;
-  size_t offViews = 0, offStartsZ = 0, offStartsY = 0, offStartsX = 0, offValues = 0, offSpaces = 0;
+  size_t offViews = 0, offStartsZ = 0, offStartsY = 0, offStartsX = 0, offStartsP = 0, offValues = 0,
+         offSpaces = 0;
   BatchView<T> view(size_t startsOff, T scaleValue) const {
     char* d = static_cast<char*>(dev.get());
     BatchView<T> v;
@@ -89,6 +100,8 @@ BatchPlan<T>::BatchPlan(std::vector<std::shared_ptr<TransformInternal<T>>> trans
   }
 
   // tile shapes per group (sized for the group's widest plane) and device tables
+  const char* planeEnv = std::getenv("SPFFT_GB300_BATCH_PLANE");
+  const std::string planeMode = planeEnv ? planeEnv : "";
   std::vector<std::unique_ptr<Group>> kept;
   for (auto& gp : groups_) {
     Group& g = *gp;
@@ -123,7 +136,25 @@ BatchPlan<T>::BatchPlan(std::vector<std::shared_ptr<TransformInternal<T>>> trans
     fast_dispatch<T>(FastOp::XSmem, g.nx, g.r2c, a);
     g.smemX = sm;
     g.rpb = std::min(g.rpb, g.ny);
-    if (g.smemZ > optin || g.smemY > optin || g.smemX > optin) {
+    // Fused plane passes for cubic planes whose compact plane fits two blocks per SM (the y and x
+    // passes then never write the compact planes to HBM). SPFFT_GB300_BATCH_PLANE=split|fused
+    // forces one (fused up to the opt-in shared memory limit).
+    if (g.nx == g.ny && planeMode != "split") {
+      const size_t limit = planeMode == "fused" ? optin : kFusedBudget;
+      for (int rows = 16; rows >= 2; rows /= 2) {
+        a.param = rows;
+        fast_dispatch<T>(FastOp::PlaneSmem, g.nx, g.r2c, a);
+        if (sm <= limit) {
+          g.fused = true;
+          g.rowsF = std::min(rows, g.ny);
+          g.rowsB = std::min(2 * rows, g.ny);
+          g.smemP = sm;
+          break;
+        }
+      }
+    }
+    const bool splitFits = g.smemY <= optin && g.smemX <= optin;
+    if (g.smemZ > optin || (!g.fused && !splitFits)) {
       for (int t : g.members) fallback_.push_back(t);
       continue;
     }
@@ -132,23 +163,27 @@ BatchPlan<T>::BatchPlan(std::vector<std::shared_ptr<TransformInternal<T>>> trans
     g.offStartsZ = align_up(m * sizeof(PlanView<T>));
     g.offStartsY = g.offStartsZ + align_up((m + 1) * sizeof(int));
     g.offStartsX = g.offStartsY + align_up((m + 1) * sizeof(int));
-    g.offValues = g.offStartsX + align_up((m + 1) * sizeof(int));
+    g.offStartsP = g.offStartsX + align_up((m + 1) * sizeof(int));
+    g.offValues = g.offStartsP + align_up((m + 1) * sizeof(int));
     g.offSpaces = g.offValues + align_up(m * sizeof(T*));
     g.dev = DeviceBuffer(g.offSpaces + align_up(m * sizeof(T*)));
-    std::vector<int> sz(m + 1, 0), sy(m + 1, 0), sx(m + 1, 0);
+    std::vector<int> sz(m + 1, 0), sy(m + 1, 0), sx(m + 1, 0), sp(m + 1, 0);
     for (size_t i = 0; i < m; ++i) {
       const IndexPlan& ip = tp_[g.members[i]]->index_plan();
       sz[i + 1] = sz[i] + (ip.num_sticks() + g.spb - 1) / g.spb;
       sy[i + 1] = sy[i] + ((ip.num_columns() + g.cpb - 1) / g.cpb) * ip.dimZ;
       sx[i + 1] = sx[i] + ((ip.dimY + g.rpb - 1) / g.rpb) * ip.dimZ;
+      sp[i + 1] = sp[i] + ip.dimZ;
     }
     g.blocksZ = sz[m];
     g.blocksY = sy[m];
     g.blocksX = sx[m];
+    g.blocksP = sp[m];
     char* d = static_cast<char*>(g.dev.get());
     check_cuda(cudaMemcpy(d + g.offStartsZ, sz.data(), (m + 1) * sizeof(int), cudaMemcpyHostToDevice));
     check_cuda(cudaMemcpy(d + g.offStartsY, sy.data(), (m + 1) * sizeof(int), cudaMemcpyHostToDevice));
     check_cuda(cudaMemcpy(d + g.offStartsX, sx.data(), (m + 1) * sizeof(int), cudaMemcpyHostToDevice));
+    check_cuda(cudaMemcpy(d + g.offStartsP, sp.data(), (m + 1) * sizeof(int), cudaMemcpyHostToDevice));
     kept.push_back(std::move(gp));
   }
   groups_ = std::move(kept);
@@ -176,7 +211,25 @@ BatchPlan<T>::~BatchPlan() {
 
 template <typename T>
 int BatchPlan<T>::launches_per_pair() const {
-  return 6 * static_cast<int>(groups_.size()) + 6 * static_cast<int>(fallback_.size());
+  int n = 6 * static_cast<int>(fallback_.size());
+  for (const auto& g : groups_) n += g->fused ? 4 : 6;
+  return n;
+}
+
+template <typename T>
+int BatchPlan<T>::transform_path(int t) const {
+  if (t < 0 || t >= static_cast<int>(tp_.size())) throw InvalidParameterError();
+  for (const auto& g : groups_) {
+    if (std::find(g->members.begin(), g->members.end(), t) != g->members.end()) return g->fused ? 2 : 1;
+  }
+  return 0;
+}
+
+template <typename T>
+int BatchPlan<T>::num_fused_groups() const {
+  int n = 0;
+  for (const auto& g : groups_) n += g->fused ? 1 : 0;
+  return n;
 }
 
 // Plan views embed the grids' scratch pointers; refresh them if a grid's scratch moved (a grid
@@ -274,28 +327,48 @@ void launch(FastOp op, int n, bool r2c, const BatchView<T>& bv, int blocks, size
 }
 }  // namespace
 
+// One pass of one group: pass 0 = z, 1 = y (or the fused plane pass), 2 = x (nothing when fused);
+// direction 0 backward, 1 forward.
+template <typename T>
+void BatchPlan<T>::run_pass(Group& g, int pass, int direction, bool scaled, cudaStream_t s) {
+  char* d = static_cast<char*>(g.dev.get());
+  const T* const* spaces = reinterpret_cast<const T* const*>(d + g.offSpaces);
+  T* const* spacesOut = reinterpret_cast<T* const*>(d + g.offSpaces);
+  if (pass == 0) {
+    BatchView<T> bz = g.view(g.offStartsZ, direction == 1 && scaled ? g.scale : T(0));
+    if (direction == 0) bz.in = reinterpret_cast<const T* const*>(d + g.offValues);
+    else bz.out = reinterpret_cast<T* const*>(d + g.offValues);
+    launch(direction == 0 ? FastOp::BatchZBackward : FastOp::BatchZForward, g.nz, g.r2c, bz, g.blocksZ, g.smemZ,
+           g.spb, s);
+  } else if (g.fused) {
+    if (pass != 1) return;
+    BatchView<T> bp = g.view(g.offStartsP, T(0));
+    if (direction == 0) {
+      bp.out = spacesOut;
+      launch(FastOp::BatchPlaneBackward, g.nx, g.r2c, bp, g.blocksP, g.smemP, g.rowsB, s);
+    } else {
+      bp.in = spaces;
+      launch(FastOp::BatchPlaneForward, g.nx, g.r2c, bp, g.blocksP, g.smemP, g.rowsF, s);
+    }
+  } else if (pass == 1) {
+    launch(direction == 0 ? FastOp::BatchYBackward : FastOp::BatchYForward, g.ny, g.r2c, g.view(g.offStartsY, T(0)),
+           g.blocksY, g.smemY, g.cpb, s);
+  } else {
+    BatchView<T> bx = g.view(g.offStartsX, T(0));
+    if (direction == 0) bx.out = spacesOut;
+    else bx.in = spaces;
+    launch(direction == 0 ? FastOp::BatchXBackward : FastOp::BatchXForward, g.nx, g.r2c, bx, g.blocksX, g.smemX,
+           g.rpb, s);
+  }
+}
+
 template <typename T>
 void BatchPlan<T>::run_group(Group& g, int what, bool scaled, cudaStream_t s) {
-  char* d = static_cast<char*>(g.dev.get());
   if (what & 1) {
-    BatchView<T> bz = g.view(g.offStartsZ, T(0));
-    bz.in = reinterpret_cast<const T* const*>(d + g.offValues);
-    launch(FastOp::BatchZBackward, g.nz, g.r2c, bz, g.blocksZ, g.smemZ, g.spb, s);
-    const BatchView<T> by = g.view(g.offStartsY, T(0));
-    launch(FastOp::BatchYBackward, g.ny, g.r2c, by, g.blocksY, g.smemY, g.cpb, s);
-    BatchView<T> bx = g.view(g.offStartsX, T(0));
-    bx.out = reinterpret_cast<T* const*>(d + g.offSpaces);
-    launch(FastOp::BatchXBackward, g.nx, g.r2c, bx, g.blocksX, g.smemX, g.rpb, s);
+    for (int pass = 0; pass < 3; ++pass) run_pass(g, pass, 0, false, s);
   }
   if (what & 2) {
-    BatchView<T> bx = g.view(g.offStartsX, T(0));
-    bx.in = reinterpret_cast<const T* const*>(d + g.offSpaces);
-    launch(FastOp::BatchXForward, g.nx, g.r2c, bx, g.blocksX, g.smemX, g.rpb, s);
-    const BatchView<T> by = g.view(g.offStartsY, T(0));
-    launch(FastOp::BatchYForward, g.ny, g.r2c, by, g.blocksY, g.smemY, g.cpb, s);
-    BatchView<T> bz = g.view(g.offStartsZ, scaled ? g.scale : T(0));
-    bz.out = reinterpret_cast<T* const*>(d + g.offValues);
-    launch(FastOp::BatchZForward, g.nz, g.r2c, bz, g.blocksZ, g.smemZ, g.spb, s);
+    for (int pass = 2; pass >= 0; --pass) run_pass(g, pass, 1, scaled, s);
   }
 }
 
@@ -360,43 +433,15 @@ void BatchPlan<T>::stage_times(int direction, bool scaled, cudaStream_t stream, 
   upload_views();
   StageEvents ev{};
   for (auto& e : ev.ev) check_cuda(cudaEventCreate(&e));
-  auto pass = [&](FastOp op, int which) {
-    for (auto& gp : groups_) {
-      Group& g = *gp;
-      char* d = static_cast<char*>(g.dev.get());
-      if (which == 0) {
-        BatchView<T> bz = g.view(g.offStartsZ, scaled ? g.scale : T(0));
-        if (op == FastOp::BatchZBackward) bz.in = reinterpret_cast<const T* const*>(d + g.offValues);
-        else bz.out = reinterpret_cast<T* const*>(d + g.offValues);
-        launch(op, g.nz, g.r2c, bz, g.blocksZ, g.smemZ, g.spb, stream);
-      } else if (which == 1) {
-        launch(op, g.ny, g.r2c, g.view(g.offStartsY, T(0)), g.blocksY, g.smemY, g.cpb, stream);
-      } else {
-        BatchView<T> bx = g.view(g.offStartsX, T(0));
-        if (op == FastOp::BatchXBackward) bx.out = reinterpret_cast<T* const*>(d + g.offSpaces);
-        else bx.in = reinterpret_cast<const T* const*>(d + g.offSpaces);
-        launch(op, g.nx, g.r2c, bx, g.blocksX, g.smemX, g.rpb, stream);
-      }
-    }
-  };
   try {
+    // backward runs the passes z, y, x; forward x, y, z (event i+1 closes the i-th of them)
     check_cuda(cudaEventRecord(ev.ev[0], stream));
-    if (direction == 0) {
-      pass(FastOp::BatchZBackward, 0);
-      check_cuda(cudaEventRecord(ev.ev[1], stream));
-      pass(FastOp::BatchYBackward, 1);
-      check_cuda(cudaEventRecord(ev.ev[2], stream));
-      pass(FastOp::BatchXBackward, 2);
-      run_fallback(1, scaled, stream);
-    } else {
-      pass(FastOp::BatchXForward, 2);
-      check_cuda(cudaEventRecord(ev.ev[1], stream));
-      pass(FastOp::BatchYForward, 1);
-      check_cuda(cudaEventRecord(ev.ev[2], stream));
-      pass(FastOp::BatchZForward, 0);
-      run_fallback(2, scaled, stream);
+    for (int i = 0; i < 3; ++i) {
+      const int pass = direction == 0 ? i : 2 - i;
+      for (auto& gp : groups_) run_pass(*gp, pass, direction, scaled, stream);
+      if (i == 2) run_fallback(direction == 0 ? 1 : 2, scaled, stream);
+      check_cuda(cudaEventRecord(ev.ev[i + 1], stream));
     }
-    check_cuda(cudaEventRecord(ev.ev[3], stream));
     check_cuda(cudaEventSynchronize(ev.ev[3]));
     for (int i = 0; i < 3; ++i) check_cuda(cudaEventElapsedTime(&ms[i], ev.ev[i], ev.ev[i + 1]));
   } catch (...) {

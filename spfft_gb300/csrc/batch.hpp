@@ -45,7 +45,8 @@ public:
   // The same for one direction (what: 1 backward, 2 forward, 3 backward then forward).
   void graph(int what, bool scaled, cudaStream_t stream);
   // One direction (0 backward, 1 forward) with the groups run pass by pass on `stream` and events
-  // between the passes; waits and returns the three pass times in milliseconds.
+  // between the passes; waits and returns the three pass times in milliseconds (z, y, x for the
+  // backward, x, y, z for the forward; a fused group runs its plane kernel in the y slot).
   void stage_times(int direction, bool scaled, cudaStream_t stream, float ms[3]);
 
   int num_transforms() const { return static_cast<int>(tp_.size()); }
@@ -57,6 +58,10 @@ public:
   const T* bound_space(int t) const { return bound_ ? spaces_[t] : nullptr; }
   int num_groups() const { return static_cast<int>(groups_.size()); }
   int num_unbatched() const { return static_cast<int>(fallback_.size()); }
+  // Groups whose y and x passes run as one fused plane kernel.
+  int num_fused_groups() const;
+  // 0 unbatched, 1 batched with split y and x passes, 2 batched with the fused plane pass.
+  int transform_path(int t) const;
   // Kernel launches of one backward + forward pair.
   int launches_per_pair() const;
 
@@ -66,6 +71,7 @@ private:
   void check_bound() const;
   // Passes of one group on `s`: bit 0 backward, bit 1 forward (after the backward).
   void run_group(Group& g, int what, bool scaled, cudaStream_t s);
+  void run_pass(Group& g, int pass, int direction, bool scaled, cudaStream_t s);
   void run_fallback(int what, bool scaled, cudaStream_t s);
   // Every group (and the unbatched transforms) as concurrent branches of `stream`.
   void run(int what, bool scaled, cudaStream_t stream);

@@ -75,6 +75,21 @@ __global__ void __launch_bounds__(kThreads) x_forward_batch(const BatchView<S> b
   x_forward_body<S, A, NX, R2C>(p, bv.in[t], rpb, lb % gx, lb / gx, &sExp);
 }
 
+// Fused y + x passes, one block per plane (cubic planes): starts count planes.
+template <typename S, typename A, int N, bool R2C>
+__global__ void __launch_bounds__(kPlaneThreads) plane_backward_batch(const BatchView<S> bv, int rows) {
+  __shared__ int sExp;
+  const int t = find_transform(bv.starts, bv.count, blockIdx.x);
+  plane_backward_body<S, A, N, N, R2C>(bv.views[t], bv.out[t], rows, blockIdx.x - bv.starts[t], &sExp);
+}
+
+template <typename S, typename A, int N, bool R2C>
+__global__ void __launch_bounds__(kPlaneThreads) plane_forward_batch(const BatchView<S> bv, int rows) {
+  __shared__ int sExp;
+  const int t = find_transform(bv.starts, bv.count, blockIdx.x);
+  plane_forward_body<S, A, N, N, R2C>(bv.views[t], bv.in[t], rows, blockIdx.x - bv.starts[t], &sExp);
+}
+
 template <typename S, typename A, int N>
 struct BatchKernels {
   static cudaError_t prepare(size_t maxSmem) {
@@ -86,6 +101,10 @@ struct BatchKernels {
     if (e == cudaSuccess) e = allow_dynamic_smem(x_backward_batch<S, A, N, true>, maxSmem);
     if (e == cudaSuccess) e = allow_dynamic_smem(x_forward_batch<S, A, N, false>, maxSmem);
     if (e == cudaSuccess) e = allow_dynamic_smem(x_forward_batch<S, A, N, true>, maxSmem);
+    if (e == cudaSuccess) e = allow_dynamic_smem(plane_backward_batch<S, A, N, false>, maxSmem);
+    if (e == cudaSuccess) e = allow_dynamic_smem(plane_backward_batch<S, A, N, true>, maxSmem);
+    if (e == cudaSuccess) e = allow_dynamic_smem(plane_forward_batch<S, A, N, false>, maxSmem);
+    if (e == cudaSuccess) e = allow_dynamic_smem(plane_forward_batch<S, A, N, true>, maxSmem);
     return e;
   }
 };

@@ -35,6 +35,7 @@ namespace fast {
 
 constexpr int kThreads = 256;       // z-pass blocks
 constexpr int kPlaneThreads = 512;  // plane blocks (one plane per block, so more warps per SM)
+constexpr int kBatchPlaneThreads = 256;  // batched plane blocks (two blocks per SM)
 
 extern __shared__ __align__(16) unsigned char g_fast_smem[];
 
@@ -86,6 +87,19 @@ __device__ __forceinline__ int max_exponent(double2 v) {
 // Scale exponent k for a block whose largest biased binary64 exponent is e: 2^k * max in [1, 2).
 // Zero, subnormal-only and non-finite blocks use k = 0.
 __device__ __forceinline__ int block_scale(int e) { return (e == 0 || e == 2047) ? 0 : 1023 - e; }
+
+// Division by a block-uniform runtime divisor d in [1, 2^16) for numerators n in [0, 2^16): one
+// high multiply by m = floor(2^32 / d) + 1 instead of the division sequence. Exact because
+// n * (m - 2^32 / d) < n * 1 < 2^32 / d, i.e. the error stays below one step of n / d.
+struct FastDiv {
+  unsigned m;
+  int d;
+  __device__ __forceinline__ explicit FastDiv(int divisor)
+      : m(divisor > 1 ? 0xFFFFFFFFu / static_cast<unsigned>(divisor) + 1u : 0u), d(divisor) {}
+  __device__ __forceinline__ int div(int n) const {
+    return d > 1 ? static_cast<int>(__umulhi(static_cast<unsigned>(n), m)) : n;
+  }
+};
 
 // Asynchronous global -> shared copy of one complex value (cp.async, 8 or 16 bytes). Lets a
 // thread keep many loads in flight instead of waiting on each.
@@ -168,6 +182,7 @@ __device__ __forceinline__ void z_backward_body(const PlanView<S>& p, const S* _
   CA* buf = tw + NZ;
   const int s0 = bx * spb;
   const int nsb = min(spb, p.numSticks - s0);
+  const FastDiv dns(nsb);
 
   load_twiddles<S, A>(tw, p.twz, NZ);
   for (int i = threadIdx.x; i < nsb * PZ; i += blockDim.x) buf[i] = czero<A>();
@@ -208,7 +223,7 @@ __device__ __forceinline__ void z_backward_body(const PlanView<S>& p, const S* _
   __syncthreads();
   CS* sticks = reinterpret_cast<CS*>(p.sticks) + s0;
   for (int i = threadIdx.x; i < nsb * Az; i += blockDim.x) {
-    const int k1 = i / nsb, sl = i - k1 * nsb;
+    const int k1 = dns.div(i), sl = i - k1 * nsb;
     CA v[Bz];
     fft_pass2<NZ, +1>(buf + sl * PZ, 1, k1, v);
 #pragma unroll
@@ -237,11 +252,12 @@ __device__ __forceinline__ void z_forward_body(const PlanView<S>& p, S* __restri
   CA* buf = tw + NZ;
   const int s0 = bx * spb;
   const int nsb = min(spb, p.numSticks - s0);
+  const FastDiv dns(nsb);
 
   load_twiddles<S, A>(tw, p.twz, NZ);
   const CS* sticks = reinterpret_cast<const CS*>(p.sticks) + s0;
   for (int i = threadIdx.x; i < NZ * nsb; i += blockDim.x) {
-    const int z = i / nsb, sl = i - z * nsb;
+    const int z = dns.div(i), sl = i - z * nsb;
     cp_async_c(buf + sl * PZ + z, sticks + static_cast<size_t>(z) * p.numSticks + sl);
   }
   // the pitch padding slots are never read; zero them so the block scale ignores them
@@ -258,7 +274,7 @@ __device__ __forceinline__ void z_forward_body(const PlanView<S>& p, S* __restri
   }
   __syncthreads();
   for (int i = threadIdx.x; i < nsb * Az; i += blockDim.x) {
-    const int k1 = i / nsb, sl = i - k1 * nsb;
+    const int k1 = dns.div(i), sl = i - k1 * nsb;
     CA v[Bz];
     fft_pass2<NZ, -1>(buf + sl * PZ, 1, k1, v);
 #pragma unroll
@@ -355,17 +371,17 @@ __device__ __forceinline__ void plane_load_tables(const PlanView<S>& p,
 }
 
 template <typename S, typename A, int NX, int NY, bool R2C>
-__global__ void __launch_bounds__(kPlaneThreads) plane_backward(const PlanView<S> p,
-                                                                S* __restrict__ space, int rows) {
+__device__ __forceinline__ void plane_backward_body(const PlanView<S>& p, S* __restrict__ space, int rows,
+                                                    int z, int* sExpPtr) {
   using TT = Types<S, A>;
   using CS = typename TT::CS;
   using CA = typename TT::CA;
   using L = PlaneLayout<NX, NY, R2C>;
   constexpr int Ay = Shape<NY>::A, By = Shape<NY>::B;
   constexpr int Ax = L::Ax, Bx = L::Bx;
-  __shared__ int sExp;
-  const int z = blockIdx.x;
+  int& sExp = *sExpPtr;
   const int nc = p.numColumns;
+  const FastDiv dnc(nc);
   PlaneSmem<CA, NX, NY, R2C> s(nc);
   plane_load_tables<S, A, NX, NY, R2C>(p, s);
   for (int i = threadIdx.x; i < NY * nc; i += blockDim.x) s.P[i] = czero<A>();
@@ -384,12 +400,12 @@ __global__ void __launch_bounds__(kPlaneThreads) plane_backward(const PlanView<S
 
   // y-FFT on every compact column, result rows left in transposed order
   for (int i = threadIdx.x; i < nc * By; i += blockDim.x) {
-    const int b = i / nc, c = i - b * nc;
+    const int b = dnc.div(i), c = i - b * nc;
     fft_pass1<NY, +1>(s.P + c, nc, b, s.twy);
   }
   __syncthreads();
   for (int i = threadIdx.x; i < nc * Ay; i += blockDim.x) {
-    const int k1 = i / nc, c = i - k1 * nc;
+    const int k1 = dnc.div(i), c = i - k1 * nc;
     CA v[By];
     fft_pass2<NY, +1>(s.P + c, nc, k1, v);
 #pragma unroll
@@ -447,17 +463,24 @@ __global__ void __launch_bounds__(kPlaneThreads) plane_backward(const PlanView<S
 }
 
 template <typename S, typename A, int NX, int NY, bool R2C>
-__global__ void __launch_bounds__(kPlaneThreads) plane_forward(const PlanView<S> p,
-                                                               const S* __restrict__ space, int rows) {
+__global__ void __launch_bounds__(kPlaneThreads) plane_backward(const PlanView<S> p,
+                                                                S* __restrict__ space, int rows) {
+  __shared__ int sExp;
+  plane_backward_body<S, A, NX, NY, R2C>(p, space, rows, blockIdx.x, &sExp);
+}
+
+template <typename S, typename A, int NX, int NY, bool R2C>
+__device__ __forceinline__ void plane_forward_body(const PlanView<S>& p, const S* __restrict__ space, int rows,
+                                                   int z, int* sExpPtr) {
   using TT = Types<S, A>;
   using CS = typename TT::CS;
   using CA = typename TT::CA;
   using L = PlaneLayout<NX, NY, R2C>;
   constexpr int Ay = Shape<NY>::A, By = Shape<NY>::B;
   constexpr int Ax = L::Ax, Bx = L::Bx;
-  __shared__ int sExp;
-  const int z = blockIdx.x;
+  int& sExp = *sExpPtr;
   const int nc = p.numColumns;
+  const FastDiv dnc(nc);
   PlaneSmem<CA, NX, NY, R2C> s(nc);
   plane_load_tables<S, A, NX, NY, R2C>(p, s);
 
@@ -536,7 +559,7 @@ __global__ void __launch_bounds__(kPlaneThreads) plane_forward(const PlanView<S>
     if (R2C) {
       // X[k] = (Z[k] + conj Z[M-k]) / 2 - i/2 e^{-2 pi i k/N} (Z[k] - conj Z[M-k]), Z[M] = Z[0]
       for (int i = threadIdx.x; i < nr * nc; i += blockDim.x) {
-        const int rl = i / nc, c = i - rl * nc;
+        const int rl = dnc.div(i), c = i - rl * nc;
         const int kk = p.columnX[c];
         const CA* wrow = wbase + rl * L::WP;
         const CA zk = wrow[L::wpos(transposed_pos<L::LX>(kk % L::M))];
@@ -550,12 +573,12 @@ __global__ void __launch_bounds__(kPlaneThreads) plane_forward(const PlanView<S>
   }
 
   for (int i = threadIdx.x; i < nc * By; i += blockDim.x) {
-    const int b = i / nc, c = i - b * nc;
+    const int b = dnc.div(i), c = i - b * nc;
     fft_pass1<NY, -1>(s.P + c, nc, b, s.twy);
   }
   __syncthreads();
   for (int i = threadIdx.x; i < nc * Ay; i += blockDim.x) {
-    const int k1 = i / nc, c = i - k1 * nc;
+    const int k1 = dnc.div(i), c = i - k1 * nc;
     CA v[By];
     fft_pass2<NY, -1>(s.P + c, nc, k1, v);
 #pragma unroll
@@ -566,6 +589,13 @@ __global__ void __launch_bounds__(kPlaneThreads) plane_forward(const PlanView<S>
   for (int st = threadIdx.x; st < p.numSticks; st += blockDim.x) {
     sticks[st] = to_storage(s.P[transposed_pos<NY>(p.stickY[st]) * nc + p.stickColumn[st]], k);
   }
+}
+
+template <typename S, typename A, int NX, int NY, bool R2C>
+__global__ void __launch_bounds__(kPlaneThreads) plane_forward(const PlanView<S> p,
+                                                               const S* __restrict__ space, int rows) {
+  __shared__ int sExp;
+  plane_forward_body<S, A, NX, NY, R2C>(p, space, rows, blockIdx.x, &sExp);
 }
 
 // ================================================================================================
@@ -635,6 +665,7 @@ __device__ __forceinline__ void y_backward_body(const PlanView<S>& p, int cpb, i
   CA* buf = tw + NY;
   const int nc = p.numColumns;
   const int c0 = bx * cpb, ncb = min(cpb, nc - c0);
+  const FastDiv dncb(ncb);
   load_twiddles<S, A>(tw, p.twy, NY);
   for (int i = threadIdx.x; i < NY * ncb; i += blockDim.x) buf[i] = czero<A>();
   __syncthreads();
@@ -649,13 +680,13 @@ __device__ __forceinline__ void y_backward_body(const PlanView<S>& p, int cpb, i
   const int k = convert_block<S, A>(buf, NY * ncb, &sExp);
   if (p.r2c && c0 == 0 && p.columnX[0] == 0) line_fill(buf, NY, ncb);
   for (int i = threadIdx.x; i < ncb * By; i += blockDim.x) {
-    const int b = i / ncb, c = i - b * ncb;
+    const int b = dncb.div(i), c = i - b * ncb;
     fft_pass1<NY, +1>(buf + c, ncb, b, tw);
   }
   __syncthreads();
   CS* planes = reinterpret_cast<CS*>(p.planes) + static_cast<size_t>(z) * NY * nc + c0;
   for (int i = threadIdx.x; i < ncb * Ay; i += blockDim.x) {
-    const int k1 = i / ncb, c = i - k1 * ncb;
+    const int k1 = dncb.div(i), c = i - k1 * ncb;
     CA v[By];
     fft_pass2<NY, +1>(buf + c, ncb, k1, v);
 #pragma unroll
@@ -681,10 +712,11 @@ __device__ __forceinline__ void y_forward_body(const PlanView<S>& p, int cpb, in
   CA* buf = tw + NY;
   const int nc = p.numColumns;
   const int c0 = bx * cpb, ncb = min(cpb, nc - c0);
+  const FastDiv dncb(ncb);
   load_twiddles<S, A>(tw, p.twy, NY);
   const CS* planes = reinterpret_cast<const CS*>(p.planes) + static_cast<size_t>(z) * NY * nc + c0;
   for (int i = threadIdx.x; i < NY * ncb; i += blockDim.x) {
-    const int y = i / ncb, c = i - y * ncb;
+    const int y = dncb.div(i), c = i - y * ncb;
     cp_async_c(buf + i, planes + static_cast<size_t>(y) * nc + c);
   }
   cp_async_commit();
@@ -692,12 +724,12 @@ __device__ __forceinline__ void y_forward_body(const PlanView<S>& p, int cpb, in
   __syncthreads();
   const int k = convert_block<S, A>(buf, NY * ncb, &sExp);
   for (int i = threadIdx.x; i < ncb * By; i += blockDim.x) {
-    const int b = i / ncb, c = i - b * ncb;
+    const int b = dncb.div(i), c = i - b * ncb;
     fft_pass1<NY, -1>(buf + c, ncb, b, tw);
   }
   __syncthreads();
   for (int i = threadIdx.x; i < ncb * Ay; i += blockDim.x) {
-    const int k1 = i / ncb, c = i - k1 * ncb;
+    const int k1 = dncb.div(i), c = i - k1 * ncb;
     CA v[By];
     fft_pass2<NY, -1>(buf + c, ncb, k1, v);
 #pragma unroll
@@ -836,6 +868,7 @@ __device__ __forceinline__ void x_forward_body(const PlanView<S>& p, const S* __
   constexpr int Ax = L::Ax, Bx = L::Bx;
   int& sExp = *sExpPtr;
   const int nc = p.numColumns, ny = p.dimY;
+  const FastDiv dnc(nc);
   const int y0 = bx * rpb, nr = min(rpb, ny - y0);
   RowSmem<CA, NX, R2C> s(nc, rpb);
   row_load_tables<S, A, NX, R2C>(p, s);
@@ -888,7 +921,7 @@ __device__ __forceinline__ void x_forward_body(const PlanView<S>& p, const S* __
   __syncthreads();
   if (R2C) {
     for (int i = threadIdx.x; i < nr * nc; i += blockDim.x) {
-      const int rl = i / nc, c = i - rl * nc;
+      const int rl = dnc.div(i), c = i - rl * nc;
       const int kk = p.columnX[c];
       const CA* wrow = s.W + rl * L::WP;
       const CA zk = wrow[L::wpos(transposed_pos<L::LX>(kk % L::M))];

@@ -31,7 +31,10 @@ enum class FastOp {
   BatchYBackward,
   BatchYForward,
   BatchXBackward,
-  BatchXForward
+  BatchXForward,
+  // batched fused plane passes (n = the cubic plane size; param = rows per x chunk)
+  BatchPlaneBackward,
+  BatchPlaneForward
 };
 
 template <typename T>

@@ -105,3 +105,43 @@ def test_batch_rejects_shared_grids_and_mixed_precision(lib):
     tf = sp.Transform(1, sp.SPFFT_PU_GPU, 0, 32, 32, 32, len(idx), 0, idx, dtype="float32")
     with pytest.raises(ValueError):
         sp.Batch([t1, tf])
+
+
+@pytest.mark.parametrize("mode", ["split", "fused"])
+@pytest.mark.parametrize("dtype", ["float64", "float32"])
+def test_batch_plane_pass_modes(lib, dtype, mode, monkeypatch):
+    """Both plane-pass forms of the batched kernels (split y and x passes with the compact planes
+    in HBM; one fused kernel per plane), forced at batch creation, against the oracle, with the
+    192^3 R2C shape of the benchmark among them."""
+    monkeypatch.setenv("SPFFT_GB300_BATCH_PLANE", mode)
+    rng = np.random.default_rng(5)
+    specs = [(64, 16, 0), (64, 20, 0), (60, 15, 1), (192, 48, 1), ((13, 12, 11), 0, 0)]
+    if dtype == "float64" and mode == "fused":
+        specs = specs[:3] + specs[4:]  # the 192^3 compact plane in double-float exceeds one block
+    items = _make(dtype, specs, rng)
+    batch = sp.Batch([it["tr"] for it in items])
+    want_path = 2 if mode == "fused" else 1
+    assert [batch.transform_path(i) for i in range(len(items) - 1)] == [want_path] * (len(items) - 1)
+    assert batch.transform_path(len(items) - 1) == 0
+    batch.bind([it["vals"] for it in items], [it["space"] for it in items])
+    host_vals = []
+    for it in items:
+        v = rng.uniform(-1, 1, len(it["idx"])) + 1j * rng.uniform(-1, 1, len(it["idx"]))
+        if it["ttype"] == 1:
+            v[(it["idx"] == 0).all(axis=1)] = v[(it["idx"] == 0).all(axis=1)].real
+        host_vals.append(v)
+        it["vals"].copy_(torch.from_numpy(v).to(it["vals"].dtype))
+    stream = torch.cuda.Stream()
+    torch.cuda.synchronize()
+    batch.backward(stream)
+    stream.synchronize()
+    for it, v in zip(items, host_vals):
+        assert rel_l2(it["space"].cpu().numpy(), it["oracle"].backward(v)) <= TOL[dtype], it["dims"]
+    batch.forward(sp.SPFFT_NO_SCALING, stream)
+    stream.synchronize()
+    for it in items:
+        want = it["oracle"].forward(it["space"].cpu().numpy().astype(
+            np.complex128 if it["ttype"] == 0 else np.float64))
+        assert rel_l2(it["vals"].cpu().numpy(), want) <= TOL[dtype], it["dims"]
+    ms_b = batch.stage_times(0, sp.SPFFT_NO_SCALING, stream)
+    assert len(ms_b) == 3 and all(t >= 0 for t in ms_b)
