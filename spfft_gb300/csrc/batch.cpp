@@ -145,9 +145,12 @@ BatchPlan<T>::BatchPlan(std::vector<std::shared_ptr<TransformInternal<T>>> trans
         a.param = rows;
         fast_dispatch<T>(FastOp::PlaneSmem, g.nx, g.r2c, a);
         if (sm <= limit) {
+          // the chunk buffer holds 2 * rows rows: the backward and (single-buffered, which measured
+          // faster than double-buffered half chunks with two blocks per SM) the forward transform
+          // chunks of that many rows
           g.fused = true;
-          g.rowsF = std::min(rows, g.ny);
           g.rowsB = std::min(2 * rows, g.ny);
+          g.rowsF = g.rowsB;
           g.smemP = sm;
           break;
         }
@@ -314,13 +317,14 @@ void BatchPlan<T>::check_bound() const {
 namespace {
 template <typename T>
 void launch(FastOp op, int n, bool r2c, const BatchView<T>& bv, int blocks, size_t smem, int param,
-            cudaStream_t s) {
+            cudaStream_t s, int param2 = 0) {
   if (blocks == 0) return;
   FastArgs<T> a;
   a.batch = &bv;
   a.blocks = blocks;
   a.smem = smem;
   a.param = param;
+  a.param2 = param2;
   a.stream = s;
   fast_dispatch<T>(op, n, r2c, a);
   check_launch(cudaGetLastError());
@@ -348,7 +352,7 @@ void BatchPlan<T>::run_pass(Group& g, int pass, int direction, bool scaled, cuda
       launch(FastOp::BatchPlaneBackward, g.nx, g.r2c, bp, g.blocksP, g.smemP, g.rowsB, s);
     } else {
       bp.in = spaces;
-      launch(FastOp::BatchPlaneForward, g.nx, g.r2c, bp, g.blocksP, g.smemP, g.rowsF, s);
+      launch(FastOp::BatchPlaneForward, g.nx, g.r2c, bp, g.blocksP, g.smemP, g.rowsF, s, g.rowsB);
     }
   } else if (pass == 1) {
     launch(direction == 0 ? FastOp::BatchYBackward : FastOp::BatchYForward, g.ny, g.r2c, g.view(g.offStartsY, T(0)),

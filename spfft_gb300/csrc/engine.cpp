@@ -123,6 +123,8 @@ GpuPlan<T>::GpuPlan(const IndexPlan& p, int device) {
     size_t offset;
   };
   std::vector<T> tz(twz.begin(), twz.end()), ty(twy.begin(), twy.end()), tx(twx.begin(), twx.end());
+  std::vector<int> planePos(ns);
+  for (int st = 0; st < ns; ++st) planePos[st] = p.stickY[st] * ncol + p.stickColumn[st];
   std::vector<Part> parts = {
       {tz.data(), tz.size() * sizeof(T), 0},
       {ty.data(), ty.size() * sizeof(T), 0},
@@ -135,6 +137,7 @@ GpuPlan<T>::GpuPlan(const IndexPlan& p, int device) {
       {p.entryUser.data(), p.entryUser.size() * sizeof(int), 0},
       {p.stickEntryStart.data(), p.stickEntryStart.size() * sizeof(int), 0},
       {p.hermitianWeight.data(), p.hermitianWeight.size(), 0},
+      {planePos.data(), planePos.size() * sizeof(int), 0},
   };
   size_t total = 0;
   for (auto& part : parts) {
@@ -256,6 +259,7 @@ GpuPlan<T>::GpuPlan(const IndexPlan& p, int device) {
   base_.twx = reinterpret_cast<const T*>(d + parts[2].offset);
   base_.stickColumn = reinterpret_cast<const int*>(d + parts[3].offset);
   base_.stickY = reinterpret_cast<const int*>(d + parts[4].offset);
+  base_.stickPlanePos = reinterpret_cast<const int*>(d + parts[11].offset);
   base_.columnX = reinterpret_cast<const int*>(d + parts[5].offset);
   base_.columnStickStart = reinterpret_cast<const int*>(d + parts[6].offset);
   base_.entryPos = reinterpret_cast<const int*>(d + parts[7].offset);

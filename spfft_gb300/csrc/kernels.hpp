@@ -28,6 +28,7 @@ struct PlanView {
   const T* twx;
   const int* stickColumn;
   const int* stickY;
+  const int* stickPlanePos;  // stickY * numColumns + stickColumn: the stick's slot in a compact plane
   const int* columnX;
   const int* columnStickStart;
   const int* entryPos;

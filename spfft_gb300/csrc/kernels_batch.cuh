@@ -84,10 +84,10 @@ __global__ void __launch_bounds__(kPlaneThreads) plane_backward_batch(const Batc
 }
 
 template <typename S, typename A, int N, bool R2C>
-__global__ void __launch_bounds__(kPlaneThreads) plane_forward_batch(const BatchView<S> bv, int rows) {
+__global__ void __launch_bounds__(kPlaneThreads) plane_forward_batch(const BatchView<S> bv, int rows, int wRows) {
   __shared__ int sExp;
   const int t = find_transform(bv.starts, bv.count, blockIdx.x);
-  plane_forward_body<S, A, N, N, R2C>(bv.views[t], bv.in[t], rows, blockIdx.x - bv.starts[t], &sExp);
+  plane_forward_body<S, A, N, N, R2C>(bv.views[t], bv.in[t], rows, wRows, blockIdx.x - bv.starts[t], &sExp);
 }
 
 template <typename S, typename A, int N>

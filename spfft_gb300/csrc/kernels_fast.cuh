@@ -388,9 +388,20 @@ __device__ __forceinline__ void plane_backward_body(const PlanView<S>& p, S* __r
   __syncthreads();
 
   // sticks of this plane -> compact columns, all copies in flight at once
+  // (slot loads four at a time, so their latencies overlap)
   const CS* sticks = reinterpret_cast<const CS*>(p.sticks) + static_cast<size_t>(z) * p.numSticks;
-  for (int st = threadIdx.x; st < p.numSticks; st += blockDim.x) {
-    cp_async_c(s.P + p.stickY[st] * nc + p.stickColumn[st], sticks + st);
+  const int ns = p.numSticks;
+  for (int st0 = threadIdx.x; st0 < ns; st0 += 4 * blockDim.x) {
+    int pos[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int st = st0 + u * blockDim.x;
+      pos[u] = st < ns ? __ldg(p.stickPlanePos + st) : -1;
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      if (pos[u] >= 0) cp_async_c(s.P + pos[u], sticks + st0 + u * blockDim.x);
+    }
   }
   cp_async_commit();
   cp_async_wait<0>();
@@ -471,7 +482,7 @@ __global__ void __launch_bounds__(kPlaneThreads) plane_backward(const PlanView<S
 
 template <typename S, typename A, int NX, int NY, bool R2C>
 __device__ __forceinline__ void plane_forward_body(const PlanView<S>& p, const S* __restrict__ space, int rows,
-                                                   int z, int* sExpPtr) {
+                                                   int wRows, int z, int* sExpPtr) {
   using TT = Types<S, A>;
   using CS = typename TT::CS;
   using CA = typename TT::CA;
@@ -484,13 +495,15 @@ __device__ __forceinline__ void plane_forward_body(const PlanView<S>& p, const S
   PlaneSmem<CA, NX, NY, R2C> s(nc);
   plane_load_tables<S, A, NX, NY, R2C>(p, s);
 
-  // Row chunks of plane z are contiguous in the space buffer: stream chunk i+1 into the other
-  // half of W while chunk i is transformed.
+  // Row chunks of plane z are contiguous in the space buffer. When W holds two chunks (wRows >=
+  // 2 * rows) chunk i+1 streams into the other half while chunk i is transformed; otherwise each
+  // chunk is loaded after the previous one is done (the other blocks of the SM cover the wait).
   const CS* plane = reinterpret_cast<const CS*>(space + static_cast<size_t>(z) * NY * NX * (R2C ? 1 : 2));
   const int nchunks = (NY + rows - 1) / rows;
+  const bool dbuf = 2 * rows <= wRows;
   auto issue_chunk = [&](int chunk) {
     const int r0 = chunk * rows, nr = min(rows, NY - r0);
-    CA* dst = s.W + (chunk & 1) * rows * L::WP;
+    CA* dst = s.W + (dbuf ? (chunk & 1) : 0) * rows * L::WP;
     const CS* src = plane + static_cast<size_t>(r0) * L::LX;
     for (int i = threadIdx.x; i < nr * L::LX; i += blockDim.x) {
       const int rl = i / L::LX, e = i - rl * L::LX;
@@ -516,8 +529,9 @@ __device__ __forceinline__ void plane_forward_body(const PlanView<S>& p, const S
   const CA* twl = R2C ? s.twm : s.twx;
   for (int chunk = 0; chunk < nchunks; ++chunk) {
     const int r0 = chunk * rows, nr = min(rows, NY - r0);
-    CA* wbase = s.W + (chunk & 1) * rows * L::WP;
-    if (chunk + 1 < nchunks) {
+    CA* wbase = s.W + (dbuf ? (chunk & 1) : 0) * rows * L::WP;
+    if (!dbuf && chunk > 0) issue_chunk(chunk);
+    if (dbuf && chunk + 1 < nchunks) {
       issue_chunk(chunk + 1);
       cp_async_wait<1>();
     } else {
@@ -586,8 +600,21 @@ __device__ __forceinline__ void plane_forward_body(const PlanView<S>& p, const S
   }
   __syncthreads();
   CS* sticks = reinterpret_cast<CS*>(p.sticks) + static_cast<size_t>(z) * p.numSticks;
-  for (int st = threadIdx.x; st < p.numSticks; st += blockDim.x) {
-    sticks[st] = to_storage(s.P[transposed_pos<NY>(p.stickY[st]) * nc + p.stickColumn[st]], k);
+  const int ns = p.numSticks;
+  for (int st0 = threadIdx.x; st0 < ns; st0 += 4 * blockDim.x) {
+    int pos[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int st = st0 + u * blockDim.x;
+      pos[u] = st < ns ? __ldg(p.stickPlanePos + st) : -1;
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      if (pos[u] >= 0) {
+        const int y = dnc.div(pos[u]), c = pos[u] - y * nc;
+        sticks[st0 + u * blockDim.x] = to_storage(s.P[transposed_pos<NY>(y) * nc + c], k);
+      }
+    }
   }
 }
 
@@ -595,7 +622,7 @@ template <typename S, typename A, int NX, int NY, bool R2C>
 __global__ void __launch_bounds__(kPlaneThreads) plane_forward(const PlanView<S> p,
                                                                const S* __restrict__ space, int rows) {
   __shared__ int sExp;
-  plane_forward_body<S, A, NX, NY, R2C>(p, space, rows, blockIdx.x, &sExp);
+  plane_forward_body<S, A, NX, NY, R2C>(p, space, rows, 2 * rows, blockIdx.x, &sExp);
 }
 
 // ================================================================================================
@@ -665,14 +692,26 @@ __device__ __forceinline__ void y_backward_body(const PlanView<S>& p, int cpb, i
   CA* buf = tw + NY;
   const int nc = p.numColumns;
   const int c0 = bx * cpb, ncb = min(cpb, nc - c0);
-  const FastDiv dncb(ncb);
+  const FastDiv dncb(ncb), dnc(nc);
   load_twiddles<S, A>(tw, p.twy, NY);
   for (int i = threadIdx.x; i < NY * ncb; i += blockDim.x) buf[i] = czero<A>();
   __syncthreads();
   const CS* sticks = reinterpret_cast<const CS*>(p.sticks) + static_cast<size_t>(z) * p.numSticks;
   const int sBegin = p.columnStickStart[c0], sEnd = p.columnStickStart[c0 + ncb];
-  for (int st = sBegin + threadIdx.x; st < sEnd; st += blockDim.x) {
-    cp_async_c(buf + p.stickY[st] * ncb + (p.stickColumn[st] - c0), sticks + st);
+  for (int st0 = sBegin + threadIdx.x; st0 < sEnd; st0 += 4 * blockDim.x) {
+    int pos[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int st = st0 + u * blockDim.x;
+      pos[u] = st < sEnd ? __ldg(p.stickPlanePos + st) : -1;
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      if (pos[u] >= 0) {
+        const int y = dnc.div(pos[u]), c = pos[u] - y * nc;
+        cp_async_c(buf + y * ncb + (c - c0), sticks + st0 + u * blockDim.x);
+      }
+    }
   }
   cp_async_commit();
   cp_async_wait<0>();
@@ -712,7 +751,7 @@ __device__ __forceinline__ void y_forward_body(const PlanView<S>& p, int cpb, in
   CA* buf = tw + NY;
   const int nc = p.numColumns;
   const int c0 = bx * cpb, ncb = min(cpb, nc - c0);
-  const FastDiv dncb(ncb);
+  const FastDiv dncb(ncb), dnc(nc);
   load_twiddles<S, A>(tw, p.twy, NY);
   const CS* planes = reinterpret_cast<const CS*>(p.planes) + static_cast<size_t>(z) * NY * nc + c0;
   for (int i = threadIdx.x; i < NY * ncb; i += blockDim.x) {
@@ -738,8 +777,20 @@ __device__ __forceinline__ void y_forward_body(const PlanView<S>& p, int cpb, in
   __syncthreads();
   CS* sticks = reinterpret_cast<CS*>(p.sticks) + static_cast<size_t>(z) * p.numSticks;
   const int sBegin = p.columnStickStart[c0], sEnd = p.columnStickStart[c0 + ncb];
-  for (int st = sBegin + threadIdx.x; st < sEnd; st += blockDim.x) {
-    sticks[st] = to_storage(buf[transposed_pos<NY>(p.stickY[st]) * ncb + (p.stickColumn[st] - c0)], k);
+  for (int st0 = sBegin + threadIdx.x; st0 < sEnd; st0 += 4 * blockDim.x) {
+    int pos[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int st = st0 + u * blockDim.x;
+      pos[u] = st < sEnd ? __ldg(p.stickPlanePos + st) : -1;
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      if (pos[u] >= 0) {
+        const int y = dnc.div(pos[u]), c = pos[u] - y * nc;
+        sticks[st0 + u * blockDim.x] = to_storage(buf[transposed_pos<NY>(y) * ncb + (c - c0)], k);
+      }
+    }
   }
 }
 

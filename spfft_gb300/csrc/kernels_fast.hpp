@@ -41,6 +41,7 @@ template <typename T>
 struct FastArgs {
   const PlanView<T>* plan = nullptr;
   int param = 0;  // sticks per block (z) or rows per chunk (plane)
+  int param2 = 0;  // batched plane forward: rows of the chunk buffer (2 * param double-buffers)
   const T* in = nullptr;
   T* out = nullptr;
   T scale = T(0);
