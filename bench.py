@@ -359,6 +359,8 @@ def measure_gpu(args, rank: int, world: int) -> dict:
            "h2d_bytes_per_step": int(hv.numel() * hv.element_size() + hspace.numel() * hspace.element_size()),
            "d2h_bytes_per_step": int(hspace.numel() * hspace.element_size() + hout.numel() * hout.element_size()),
            "host_access": os.environ.get("SPFFT_GB300_HOST_ACCESS", "direct"),
+           "host_path": "forward input: plane-chunk copies overlapped with the x pass; backward output: "
+                        "written by the x pass over the host link (copy mode: chunk copies both ways)",
            "buffers": "pinned host (torch pin_memory), synchronous calls"}
     # the same pair with the reference's staged copies, for comparison
     if os.environ.get("SPFFT_GB300_HOST_ACCESS", "direct") != "copy":

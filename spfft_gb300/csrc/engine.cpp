@@ -415,6 +415,94 @@ void GpuPlan<T>::forward(const T* space, T* values, bool scaled, void* scratch,
   mark(events, 3, stream);
 }
 
+template <typename T>
+bool GpuPlan<T>::forward_staged(const T* hostSpace, T* devSpace, T* values, bool scaled, void* scratch,
+                                cudaStream_t stream, cudaStream_t copyStream, cudaEvent_t* events) const {
+  bool aligned = true;
+  check_alignment(values, devSpace, &aligned);
+  if (planePath_ != PlanePath::Split || !aligned) return false;
+  const PlanView<T> v = view(scratch);
+  const size_t plane = static_cast<size_t>(base_.dimX) * base_.dimY * (base_.r2c ? 1 : 2);
+  const int nz = base_.dimZ, per = (nz + kStagedChunks - 1) / kStagedChunks;
+  // the copies overwrite devSpace: start them after the work already on `stream`
+  check_cuda(cudaEventRecord(events[kStagedChunks], stream));
+  check_cuda(cudaStreamWaitEvent(copyStream, events[kStagedChunks], 0));
+  FastArgs<T> a;
+  a.plan = &v;
+  a.stream = stream;
+  a.param = splitRpb_;
+  a.in = devSpace;
+  for (int c = 0, z0 = 0; z0 < nz; ++c, z0 += per) {
+    const int cnt = std::min(per, nz - z0);
+    check_cuda(cudaMemcpyAsync(devSpace + z0 * plane, hostSpace + z0 * plane, cnt * plane * sizeof(T),
+                               cudaMemcpyHostToDevice, copyStream));
+    check_cuda(cudaEventRecord(events[c], copyStream));
+    check_cuda(cudaStreamWaitEvent(stream, events[c], 0));
+    a.zBegin = z0;
+    a.zCount = cnt;
+    fast_dispatch<T>(FastOp::XForward, base_.dimX, base_.r2c != 0, a);
+    check_launch(cudaGetLastError());
+  }
+  a.zBegin = 0;
+  a.zCount = -1;
+  a.param = splitCpb_;
+  fast_dispatch<T>(FastOp::YForward, base_.dimY, base_.r2c != 0, a);
+  check_launch(cudaGetLastError());
+  const T scale = scaled ? scale_ : T(0);
+  if (fastZ_) {
+    a.param = fastSpb_;
+    a.out = values;
+    a.scale = scale;
+    fast_dispatch<T>(FastOp::ZForward, base_.dimZ, base_.r2c != 0, a);
+    check_launch(cudaGetLastError());
+  } else {
+    check_launch(launch_generic<T>(GenericPass::ZForward, v, config_, nullptr, values, scale, stream));
+  }
+  return true;
+}
+
+template <typename T>
+bool GpuPlan<T>::backward_staged(const T* values, T* devSpace, T* hostSpace, void* scratch, cudaStream_t stream,
+                                 cudaStream_t copyStream, cudaEvent_t* events) const {
+  bool aligned = true;
+  check_alignment(values, devSpace, &aligned);
+  if (planePath_ != PlanePath::Split || !aligned) return false;
+  const PlanView<T> v = view(scratch);
+  FastArgs<T> a;
+  a.plan = &v;
+  a.stream = stream;
+  if (fastZ_) {
+    a.param = fastSpb_;
+    a.in = values;
+    fast_dispatch<T>(FastOp::ZBackward, base_.dimZ, base_.r2c != 0, a);
+  } else {
+    check_launch(launch_generic<T>(GenericPass::ZBackward, v, config_, values, nullptr, T(0), stream));
+  }
+  check_launch(cudaGetLastError());
+  a.param = splitCpb_;
+  fast_dispatch<T>(FastOp::YBackward, base_.dimY, base_.r2c != 0, a);
+  check_launch(cudaGetLastError());
+  const size_t plane = static_cast<size_t>(base_.dimX) * base_.dimY * (base_.r2c ? 1 : 2);
+  const int nz = base_.dimZ, per = (nz + kStagedChunks - 1) / kStagedChunks;
+  a.param = splitRpb_;
+  a.out = devSpace;
+  for (int c = 0, z0 = 0; z0 < nz; ++c, z0 += per) {
+    const int cnt = std::min(per, nz - z0);
+    a.zBegin = z0;
+    a.zCount = cnt;
+    fast_dispatch<T>(FastOp::XBackward, base_.dimX, base_.r2c != 0, a);
+    check_launch(cudaGetLastError());
+    check_cuda(cudaEventRecord(events[c], stream));
+    check_cuda(cudaStreamWaitEvent(copyStream, events[c], 0));
+    check_cuda(cudaMemcpyAsync(hostSpace + z0 * plane, devSpace + z0 * plane, cnt * plane * sizeof(T),
+                               cudaMemcpyDeviceToHost, copyStream));
+  }
+  // `stream` continues once every chunk is back in host memory
+  check_cuda(cudaEventRecord(events[kStagedChunks], copyStream));
+  check_cuda(cudaStreamWaitEvent(stream, events[kStagedChunks], 0));
+  return true;
+}
+
 size_t smem_optin(int device) { return static_cast<size_t>(max_smem_optin(device)); }
 template <typename T>
 bool fast_prepare(int device, int n) {

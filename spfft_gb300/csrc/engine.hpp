@@ -34,6 +34,18 @@ public:
   void forward(const T* space, T* values, bool scaled, void* scratch, cudaStream_t stream,
                const StageEvents* events = nullptr) const;
 
+  // Transforms whose space domain lives in host memory, staged through the device buffer
+  // `devSpace` in plane chunks so that the host link and the x pass overlap: the forward copies
+  // chunk c on `copyStream` while the x pass of chunk c - 1 runs on `stream`; the backward copies
+  // chunk c back while the x pass of chunk c + 1 runs. `events` holds kStagedEvents events. Both
+  // return false, doing nothing, when the plan has no split x pass (the caller then copies the
+  // whole domain at once).
+  static constexpr int kStagedChunks = 8, kStagedEvents = kStagedChunks + 1;
+  bool forward_staged(const T* hostSpace, T* devSpace, T* values, bool scaled, void* scratch,
+                      cudaStream_t stream, cudaStream_t copyStream, cudaEvent_t* events) const;
+  bool backward_staged(const T* values, T* devSpace, T* hostSpace, void* scratch, cudaStream_t stream,
+                       cudaStream_t copyStream, cudaEvent_t* events) const;
+
   // Adjoints (with respect to the real inner product Re <a, b>): of backward (space gradient ->
   // value gradient) and of forward (value gradient -> space gradient).
   void adjoint_backward(const T* gradSpace, T* gradValues, void* scratch, cudaStream_t stream) const;

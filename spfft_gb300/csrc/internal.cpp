@@ -152,12 +152,25 @@ T* TransformInternal<T>::space_domain_data(SpfftProcessingUnitType location) {
 }
 
 template <typename T>
+gb300::Stream& TransformInternal<T>::copy_stream() {
+  if (!copyStream_) copyStream_.reset(new gb300::Stream());
+  return *copyStream_;
+}
+
+template <typename T>
+cudaEvent_t* TransformInternal<T>::staged_events() {
+  if (!stagedEvents_) stagedEvents_.reset(new gb300::EventSet(gb300::GpuPlan<T>::kStagedEvents));
+  return stagedEvents_->data();
+}
+
+template <typename T>
 void TransformInternal<T>::backward_enqueue(const T* input, T* output) {
   cudaStream_t s = begin();
   auto in = gb300::split_pointer(input);
   auto out = gb300::split_pointer(output);
   if (directHost_) {
-    // pinned host buffers: let the kernels read / write them over the coherent host link
+    // pinned host buffers: let the kernels read / write them over the coherent host link (the x
+    // pass writes the space domain at about the link's rate)
     if (in.first) {
       if (const T* d = gb300::mapped_host_alias(in.first)) in = {nullptr, d};
     }
@@ -176,6 +189,11 @@ void TransformInternal<T>::backward_enqueue(const T* input, T* output) {
     values = staging;
   }
   T* space = out.second ? out.second : grid_->space_device();
+  // host output: copies of plane chunks overlap the x pass of the next chunks
+  if (out.first &&
+      gpu_->backward_staged(values, space, out.first, scratch, s, copy_stream().get(), staged_events())) {
+    return;
+  }
   gpu_->backward(values, space, scratch, s);
   if (out.first) {
     check_cuda(cudaMemcpyAsync(out.first, space, sizeof(T) * space_elements(),
@@ -188,22 +206,30 @@ void TransformInternal<T>::forward_enqueue(const T* input, T* output, SpfftScali
   cudaStream_t s = begin();
   auto in = gb300::split_pointer(input);
   auto out = gb300::split_pointer(output);
-  if (directHost_) {
-    if (in.first) {
-      if (const T* d = gb300::mapped_host_alias(in.first)) in = {nullptr, d};
-    }
-    if (out.first) {
-      if (T* d = gb300::mapped_host_alias(out.first)) out = {nullptr, d};
-    }
+  if (directHost_ && out.first) {
+    if (T* d = gb300::mapped_host_alias(out.first)) out = {nullptr, d};
   }
   void* scratch = grid_->scratch();
+  T* values = out.second ? out.second : gpu_->staging(scratch);
+  // Host input: copy plane chunks to the device buffer, each chunk's x pass starting when it has
+  // arrived (faster than kernels reading host memory, whose reads stall the x pass).
+  if (in.first && gpu_->forward_staged(in.first, grid_->space_device(), values, scaling == SPFFT_FULL_SCALING,
+                                       scratch, s, copy_stream().get(), staged_events())) {
+    if (out.first && plan_->numValues > 0) {
+      check_cuda(cudaMemcpyAsync(out.first, values, sizeof(T) * 2 * plan_->numValues,
+                                 cudaMemcpyDeviceToHost, s));
+    }
+    return;
+  }
+  if (directHost_ && in.first) {
+    if (const T* d = gb300::mapped_host_alias(in.first)) in = {nullptr, d};
+  }
   const T* space = in.second;
   if (in.first) {
     check_cuda(cudaMemcpyAsync(grid_->space_device(), in.first, sizeof(T) * space_elements(),
                                cudaMemcpyHostToDevice, s));
     space = grid_->space_device();
   }
-  T* values = out.second ? out.second : gpu_->staging(scratch);
   gpu_->forward(space, values, scaling == SPFFT_FULL_SCALING, scratch, s);
   if (out.first && plan_->numValues > 0) {
     check_cuda(cudaMemcpyAsync(out.first, values, sizeof(T) * 2 * plan_->numValues,

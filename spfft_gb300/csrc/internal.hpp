@@ -142,6 +142,11 @@ private:
   cudaStream_t userStream_ = nullptr;
   bool hasUserStream_ = false;
   bool directHost_ = true;  // kernels access pinned host buffers directly (else: staged copies)
+  // second stream and events of the chunked host <-> device copies (created on first use)
+  gb300::Stream& copy_stream();
+  cudaEvent_t* staged_events();
+  std::unique_ptr<gb300::Stream> copyStream_;
+  std::unique_ptr<gb300::EventSet> stagedEvents_;
 };
 
 extern template class GridInternal<double>;

@@ -901,11 +901,12 @@ __device__ __forceinline__ void x_backward_body(const PlanView<S>& p, S* __restr
   }
 }
 
+// Planes z0 + blockIdx.y (z0 > 0 when a plane range is transformed on its own).
 template <typename S, typename A, int NX, bool R2C>
 __global__ void __launch_bounds__(kThreads) x_backward_split(const PlanView<S> p, S* __restrict__ space,
-                                                             int rpb) {
+                                                             int rpb, int z0) {
   __shared__ int sExp;
-  x_backward_body<S, A, NX, R2C>(p, space, rpb, blockIdx.x, blockIdx.y, &sExp);
+  x_backward_body<S, A, NX, R2C>(p, space, rpb, blockIdx.x, z0 + blockIdx.y, &sExp);
 }
 
 // x forward: block (row group, z); space rows -> x-FFT -> compact rows to HBM
@@ -989,9 +990,9 @@ __device__ __forceinline__ void x_forward_body(const PlanView<S>& p, const S* __
 
 template <typename S, typename A, int NX, bool R2C>
 __global__ void __launch_bounds__(kThreads) x_forward_split(const PlanView<S> p, const S* __restrict__ space,
-                                                            int rpb) {
+                                                            int rpb, int z0) {
   __shared__ int sExp;
-  x_forward_body<S, A, NX, R2C>(p, space, rpb, blockIdx.x, blockIdx.y, &sExp);
+  x_forward_body<S, A, NX, R2C>(p, space, rpb, blockIdx.x, z0 + blockIdx.y, &sExp);
 }
 
 template <typename S, typename A, int NY>
@@ -1024,13 +1025,14 @@ struct XSplitKernels {
     cudaError_t e2 = allow_dynamic_smem(x_forward_split<S, A, NX, R2C>, maxSmem);
     return e1 != cudaSuccess ? e1 : e2;
   }
-  static void backward(const PlanView<S>& p, int rpb, S* space, cudaStream_t st) {
-    const dim3 g((p.dimY + rpb - 1) / rpb, p.dimZ);
-    x_backward_split<S, A, NX, R2C><<<g, kThreads, smem(p.numColumns, rpb), st>>>(p, space, rpb);
+  // planes [z0, z0 + nz) (nz < 0: all planes from z0)
+  static void backward(const PlanView<S>& p, int rpb, S* space, cudaStream_t st, int z0, int nz) {
+    const dim3 g((p.dimY + rpb - 1) / rpb, nz < 0 ? p.dimZ - z0 : nz);
+    x_backward_split<S, A, NX, R2C><<<g, kThreads, smem(p.numColumns, rpb), st>>>(p, space, rpb, z0);
   }
-  static void forward(const PlanView<S>& p, int rpb, const S* space, cudaStream_t st) {
-    const dim3 g((p.dimY + rpb - 1) / rpb, p.dimZ);
-    x_forward_split<S, A, NX, R2C><<<g, kThreads, smem(p.numColumns, rpb), st>>>(p, space, rpb);
+  static void forward(const PlanView<S>& p, int rpb, const S* space, cudaStream_t st, int z0, int nz) {
+    const dim3 g((p.dimY + rpb - 1) / rpb, nz < 0 ? p.dimZ - z0 : nz);
+    x_forward_split<S, A, NX, R2C><<<g, kThreads, smem(p.numColumns, rpb), st>>>(p, space, rpb, z0);
   }
 };
 

@@ -154,6 +154,35 @@ private:
   cudaEvent_t e_ = nullptr;
 };
 
+// A fixed set of events without timing, for fork / join patterns.
+class EventSet {
+public:
+  explicit EventSet(int n) : n_(n), e_(new cudaEvent_t[n]()) {
+    for (int i = 0; i < n; ++i) {
+      if (cudaEventCreateWithFlags(&e_[i], cudaEventDisableTiming) != cudaSuccess) {
+        destroy();
+        throw GPUError();
+      }
+    }
+  }
+  ~EventSet() { destroy(); }
+  EventSet(const EventSet&) = delete;
+  EventSet& operator=(const EventSet&) = delete;
+  cudaEvent_t* data() { return e_; }
+
+private:
+  void destroy() {
+    if (!e_) return;
+    for (int i = 0; i < n_; ++i) {
+      if (e_[i]) (void)cudaEventDestroy(e_[i]);
+    }
+    delete[] e_;
+    e_ = nullptr;
+  }
+  int n_;
+  cudaEvent_t* e_;
+};
+
 // Host or device? Mirrors translate_gpu_pointer (src/gpu_util/gpu_pointer_translation.hpp:41-71):
 // only memory of type cudaMemoryTypeDevice counts as device memory; managed and registered host
 // memory take the host path.
