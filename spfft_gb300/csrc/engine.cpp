@@ -170,12 +170,14 @@ GpuPlan<T>::GpuPlan(const IndexPlan& p, int device) {
       size_t sm = 0;
       a.smemOut = &sm;
       // Largest group of sticks per block (<= 32) that still gives one block per SM.
+      int numSms = 0;
+      check_cuda(cudaDeviceGetAttribute(&numSms, cudaDevAttrMultiProcessorCount, device));
       int spb = 32;
       for (; spb > 4; spb /= 2) {
         a.param = spb;
         fast_dispatch<T>(FastOp::ZSmem, nz, false, a);
         const int blocks = (ns + spb - 1) / spb;
-        if (sm <= kFastZBudget && blocks >= 152) break;
+        if (sm <= kFastZBudget && blocks >= numSms) break;
       }
       a.param = spb;
       fast_dispatch<T>(FastOp::ZSmem, nz, false, a);

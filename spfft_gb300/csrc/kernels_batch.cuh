@@ -36,7 +36,7 @@ __global__ void __launch_bounds__(kThreads) z_forward_batch(const BatchView<S> b
 }
 
 template <typename S, typename A, int NY>
-__global__ void __launch_bounds__(kThreads) y_backward_batch(const BatchView<S> bv, int cpb) {
+__global__ void __launch_bounds__(kThreads, YMinBlocks<A>::value) y_backward_batch(const BatchView<S> bv, int cpb) {
   __shared__ int sExp;
   const int t = find_transform(bv.starts, bv.count, blockIdx.x);
   const PlanView<S>& p = bv.views[t];
@@ -46,7 +46,7 @@ __global__ void __launch_bounds__(kThreads) y_backward_batch(const BatchView<S> 
 }
 
 template <typename S, typename A, int NY>
-__global__ void __launch_bounds__(kThreads) y_forward_batch(const BatchView<S> bv, int cpb) {
+__global__ void __launch_bounds__(kThreads, YMinBlocks<A>::value) y_forward_batch(const BatchView<S> bv, int cpb) {
   __shared__ int sExp;
   const int t = find_transform(bv.starts, bv.count, blockIdx.x);
   const PlanView<S>& p = bv.views[t];

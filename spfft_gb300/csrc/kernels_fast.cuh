@@ -36,6 +36,19 @@ namespace fast {
 constexpr int kThreads = 256;       // z-pass blocks
 constexpr int kPlaneThreads = 512;  // plane blocks (one plane per block, so more warps per SM)
 constexpr int kBatchPlaneThreads = 256;  // batched plane blocks (two blocks per SM)
+// Minimum resident blocks per SM asked of the compiler for the split y kernels: double-float
+// kernels are capped at 80 registers so that three 256-thread blocks share an SM (24 warps to
+// hide the FP32 pipe latencies of the dd dependency chains; measured 10% faster than two blocks
+// at 128 registers on the 192^3 R2C transform, while the z kernels measured slower that way);
+// FP32 kernels fit three anyway.
+template <typename A>
+struct YMinBlocks {
+  static constexpr int value = 1;
+};
+template <>
+struct YMinBlocks<dd> {
+  static constexpr int value = 3;
+};
 
 extern __shared__ __align__(16) unsigned char g_fast_smem[];
 
@@ -326,10 +339,18 @@ struct PlaneLayout {
   static size_t bytes(int numColumns, int rows) {
     const size_t c = sizeof(CA);
     size_t b = (NY + NX + (R2C ? M : 0)) * c;
-    b += ((NXF * sizeof(int) + c - 1) / c) * c;
+    b += col_table_bytes();
     b += static_cast<size_t>(NY) * numColumns * c;
     b += 2 * static_cast<size_t>(rows) * WP * c;
     return b;
+  }
+  // colOf[NXF] (int, padded to 16 bytes) then colInfo[NXF] (int4)
+  __host__ __device__ static constexpr size_t col_table_bytes() {
+    return (NXF * sizeof(int) + 15) / 16 * 16 + NXF * 16;
+  }
+  // R2C forward: W slots of Z[k] and Z[M-k] for the output column with x = k, and k itself
+  __host__ __device__ static int4 col_info(int kk) {
+    return make_int4(wpos(transposed_pos<LX>(kk % M)), wpos(transposed_pos<LX>((M - kk) % M)), kk, 0);
   }
 };
 
@@ -340,16 +361,16 @@ struct PlaneSmem {
   CA* twx;
   CA* twm;
   int* colOf;
+  int4* colInfo;
   CA* P;
   CA* W;
   __device__ __forceinline__ explicit PlaneSmem(int numColumns) {
-    const size_t c = sizeof(CA);
     twy = reinterpret_cast<CA*>(g_fast_smem);
     twx = twy + NY;
     twm = twx + NX;
     colOf = reinterpret_cast<int*>(twm + (R2C ? L::M : 0));
-    P = reinterpret_cast<CA*>(reinterpret_cast<unsigned char*>(colOf) +
-                              ((L::NXF * sizeof(int) + c - 1) / c) * c);
+    colInfo = reinterpret_cast<int4*>(reinterpret_cast<unsigned char*>(colOf) + (L::NXF * sizeof(int) + 15) / 16 * 16);
+    P = reinterpret_cast<CA*>(reinterpret_cast<unsigned char*>(colOf) + L::col_table_bytes());
     W = P + NY * numColumns;
   }
 };
@@ -367,7 +388,11 @@ __device__ __forceinline__ void plane_load_tables(const PlanView<S>& p,
   }
   for (int i = threadIdx.x; i < L::NXF; i += blockDim.x) s.colOf[i] = -1;
   __syncthreads();
-  for (int c = threadIdx.x; c < p.numColumns; c += blockDim.x) s.colOf[p.columnX[c]] = c;
+  for (int c = threadIdx.x; c < p.numColumns; c += blockDim.x) {
+    const int kk = p.columnX[c];
+    s.colOf[kk] = c;
+    if (R2C) s.colInfo[c] = L::col_info(kk);
+  }
 }
 
 template <typename S, typename A, int NX, int NY, bool R2C>
@@ -574,12 +599,12 @@ __device__ __forceinline__ void plane_forward_body(const PlanView<S>& p, const S
       // X[k] = (Z[k] + conj Z[M-k]) / 2 - i/2 e^{-2 pi i k/N} (Z[k] - conj Z[M-k]), Z[M] = Z[0]
       for (int i = threadIdx.x; i < nr * nc; i += blockDim.x) {
         const int rl = dnc.div(i), c = i - rl * nc;
-        const int kk = p.columnX[c];
+        const int4 ci = s.colInfo[c];
         const CA* wrow = wbase + rl * L::WP;
-        const CA zk = wrow[L::wpos(transposed_pos<L::LX>(kk % L::M))];
-        const CA zm = wrow[L::wpos(transposed_pos<L::LX>((L::M - kk) % L::M))];
+        const CA zk = wrow[ci.x];
+        const CA zm = wrow[ci.y];
         const CA dif = make_c(zk.x - zm.x, zk.y + zm.y);
-        const CA u = cmul(dif, s.twx[kk]);
+        const CA u = cmul(dif, s.twx[ci.z]);
         s.P[(r0 + rl) * nc + c] = make_c(half_of(zk.x + zm.x + u.y), half_of(zk.y - zm.y - u.x));
       }
       __syncthreads();
@@ -734,7 +759,7 @@ __device__ __forceinline__ void y_backward_body(const PlanView<S>& p, int cpb, i
 }
 
 template <typename S, typename A, int NY>
-__global__ void __launch_bounds__(kThreads) y_backward_split(const PlanView<S> p, int cpb) {
+__global__ void __launch_bounds__(kThreads, YMinBlocks<A>::value) y_backward_split(const PlanView<S> p, int cpb) {
   __shared__ int sExp;
   y_backward_body<S, A, NY>(p, cpb, blockIdx.x, blockIdx.y, &sExp);
 }
@@ -795,7 +820,7 @@ __device__ __forceinline__ void y_forward_body(const PlanView<S>& p, int cpb, in
 }
 
 template <typename S, typename A, int NY>
-__global__ void __launch_bounds__(kThreads) y_forward_split(const PlanView<S> p, int cpb) {
+__global__ void __launch_bounds__(kThreads, YMinBlocks<A>::value) y_forward_split(const PlanView<S> p, int cpb) {
   __shared__ int sExp;
   y_forward_body<S, A, NY>(p, cpb, blockIdx.x, blockIdx.y, &sExp);
 }
@@ -808,21 +833,22 @@ struct RowSmem {
   CA* twx;
   CA* twm;
   int* colOf;
+  int4* colInfo;
   CA* P;
   CA* W;
   __device__ __forceinline__ RowSmem(int numColumns, int rows) {
-    const size_t c = sizeof(CA);
     twx = reinterpret_cast<CA*>(g_fast_smem);
     twm = twx + NX;
     colOf = reinterpret_cast<int*>(twm + (R2C ? L::M : 0));
-    P = reinterpret_cast<CA*>(reinterpret_cast<unsigned char*>(colOf) + ((L::NXF * sizeof(int) + c - 1) / c) * c);
+    colInfo = reinterpret_cast<int4*>(reinterpret_cast<unsigned char*>(colOf) + (L::NXF * sizeof(int) + 15) / 16 * 16);
+    P = reinterpret_cast<CA*>(reinterpret_cast<unsigned char*>(colOf) + L::col_table_bytes());
     W = P + rows * numColumns;
   }
   template <typename CAT>
   static size_t bytes(int numColumns, int rows) {
     const size_t c = sizeof(CAT);
-    return (NX + (R2C ? L::M : 0)) * c + ((L::NXF * sizeof(int) + c - 1) / c) * c +
-           static_cast<size_t>(rows) * numColumns * c + static_cast<size_t>(rows) * L::WP * c;
+    return (NX + (R2C ? L::M : 0)) * c + L::col_table_bytes() + static_cast<size_t>(rows) * numColumns * c +
+           static_cast<size_t>(rows) * L::WP * c;
   }
 };
 
@@ -837,7 +863,11 @@ __device__ __forceinline__ void row_load_tables(const PlanView<S>& p, RowSmem<ty
   }
   for (int i = threadIdx.x; i < L::NXF; i += blockDim.x) s.colOf[i] = -1;
   __syncthreads();
-  for (int c = threadIdx.x; c < p.numColumns; c += blockDim.x) s.colOf[p.columnX[c]] = c;
+  for (int c = threadIdx.x; c < p.numColumns; c += blockDim.x) {
+    const int kk = p.columnX[c];
+    s.colOf[kk] = c;
+    if (R2C) s.colInfo[c] = L::col_info(kk);
+  }
 }
 
 // x backward: block (row group, z); compact rows from HBM -> x-FFT -> space rows
@@ -974,12 +1004,12 @@ __device__ __forceinline__ void x_forward_body(const PlanView<S>& p, const S* __
   if (R2C) {
     for (int i = threadIdx.x; i < nr * nc; i += blockDim.x) {
       const int rl = dnc.div(i), c = i - rl * nc;
-      const int kk = p.columnX[c];
+      const int4 ci = s.colInfo[c];
       const CA* wrow = s.W + rl * L::WP;
-      const CA zk = wrow[L::wpos(transposed_pos<L::LX>(kk % L::M))];
-      const CA zm = wrow[L::wpos(transposed_pos<L::LX>((L::M - kk) % L::M))];
+      const CA zk = wrow[ci.x];
+      const CA zm = wrow[ci.y];
       const CA dif = make_c(zk.x - zm.x, zk.y + zm.y);
-      const CA u = cmul(dif, s.twx[kk]);
+      const CA u = cmul(dif, s.twx[ci.z]);
       s.P[rl * nc + c] = make_c(half_of(zk.x + zm.x + u.y), half_of(zk.y - zm.y - u.x));
     }
     __syncthreads();
