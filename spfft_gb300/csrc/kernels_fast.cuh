@@ -36,11 +36,11 @@ namespace fast {
 constexpr int kThreads = 256;       // z-pass blocks
 constexpr int kPlaneThreads = 512;  // plane blocks (one plane per block, so more warps per SM)
 constexpr int kBatchPlaneThreads = 256;  // batched plane blocks (two blocks per SM)
-// Minimum resident blocks per SM asked of the compiler for the split y kernels: double-float
-// kernels are capped at 80 registers so that three 256-thread blocks share an SM (24 warps to
-// hide the FP32 pipe latencies of the dd dependency chains; measured 10% faster than two blocks
-// at 128 registers on the 192^3 R2C transform, while the z kernels measured slower that way);
-// FP32 kernels fit three anyway.
+// Minimum resident blocks per SM asked of the compiler for the split y kernels and the split x
+// forward kernel: double-float kernels are capped at 80 registers so that three 256-thread
+// blocks share an SM (24 warps to hide the FP32 pipe latencies of the dd dependency chains;
+// measured 10% faster than two blocks at 128 registers on the 192^3 R2C transform, while the z
+// kernels measured slower that way); FP32 kernels fit three anyway.
 template <typename A>
 struct YMinBlocks {
   static constexpr int value = 1;
@@ -836,19 +836,21 @@ struct RowSmem {
   int4* colInfo;
   CA* P;
   CA* W;
-  __device__ __forceinline__ RowSmem(int numColumns, int rows) {
+  // withP = false: no compact-row buffer (the R2C forward stores its output columns straight to
+  // HBM), W starts where P would.
+  __device__ __forceinline__ RowSmem(int numColumns, int rows, bool withP = true) {
     twx = reinterpret_cast<CA*>(g_fast_smem);
     twm = twx + NX;
     colOf = reinterpret_cast<int*>(twm + (R2C ? L::M : 0));
     colInfo = reinterpret_cast<int4*>(reinterpret_cast<unsigned char*>(colOf) + (L::NXF * sizeof(int) + 15) / 16 * 16);
     P = reinterpret_cast<CA*>(reinterpret_cast<unsigned char*>(colOf) + L::col_table_bytes());
-    W = P + rows * numColumns;
+    W = P + (withP ? rows * numColumns : 0);
   }
   template <typename CAT>
-  static size_t bytes(int numColumns, int rows) {
+  static size_t bytes(int numColumns, int rows, bool withP = true) {
     const size_t c = sizeof(CAT);
-    return (NX + (R2C ? L::M : 0)) * c + L::col_table_bytes() + static_cast<size_t>(rows) * numColumns * c +
-           static_cast<size_t>(rows) * L::WP * c;
+    return (NX + (R2C ? L::M : 0)) * c + L::col_table_bytes() +
+           (withP ? static_cast<size_t>(rows) * numColumns * c : 0) + static_cast<size_t>(rows) * L::WP * c;
   }
 };
 
@@ -952,7 +954,8 @@ __device__ __forceinline__ void x_forward_body(const PlanView<S>& p, const S* __
   const int nc = p.numColumns, ny = p.dimY;
   const FastDiv dnc(nc);
   const int y0 = bx * rpb, nr = min(rpb, ny - y0);
-  RowSmem<CA, NX, R2C> s(nc, rpb);
+  RowSmem<CA, NX, R2C> s(nc, rpb, !R2C);
+  if (TT::kScaled && threadIdx.x == 0) sExp = 0;
   row_load_tables<S, A, NX, R2C>(p, s);
   const CS* rows = reinterpret_cast<const CS*>(space + (static_cast<size_t>(z) * ny + y0) * NX * (R2C ? 1 : 2));
   for (int i = threadIdx.x; i < nr * L::LX; i += blockDim.x) {
@@ -960,15 +963,17 @@ __device__ __forceinline__ void x_forward_body(const PlanView<S>& p, const S* __
     cp_async_c(s.W + rl * L::WP + L::wpos(e), rows + i);
   }
   cp_async_commit();
+  cp_async_wait<0>();
   int k = 0;
   if (TT::kScaled) {
-    if (threadIdx.x == 0) sExp = 0;
-    __syncthreads();
+    // block scale from the thread's own copies, now in shared memory
     int e = 0;
-    for (int i = threadIdx.x; i < nr * L::LX; i += blockDim.x) e = max(e, max_exponent(rows[i]));
+    for (int i = threadIdx.x; i < nr * L::LX; i += blockDim.x) {
+      const int rl = i / L::LX, el = i - rl * L::LX;
+      e = max(e, max_exponent(reinterpret_cast<const CS*>(s.W)[rl * L::WP + L::wpos(el)]));
+    }
     atomicMax(&sExp, e);
   }
-  cp_async_wait<0>();
   __syncthreads();
   if (TT::kScaled) k = block_scale(sExp);
   const CA* twl = R2C ? s.twm : s.twx;
@@ -1001,7 +1006,9 @@ __device__ __forceinline__ void x_forward_body(const PlanView<S>& p, const S* __
     }
   }
   __syncthreads();
+  CS* planes = reinterpret_cast<CS*>(p.planes) + (static_cast<size_t>(z) * ny + y0) * nc;
   if (R2C) {
+    // output columns straight to the compact plane rows (consecutive threads, consecutive columns)
     for (int i = threadIdx.x; i < nr * nc; i += blockDim.x) {
       const int rl = dnc.div(i), c = i - rl * nc;
       const int4 ci = s.colInfo[c];
@@ -1010,16 +1017,15 @@ __device__ __forceinline__ void x_forward_body(const PlanView<S>& p, const S* __
       const CA zm = wrow[ci.y];
       const CA dif = make_c(zk.x - zm.x, zk.y + zm.y);
       const CA u = cmul(dif, s.twx[ci.z]);
-      s.P[rl * nc + c] = make_c(half_of(zk.x + zm.x + u.y), half_of(zk.y - zm.y - u.x));
+      planes[i] = to_storage(make_c(half_of(zk.x + zm.x + u.y), half_of(zk.y - zm.y - u.x)), k);
     }
-    __syncthreads();
+  } else {
+    for (int i = threadIdx.x; i < nr * nc; i += blockDim.x) planes[i] = to_storage(s.P[i], k);
   }
-  CS* planes = reinterpret_cast<CS*>(p.planes) + (static_cast<size_t>(z) * ny + y0) * nc;
-  for (int i = threadIdx.x; i < nr * nc; i += blockDim.x) planes[i] = to_storage(s.P[i], k);
 }
 
 template <typename S, typename A, int NX, bool R2C>
-__global__ void __launch_bounds__(kThreads) x_forward_split(const PlanView<S> p, const S* __restrict__ space,
+__global__ void __launch_bounds__(kThreads, YMinBlocks<A>::value) x_forward_split(const PlanView<S> p, const S* __restrict__ space,
                                                             int rpb, int z0) {
   __shared__ int sExp;
   x_forward_body<S, A, NX, R2C>(p, space, rpb, blockIdx.x, z0 + blockIdx.y, &sExp);
@@ -1050,6 +1056,9 @@ struct XSplitKernels {
   static size_t smem(int numColumns, int rpb) {
     return RowSmem<CA, NX, R2C>::template bytes<CA>(numColumns, rpb);
   }
+  static size_t smem_forward(int numColumns, int rpb) {
+    return RowSmem<CA, NX, R2C>::template bytes<CA>(numColumns, rpb, !R2C);
+  }
   static cudaError_t prepare(size_t maxSmem) {
     cudaError_t e1 = allow_dynamic_smem(x_backward_split<S, A, NX, R2C>, maxSmem);
     cudaError_t e2 = allow_dynamic_smem(x_forward_split<S, A, NX, R2C>, maxSmem);
@@ -1062,7 +1071,7 @@ struct XSplitKernels {
   }
   static void forward(const PlanView<S>& p, int rpb, const S* space, cudaStream_t st, int z0, int nz) {
     const dim3 g((p.dimY + rpb - 1) / rpb, nz < 0 ? p.dimZ - z0 : nz);
-    x_forward_split<S, A, NX, R2C><<<g, kThreads, smem(p.numColumns, rpb), st>>>(p, space, rpb, z0);
+    x_forward_split<S, A, NX, R2C><<<g, kThreads, smem_forward(p.numColumns, rpb), st>>>(p, space, rpb, z0);
   }
 };
 
