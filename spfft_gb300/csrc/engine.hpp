@@ -79,7 +79,7 @@ private:
   LaunchConfig config_{};
   bool fastZ_ = false;
   PlanePath planePath_ = PlanePath::Generic;
-  int fastSpb_ = 0, fastRows_ = 0, splitCpb_ = 0, splitRpb_ = 0;
+  int fastSpb_ = 0, fastRows_ = 0, splitCpb_ = 0, splitRpb_ = 0, fusedThreads_ = 512;
   ScratchLayout layout_{};
   T scale_ = T(1);
   int numValues_ = 0;

@@ -647,7 +647,7 @@ template <typename S, typename A, int NX, int NY, bool R2C>
 __global__ void __launch_bounds__(kPlaneThreads) plane_forward(const PlanView<S> p,
                                                                const S* __restrict__ space, int rows) {
   __shared__ int sExp;
-  plane_forward_body<S, A, NX, NY, R2C>(p, space, rows, 2 * rows, blockIdx.x, &sExp);
+  plane_forward_body<S, A, NX, NY, R2C>(p, space, rows, rows, blockIdx.x, &sExp);
 }
 
 // ================================================================================================
@@ -692,11 +692,13 @@ struct PlaneKernels {
     cudaError_t e2 = allow_dynamic_smem(plane_forward<S, A, NX, NY, R2C>, maxSmem);
     return e1 != cudaSuccess ? e1 : e2;
   }
-  static void backward(const PlanView<S>& p, int rows, S* space, cudaStream_t st) {
-    plane_backward<S, A, NX, NY, R2C><<<p.dimZ, kPlaneThreads, smem(p.numColumns, rows), st>>>(p, space, rows);
+  // `half`: the shared memory holds 2 * half rows of x chunk buffer, which both directions use as
+  // one chunk of 2 * half rows (single-buffered, like the batched plane passes).
+  static void backward(const PlanView<S>& p, int half, S* space, cudaStream_t st, int threads) {
+    plane_backward<S, A, NX, NY, R2C><<<p.dimZ, threads, smem(p.numColumns, half), st>>>(p, space, 2 * half);
   }
-  static void forward(const PlanView<S>& p, int rows, const S* space, cudaStream_t st) {
-    plane_forward<S, A, NX, NY, R2C><<<p.dimZ, kPlaneThreads, smem(p.numColumns, rows), st>>>(p, space, rows);
+  static void forward(const PlanView<S>& p, int half, const S* space, cudaStream_t st, int threads) {
+    plane_forward<S, A, NX, NY, R2C><<<p.dimZ, threads, smem(p.numColumns, half), st>>>(p, space, 2 * half);
   }
 };
 
