@@ -335,7 +335,11 @@ def measure_gpu(args, rank: int, world: int) -> dict:
     roofline = {"bound": "hbm", "kernel": dominant, "achieved": round(achieved, 1), "peak": peak,
                 "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_source": peak_src,
                 "traffic": traffic, "algorithmic_bytes": ab["kernels"][dominant],
-                "kernel_ms": {k: round(v, 4) for k, v in kern_ms.items()}}
+                "kernel_ms": {k: round(v, 4) for k, v in kern_ms.items()},
+                "kernel_gbs": {k: round(ab["kernels"][k] / (v * 1e-3) / 1e9, 1) for k, v in kern_ms.items()},
+                "limiter": ("instruction issue: FP64 runs as double-float arithmetic on the FP32 pipes "
+                            "(GB300's FP64 pipe is 57x slower), so the HBM fraction is not reachable"
+                            if dtype == "float64" else "latency of a single small transform")}
     pair_gbs = ab["pair"] * pairs_per_s / world / 1e9
 
     # ---- end to end through the public API with pinned host buffers ----------------------------
@@ -456,6 +460,13 @@ def measure_batched(args, workload: str, batch: int, dtype: str, radii=None) -> 
             acc[nm].append(t)
     pass_ms = {k: statistics.median(v) for k, v in acc.items()}
     pass_gbs = {k: round(pb["passes"][k] / (pass_ms[k] * 1e-3) / 1e9, 1) for k in pass_ms if pb["passes"][k]}
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    dom = max(pass_ms, key=pass_ms.get)
+    batch_roof = {"bound": "hbm", "kernel": dom + "_batch", "achieved": pass_gbs.get(dom), "peak": peak,
+                  "unit": "GB/s", "frac": round(pass_gbs.get(dom, 0.0) / peak, 4),
+                  "peak_source": "measured" if "hbm_gbs" in peaks else "fallback",
+                  "algorithmic_bytes": pb["passes"][dom]}
     for b in range(batch):  # the stage-timed passes changed the values: restore them
         vals[b].copy_(torch.from_numpy(hosts[b]).to(ct))
     bt.pair_graph(sp.SPFFT_FULL_SCALING, stream)
@@ -473,6 +484,7 @@ def measure_batched(args, workload: str, batch: int, dtype: str, radii=None) -> 
             "shape_groups": info["groups"], "roundtrip_rel_l2_max": max(errs),
             "plane_pass": "fused" if bt.transform_path(0) == 2 else "split",
             "pass_ms": {k: round(v, 4) for k, v in pass_ms.items()}, "pass_gbs": pass_gbs,
+            "roofline": batch_roof,
             "hbm_gbs_per_pair_accounting": round(pb["pair"] / (ms / args.steps * 1e-3) / 1e9, 1),
             "workload": workload, "l2": "batch working set > L2 (no flush)"}
 
