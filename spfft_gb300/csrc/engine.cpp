@@ -169,15 +169,28 @@ GpuPlan<T>::GpuPlan(const IndexPlan& p, int device) {
     if (ns > 0 && fast_dispatch<T>(FastOp::Has, nz, false, a) && prepare_fast_once<T>(device, nz)) {
       size_t sm = 0;
       a.smemOut = &sm;
-      // Largest group of sticks per block (<= 32) that still gives one block per SM.
+      // Sticks per block: of 32, 24, 16, 12 and 8, the one with the least modelled time, waves of
+      // resident blocks x (sticks per block + 4 for the fixed cost of a block), ties to the larger
+      // (measured on 192^3 R2C: 12 in double-float, 8 in FP32).
       int numSms = 0;
       check_cuda(cudaDeviceGetAttribute(&numSms, cudaDevAttrMultiProcessorCount, device));
       int spb = 32;
-      for (; spb > 4; spb /= 2) {
-        a.param = spb;
+      long long best = -1;
+      for (int cand : {32, 24, 16, 12, 8}) {
+        a.param = cand;
         fast_dispatch<T>(FastOp::ZSmem, nz, false, a);
-        const int blocks = (ns + spb - 1) / spb;
-        if (sm <= kFastZBudget && blocks >= numSms) break;
+        if (sm > kFastZBudget) continue;
+        size_t perSm = 1;
+        a.smemOut = &perSm;
+        fast_dispatch<T>(FastOp::ZOccupancy, nz, false, a);
+        a.smemOut = &sm;
+        const long long slots = static_cast<long long>(numSms) * static_cast<long long>(perSm);
+        const long long blocks = (ns + cand - 1) / cand;
+        const long long cost = (blocks + slots - 1) / slots * (cand + 4);
+        if (best < 0 || cost < best) {
+          best = cost;
+          spb = cand;
+        }
       }
       a.param = spb;
       fast_dispatch<T>(FastOp::ZSmem, nz, false, a);
@@ -188,7 +201,8 @@ GpuPlan<T>::GpuPlan(const IndexPlan& p, int device) {
     }
     const bool r2c = p.type == SPFFT_TRANS_R2C;
     // Candidate plane strategies. SPFFT_GB300_PLANE=fused|split|generic forces one (when it is
-    // available for this shape); otherwise split is preferred, then fused, then generic.
+    // available for this shape); otherwise fused where two blocks fit an SM and there is a plane
+    // per SM, then split, then fused with one block per SM, then generic.
     bool fusedOk = false, splitOk = false;
     int fusedRows = 0, cpb = 0, rpb = 0;
     if (ns > 0 && p.dimX == p.dimY && fast_dispatch<T>(FastOp::Has, p.dimX, r2c, a) &&

@@ -338,15 +338,18 @@ struct PlaneLayout {
   template <typename CA>
   static size_t bytes(int numColumns, int rows) {
     const size_t c = sizeof(CA);
-    size_t b = (NY + NX + (R2C ? M : 0)) * c;
+    size_t b = round16((NY + NX + (R2C ? M : 0)) * c);
     b += col_table_bytes();
     b += static_cast<size_t>(NY) * numColumns * c;
     b += 2 * static_cast<size_t>(rows) * WP * c;
     return b;
   }
-  // colOf[NXF] (int, padded to 16 bytes) then colInfo[NXF] (int4)
+  // colOf[NXF] (int, padded to 16 bytes) then colInfo[NXF] (int4). The tables start on a 16-byte
+  // boundary (the twiddle tables before them are padded to one), so colInfo and the buffers after
+  // it are 16-byte aligned for every length (20 * N bytes of FP32 twiddles are not, for N = 90).
+  __host__ __device__ static constexpr size_t round16(size_t b) { return (b + 15) / 16 * 16; }
   __host__ __device__ static constexpr size_t col_table_bytes() {
-    return (NXF * sizeof(int) + 15) / 16 * 16 + NXF * 16;
+    return round16(NXF * sizeof(int)) + NXF * 16;
   }
   // R2C forward: W slots of Z[k] and Z[M-k] for the output column with x = k, and k itself
   __host__ __device__ static int4 col_info(int kk) {
@@ -368,8 +371,8 @@ struct PlaneSmem {
     twy = reinterpret_cast<CA*>(g_fast_smem);
     twx = twy + NY;
     twm = twx + NX;
-    colOf = reinterpret_cast<int*>(twm + (R2C ? L::M : 0));
-    colInfo = reinterpret_cast<int4*>(reinterpret_cast<unsigned char*>(colOf) + (L::NXF * sizeof(int) + 15) / 16 * 16);
+    colOf = reinterpret_cast<int*>(g_fast_smem + L::round16((NY + NX + (R2C ? L::M : 0)) * sizeof(CA)));
+    colInfo = reinterpret_cast<int4*>(reinterpret_cast<unsigned char*>(colOf) + L::round16(L::NXF * sizeof(int)));
     P = reinterpret_cast<CA*>(reinterpret_cast<unsigned char*>(colOf) + L::col_table_bytes());
     W = P + NY * numColumns;
   }
@@ -843,15 +846,15 @@ struct RowSmem {
   __device__ __forceinline__ RowSmem(int numColumns, int rows, bool withP = true) {
     twx = reinterpret_cast<CA*>(g_fast_smem);
     twm = twx + NX;
-    colOf = reinterpret_cast<int*>(twm + (R2C ? L::M : 0));
-    colInfo = reinterpret_cast<int4*>(reinterpret_cast<unsigned char*>(colOf) + (L::NXF * sizeof(int) + 15) / 16 * 16);
+    colOf = reinterpret_cast<int*>(g_fast_smem + L::round16((NX + (R2C ? L::M : 0)) * sizeof(CA)));
+    colInfo = reinterpret_cast<int4*>(reinterpret_cast<unsigned char*>(colOf) + L::round16(L::NXF * sizeof(int)));
     P = reinterpret_cast<CA*>(reinterpret_cast<unsigned char*>(colOf) + L::col_table_bytes());
     W = P + (withP ? rows * numColumns : 0);
   }
   template <typename CAT>
   static size_t bytes(int numColumns, int rows, bool withP = true) {
     const size_t c = sizeof(CAT);
-    return (NX + (R2C ? L::M : 0)) * c + L::col_table_bytes() +
+    return L::round16((NX + (R2C ? L::M : 0)) * c) + L::col_table_bytes() +
            (withP ? static_cast<size_t>(rows) * numColumns * c : 0) + static_cast<size_t>(rows) * L::WP * c;
   }
 };

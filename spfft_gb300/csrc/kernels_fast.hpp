@@ -18,6 +18,7 @@ enum class FastOp {
   PlaneForward,
   PlaneSmem,
   ZSmem,
+  ZOccupancy,  // resident z_backward blocks per SM for param sticks per block (into *smemOut)
   YBackward,  // split y pass (n = dimY), param = columns per block
   YForward,
   YSmem,

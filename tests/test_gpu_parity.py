@@ -356,3 +356,37 @@ def test_pinned_host_buffers(lib, access, dtype, monkeypatch):
             buf.view(-1)[: len(idx)] = torch.from_numpy(vals).to(st)
             tr.backward(buf, buf)
             assert rel_l2(buf.numpy(), want) <= TOL[dtype]
+
+
+@pytest.mark.parametrize("dtype", ["float64", "float32"])
+def test_every_specialised_length(lib, dtype):
+    """Every length with size-specialised kernels, C2C and R2C, single transforms and one batch
+    of them: shared-memory tables and buffers of each layout must be aligned for every length
+    (the FP32 R2C twiddle tables of N = 90 and 150 end on an 8-byte boundary)."""
+    rng = np.random.default_rng(41)
+    items = []
+    for n in (12, 48, 60, 64, 72, 90, 96, 100, 108, 120, 128, 150, 160, 192):
+        for ttype in (0, 1):
+            idx = sphere_indices(n, max(2, n // 6), r2c=(ttype == 1))
+            vals = _values(rng, idx.shape[0])
+            if ttype == 1:
+                vals[(idx == 0).all(axis=1)] = vals[(idx == 0).all(axis=1)].real
+            oracle = pipeline.HostPipeline(ttype, n, n, n, idx)
+            tr = _transform(dtype, ttype, (n, n, n), idx)
+            assert tr.path_info()["fast_z"], (n, ttype)
+            v = torch.from_numpy(vals).to(CT[dtype]).cuda()
+            out = torch.empty((n, n, n), dtype=CT[dtype] if ttype == 0 else RT[dtype], device="cuda")
+            tr.backward(v, out)
+            want = oracle.backward(vals)
+            assert rel_l2(out.cpu().numpy(), want) <= TOL[dtype], (n, ttype)
+            f = torch.empty_like(v)
+            tr.forward(out, f)
+            assert rel_l2(f.cpu().numpy(), oracle.forward(want)) <= TOL[dtype], (n, ttype)
+            items.append((tr, v, torch.zeros_like(out), oracle, vals))
+    batch = sp.Batch([it[0] for it in items])
+    batch.bind([it[1] for it in items], [it[2] for it in items])
+    stream = torch.cuda.Stream()
+    batch.backward(stream)
+    stream.synchronize()
+    for tr, v, space, oracle, vals in items:
+        assert rel_l2(space.cpu().numpy(), oracle.backward(vals)) <= TOL[dtype]
