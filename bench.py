@@ -270,6 +270,10 @@ def measure_gpu(args, rank: int, world: int) -> dict:
     space = torch.empty((n, n, n), dtype=rt if r2c else ct, device="cuda")
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")  # > L2 (126 MB)
     stream = torch.cuda.Stream()
+    tuned = None
+    if not args.no_autotune:  # plan-time autotuner (outside every timed region)
+        tr.autotune(3)
+        tuned = tr.tuning()
     tr.set_stream(stream)
     tr.set_execution_mode(sp.SPFFT_EXEC_ASYNCHRONOUS)
 
@@ -397,7 +401,8 @@ def measure_gpu(args, rank: int, world: int) -> dict:
         "pairs_per_s": pairs_per_s, "ms_per_step": total_ms / args.steps, "wall_s": wall,
         "clocks": clocks.summary(), "roofline": roofline, "e2e": e2e,
         "pair_gbs": pair_gbs, "roundtrip_rel_l2": err,
-        "launches_per_step": 6, "npts": npts, "nsticks": nsticks, "ncols": ncols,
+        "launches_per_step": 6 if tr.path_info()["split_plane"] else 4, "npts": npts, "nsticks": nsticks,
+        "ncols": ncols, "tuning": tuned or tr.tuning(),
     }
 
 
@@ -432,6 +437,8 @@ def measure_batched(args, workload: str, batch: int, dtype: str, radii=None) -> 
     bt = sp.Batch(trs)
     bt.bind(vals, spaces)
     stream = torch.cuda.Stream()
+    if not args.no_autotune:
+        bt.autotune(2, stream)
     for _ in range(args.warmup):
         bt.pair_graph(sp.SPFFT_FULL_SCALING, stream)  # scaled pairs keep the values bounded
     torch.cuda.synchronize()
@@ -539,6 +546,10 @@ def measure_batch_workload(args, rank: int, world: int) -> dict:
     trs32, vals32, spaces32, ct32 = make("float32")
     bt = sp.Batch(trs32)
     bt.bind(vals32, spaces32)
+    if not args.no_autotune:
+        bt.autotune(2, stream)
+        for d, h in zip(vals32, hosts):  # the autotuner overwrote the bound buffers
+            d.copy_(torch.from_numpy(h).to(ct32))
     for _ in range(args.warmup):
         bt.pair_graph(sp.SPFFT_FULL_SCALING, stream)
     torch.cuda.synchronize()
@@ -712,6 +723,8 @@ def main() -> int:
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--batch", type=int, default=64, help="transforms in the FP32-batched leg")
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="keep the plan-time default tile shapes instead of running the autotuner")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -764,7 +777,7 @@ def main() -> int:
         "hbm_gbs_per_pair_accounting": round(res["pair_gbs"], 1),
         "e2e": res["e2e"], "clocks": res["clocks"],
         "gpu_launches": res["launches_per_step"] * args.steps,
-        "roundtrip_rel_l2": res["roundtrip_rel_l2"],
+        "roundtrip_rel_l2": res["roundtrip_rel_l2"], "tuning": res["tuning"],
     }
     if res["batched"]:
         line["fp32_batched"] = res["batched"]

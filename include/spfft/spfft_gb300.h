@@ -100,6 +100,24 @@ SPFFT_EXPORT SpfftError spfft_gb300_transform_path_info(SpfftTransform transform
 SPFFT_EXPORT SpfftError spfft_gb300_float_transform_path_info(SpfftFloatTransform transform,
                                                               int* flags);
 
+/* Autotuner (no counterpart in the reference). Times `repetitions` backward + scaled forward pairs
+ * of every valid tile shape and plane strategy of the transform (first the sticks per z block with
+ * the current plane strategy, then the fused plane pass with each chunk size and thread count and
+ * the split passes with each column / row group size) on the transform's own device buffers, and
+ * keeps the fastest; writes its time per pair in milliseconds to msPerPair (may be NULL).
+ * Synchronous; overwrites the grid's internal device space-domain buffer; no other call on the
+ * transform may run meanwhile. The choice lasts for the transform (clones start from the default
+ * choice). */
+SPFFT_EXPORT SpfftError spfft_gb300_transform_autotune(SpfftTransform transform, int repetitions,
+                                                       float* msPerPair);
+SPFFT_EXPORT SpfftError spfft_gb300_float_transform_autotune(SpfftFloatTransform transform,
+                                                             int repetitions, float* msPerPair);
+/* The tile shapes the transform runs with: tuning[0] sticks per z block (0: generic z kernels),
+ * [1] plane strategy (0 generic, 1 fused, 2 split), [2] fused: half the x chunk rows, [3] fused:
+ * threads per block, [4] split: columns per y block, [5] split: rows per x block. */
+SPFFT_EXPORT SpfftError spfft_gb300_transform_tuning(SpfftTransform transform, int* tuning);
+SPFFT_EXPORT SpfftError spfft_gb300_float_transform_tuning(SpfftFloatTransform transform, int* tuning);
+
 /* ---- batched execution (no counterpart in the reference; the GB300 form of its multi-transform)
  * A batch holds many transforms (all double or all float, on distinct grids, same device). Each
  * pass of each group of equally shaped transforms runs as ONE kernel launch over all of them, so
@@ -129,6 +147,13 @@ SPFFT_EXPORT SpfftError spfft_gb300_batch_pair_graph(SpfftGb300Batch batch, Spff
                                                      void* stream);
 SPFFT_EXPORT SpfftError spfft_gb300_batch_info(SpfftGb300Batch batch, int* numGroups,
                                                int* numUnbatched, int* launchesPerPair);
+/* Autotuner of a bound batch: for each group of equally shaped transforms, times `repetitions`
+ * backward + scaled forward pairs of the group alone on `stream` for each plane strategy that fits
+ * (fused, split) and each sticks-per-z-block size, and keeps the fastest. Overwrites the contents of
+ * the bound buffers; drops captured graphs (the next graph call captures anew). Writes the sum of
+ * the groups' best times per pair in milliseconds to msPerPair (may be NULL). Synchronous. */
+SPFFT_EXPORT SpfftError spfft_gb300_batch_autotune(SpfftGb300Batch batch, int repetitions, void* stream,
+                                                   float* msPerPair);
 /* How transform `index` (its position at creation) runs: 0 one by one (no batched kernels for its
  * lengths), 1 batched with split y and x passes, 2 batched with one fused plane pass (y and x per
  * plane with the compact plane on chip; chosen for cubic planes that fit two blocks per SM, or

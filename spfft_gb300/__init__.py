@@ -131,6 +131,8 @@ def _declare(lib: ctypes.CDLL) -> None:
         getattr(lib, prefix + "transform_backward_device").argtypes = [_vp, _vp, _vp, _vp]
         getattr(lib, prefix + "transform_forward_device").argtypes = [_vp, _vp, _vp, _i, _vp]
         getattr(lib, prefix + "transform_path_info").argtypes = [_vp, _ip]
+        getattr(lib, prefix + "transform_autotune").argtypes = [_vp, _i, ctypes.POINTER(ctypes.c_float)]
+        getattr(lib, prefix + "transform_tuning").argtypes = [_vp, _ip]
         getattr(lib, prefix + "transform_adjoint_backward").argtypes = [_vp, _vp, _vp, _vp]
         getattr(lib, prefix + "transform_adjoint_forward").argtypes = [_vp, _vp, _vp, _i, _vp]
         getattr(lib, prefix + "transform_stage_times").argtypes = [_vp, _i, _vp, _vp, _i, _vp,
@@ -145,6 +147,7 @@ def _declare(lib: ctypes.CDLL) -> None:
     lib.spfft_gb300_batch_pair_graph.argtypes = [_vp, _i, _vp]
     lib.spfft_gb300_batch_info.argtypes = [_vp, _ip, _ip, _ip]
     lib.spfft_gb300_batch_transform_path.argtypes = [_vp, _i, _ip]
+    lib.spfft_gb300_batch_autotune.argtypes = [_vp, _i, _vp, ctypes.POINTER(ctypes.c_float)]
     lib.spfft_gb300_multi_batched_calls.argtypes = [ctypes.POINTER(ctypes.c_longlong)]
     lib.spfft_gb300_batch_stage_times.argtypes = [_vp, _i, _i, _vp, ctypes.POINTER(ctypes.c_float)]
     lib.spfft_gb300_transform_backward_noalloc.argtypes = [_vp, _vp, _vp, _vp]
@@ -360,6 +363,22 @@ class Transform:
         return {"fast_z": bool(v.value & 1), "fused_plane": bool(v.value & 2),
                 "split_plane": bool(v.value & 4)}
 
+    def autotune(self, repetitions: int = 5) -> float:
+        """Time every valid tile shape and plane strategy and keep the fastest; returns its time
+        per backward + forward pair in ms (overwrites the grid's internal device space domain)."""
+        ms = ctypes.c_float(0.0)
+        _call("spfft_gb300_" + self._p[len("spfft_"):] + "transform_autotune", self._h, int(repetitions),
+              ctypes.byref(ms))
+        return float(ms.value)
+
+    def tuning(self) -> dict:
+        """The tile shapes the transform runs with."""
+        v = (ctypes.c_int * 6)()
+        _call("spfft_gb300_" + self._p[len("spfft_"):] + "transform_tuning", self._h, v)
+        return {"sticks_per_z_block": v[0], "plane": ("generic", "fused", "split")[v[1]],
+                "fused_half_rows": v[2], "fused_threads": v[3], "columns_per_y_block": v[4],
+                "rows_per_x_block": v[5]}
+
     def set_stream(self, stream: Any) -> None:
         """Run every later call on this CUDA stream (torch.cuda.Stream, cudaStream_t int or None)."""
         ptr = None if stream is None else int(getattr(stream, "cuda_stream", stream))
@@ -494,6 +513,13 @@ class Batch:
         g, u, l = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
         _call("spfft_gb300_batch_info", self._h, ctypes.byref(g), ctypes.byref(u), ctypes.byref(l))
         return {"groups": g.value, "unbatched": u.value, "launches_per_pair": l.value}
+
+    def autotune(self, repetitions: int = 3, stream: Any = None) -> float:
+        """Per shape group, keep the fastest plane strategy and z block size (overwrites the bound
+        buffers; drops captured graphs). Returns the sum of the groups' best ms per pair."""
+        ms = ctypes.c_float(0.0)
+        _call("spfft_gb300_batch_autotune", self._h, int(repetitions), _stream_handle(stream), ctypes.byref(ms))
+        return float(ms.value)
 
     def transform_path(self, index: int) -> int:
         """0 unbatched, 1 batched with split y and x passes, 2 batched with the fused plane pass."""

@@ -240,6 +240,25 @@ SPFFT_GB300_GRID_C_API(spfft_float_grid_, GridFloat)
       *flags = spfft::TransformAccess::get(t).path_flags();                                       \
     });                                                                                           \
   }                                                                                               \
+  SpfftError GPREFIX##autotune(void* transform, int repetitions, float* msPerPair) {              \
+    if (repetitions < 1) return SPFFT_INVALID_PARAMETER_ERROR;                                    \
+    return with_handle<spfft::TRANSFORM>(transform, [&](spfft::TRANSFORM& t) {                    \
+      const float ms = spfft::TransformAccess::get(t).autotune(repetitions);                      \
+      if (msPerPair) *msPerPair = ms;                                                             \
+    });                                                                                           \
+  }                                                                                               \
+  SpfftError GPREFIX##tuning(void* transform, int* tuning) {                                      \
+    if (!tuning) return SPFFT_INVALID_PARAMETER_ERROR;                                            \
+    return with_handle<spfft::TRANSFORM>(transform, [&](spfft::TRANSFORM& t) {                    \
+      const auto tu = spfft::TransformAccess::get(t).gpu_plan().tuning();                         \
+      tuning[0] = tu.spb;                                                                         \
+      tuning[1] = tu.path;                                                                        \
+      tuning[2] = tu.fusedRows;                                                                   \
+      tuning[3] = tu.fusedThreads;                                                                \
+      tuning[4] = tu.cpb;                                                                         \
+      tuning[5] = tu.rpb;                                                                         \
+    });                                                                                           \
+  }                                                                                               \
   SpfftError GPREFIX##forward_device(void* transform, const T* space, T* values,                  \
                                      SpfftScalingType scaling, void* stream) {                    \
     return with_handle<spfft::TRANSFORM>(transform, [&](spfft::TRANSFORM& t) {                    \

@@ -35,6 +35,8 @@ struct BatchPlan<T>::Group {
   // fused plane passes: one block per plane, rows per x chunk (backward uses both halves of the
   // forward's double buffer, so twice the rows)
   bool fused = false;
+  bool fusedAvail = false, splitAvail = false;  // which plane strategies fit (for the autotuner)
+  std::vector<int> zCands;                      // sticks per z block that fit (for the autotuner)
   int rowsF = 0, rowsB = 0, blocksP = 0;
   size_t smemP = 0;
   T scale = T(0);
@@ -149,6 +151,7 @@ BatchPlan<T>::BatchPlan(std::vector<std::shared_ptr<TransformInternal<T>>> trans
           // faster than double-buffered half chunks with two blocks per SM) the forward transform
           // chunks of that many rows
           g.fused = true;
+          g.fusedAvail = true;
           g.rowsB = std::min(2 * rows, g.ny);
           g.rowsF = g.rowsB;
           g.smemP = sm;
@@ -157,6 +160,12 @@ BatchPlan<T>::BatchPlan(std::vector<std::shared_ptr<TransformInternal<T>>> trans
       }
     }
     const bool splitFits = g.smemY <= optin && g.smemX <= optin;
+    g.splitAvail = splitFits;
+    for (int cand : {8, 16, 32}) {
+      a.param = cand;
+      fast_dispatch<T>(FastOp::ZSmem, g.nz, g.r2c, a);
+      if (sm <= optin) g.zCands.push_back(cand);
+    }
     if (g.smemZ > optin || (!g.fused && !splitFits)) {
       for (int t : g.members) fallback_.push_back(t);
       continue;
@@ -453,6 +462,84 @@ void BatchPlan<T>::stage_times(int direction, bool scaled, cudaStream_t stream, 
     throw;
   }
   for (auto& e : ev.ev) (void)cudaEventDestroy(e);
+}
+
+template <typename T>
+void BatchPlan<T>::set_z_shape(Group& g, int spb) {
+  FastArgs<T> a;
+  size_t sm = 0;
+  a.smemOut = &sm;
+  a.param = spb;
+  fast_dispatch<T>(FastOp::ZSmem, g.nz, g.r2c, a);
+  const size_t m = g.members.size();
+  std::vector<int> sz(m + 1, 0);
+  for (size_t i = 0; i < m; ++i) {
+    sz[i + 1] = sz[i] + (tp_[g.members[i]]->index_plan().num_sticks() + spb - 1) / spb;
+  }
+  check_cuda(cudaMemcpy(static_cast<char*>(g.dev.get()) + g.offStartsZ, sz.data(), (m + 1) * sizeof(int),
+                        cudaMemcpyHostToDevice));
+  g.spb = spb;
+  g.smemZ = sm;
+  g.blocksZ = sz[m];
+}
+
+template <typename T>
+float BatchPlan<T>::autotune(cudaStream_t stream, int reps) {
+  check_bound();
+  if (reps < 1) throw InvalidParameterError();
+  DeviceGuard guard(device_);
+  upload_views();
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  check_cuda(cudaEventCreate(&e0));
+  check_cuda(cudaEventCreate(&e1));
+  float total = 0.0f;
+  try {
+    for (auto& gp : groups_) {
+      Group& g = *gp;
+      auto time_group = [&]() {
+        run_group(g, 3, true, stream);  // warm-up
+        check_cuda(cudaEventRecord(e0, stream));
+        for (int r = 0; r < reps; ++r) run_group(g, 3, true, stream);
+        check_cuda(cudaEventRecord(e1, stream));
+        check_cuda(cudaEventSynchronize(e1));
+        float ms = 0.0f;
+        check_cuda(cudaEventElapsedTime(&ms, e0, e1));
+        return ms / reps;
+      };
+      int bestSpb = g.spb;
+      bool bestFused = g.fused;
+      float best = time_group();
+      for (int f = 0; f < 2; ++f) {
+        const bool fused = f == 1;
+        if ((fused && !g.fusedAvail) || (!fused && !g.splitAvail)) continue;
+        g.fused = fused;
+        for (int spb : g.zCands) {
+          set_z_shape(g, spb);
+          const float ms = time_group();
+          if (ms < best) {
+            best = ms;
+            bestSpb = spb;
+            bestFused = fused;
+          }
+        }
+      }
+      g.fused = bestFused;
+      set_z_shape(g, bestSpb);
+      total += best;
+    }
+  } catch (...) {
+    (void)cudaEventDestroy(e0);
+    (void)cudaEventDestroy(e1);
+    throw;
+  }
+  (void)cudaEventDestroy(e0);
+  (void)cudaEventDestroy(e1);
+  // the captured graphs hold the old launch shapes
+  for (auto& ge : graphs_) {
+    if (ge) (void)cudaGraphExecDestroy(ge);
+    ge = nullptr;
+  }
+  return total;
 }
 
 template <typename T>

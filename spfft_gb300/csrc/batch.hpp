@@ -49,6 +49,12 @@ public:
   // backward, x, y, z for the forward; a fused group runs its plane kernel in the y slot).
   void stage_times(int direction, bool scaled, cudaStream_t stream, float ms[3]);
 
+  // Autotuner: per shape group, times `reps` backward + scaled forward pairs of the group alone on
+  // the bound buffers (overwriting them) for each plane strategy that fits (fused, split) and each
+  // sticks-per-z-block size, and keeps the fastest; drops captured graphs. Returns the sum over
+  // the groups of their best times per pair in milliseconds. Synchronous.
+  float autotune(cudaStream_t stream, int reps);
+
   int num_transforms() const { return static_cast<int>(tp_.size()); }
   // Stop keeping the transforms alive (for an owner that tracks their lifetime itself and drops
   // the plan before any of them goes away).
@@ -72,6 +78,7 @@ private:
   // Passes of one group on `s`: bit 0 backward, bit 1 forward (after the backward).
   void run_group(Group& g, int what, bool scaled, cudaStream_t s);
   void run_pass(Group& g, int pass, int direction, bool scaled, cudaStream_t s);
+  void set_z_shape(Group& g, int spb);
   void run_fallback(int what, bool scaled, cudaStream_t s);
   // Every group (and the unbatched transforms) as concurrent branches of `stream`.
   void run(int what, bool scaled, cudaStream_t stream);

@@ -198,6 +198,11 @@ GpuPlan<T>::GpuPlan(const IndexPlan& p, int device) {
         fastZ_ = true;
         fastSpb_ = spb;
       }
+      for (int cand : {32, 24, 16, 12, 8}) {
+        a.param = cand;
+        fast_dispatch<T>(FastOp::ZSmem, nz, false, a);
+        if (sm <= optin) zCands_.push_back(cand);
+      }
     }
     const bool r2c = p.type == SPFFT_TRANS_R2C;
     // Candidate plane strategies. SPFFT_GB300_PLANE=fused|split|generic forces one (when it is
@@ -212,22 +217,28 @@ GpuPlan<T>::GpuPlan(const IndexPlan& p, int device) {
       a.numColumns = ncol;
       // x chunk buffer of 2 * rows rows: two 256-thread blocks per SM when the block fits 112 KB
       // of shared memory, else the largest (<= 64 rows) that fits one 512-thread block per SM.
-      for (int rows = 16; rows >= 1 && !fusedOk; rows /= 2) {
+      for (int rows = 16; rows >= 1; rows /= 2) {
         a.param = rows;
         fast_dispatch<T>(FastOp::PlaneSmem, p.dimX, r2c, a);
         if (sm <= 112 * 1024) {
-          fusedOk = true;
-          fusedRows = rows;
-          fusedThreads_ = 256;
+          if (!fusedOk) {
+            fusedOk = true;
+            fusedRows = rows;
+            fusedThreads_ = 256;
+          }
+          fusedCands_.emplace_back(rows, 256);
         }
       }
-      for (int rows = 32; rows >= 1 && !fusedOk; rows /= 2) {
+      for (int rows = 32; rows >= 1; rows /= 2) {
         a.param = rows;
         fast_dispatch<T>(FastOp::PlaneSmem, p.dimX, r2c, a);
         if (sm <= optin) {
-          fusedOk = true;
-          fusedRows = rows;
-          fusedThreads_ = 512;
+          if (!fusedOk) {
+            fusedOk = true;
+            fusedRows = rows;
+            fusedThreads_ = 512;
+          }
+          fusedCands_.emplace_back(rows, 512);
         }
       }
     }
@@ -258,6 +269,21 @@ GpuPlan<T>::GpuPlan(const IndexPlan& p, int device) {
       splitOk = yFits && sm <= optin;
       cpb = std::min(cpb, std::max(1, ncol));
       rpb = std::min(rpb, p.dimY);
+      if (splitOk) {
+        for (int c : {4, 8, 16, 32}) {
+          a.param = c;
+          fast_dispatch<T>(FastOp::YSmem, p.dimY, r2c, a);
+          if (sm > optin || c > std::max(1, ncol)) continue;
+          for (int r : {8, 16, 32}) {
+            a.param = r;
+            fast_dispatch<T>(FastOp::XSmem, p.dimX, r2c, a);
+            if (sm <= optin && r <= p.dimY) splitCands_.emplace_back(c, r);
+          }
+        }
+        if (std::find(splitCands_.begin(), splitCands_.end(), std::make_pair(cpb, rpb)) == splitCands_.end()) {
+          splitCands_.emplace_back(cpb, rpb);
+        }
+      }
     }
     const char* force = std::getenv("SPFFT_GB300_PLANE");
     const std::string want = force ? force : "";
@@ -535,6 +561,126 @@ bool GpuPlan<T>::backward_staged(const T* values, T* devSpace, T* hostSpace, voi
   check_cuda(cudaEventRecord(events[kStagedChunks], copyStream));
   check_cuda(cudaStreamWaitEvent(stream, events[kStagedChunks], 0));
   return true;
+}
+
+template <typename T>
+typename GpuPlan<T>::Tuning GpuPlan<T>::tuning() const {
+  Tuning t;
+  t.spb = fastZ_ ? fastSpb_ : 0;
+  t.path = planePath_ == PlanePath::Fused ? 1 : planePath_ == PlanePath::Split ? 2 : 0;
+  if (t.path == 1) {
+    t.fusedRows = fastRows_;
+    t.fusedThreads = fusedThreads_;
+  }
+  if (t.path == 2) {
+    t.cpb = splitCpb_;
+    t.rpb = splitRpb_;
+  }
+  return t;
+}
+
+template <typename T>
+std::vector<typename GpuPlan<T>::Tuning> GpuPlan<T>::candidates() const {
+  std::vector<int> zs = zCands_;
+  if (zs.empty()) zs.push_back(0);
+  std::vector<Tuning> out;
+  for (int spb : zs) {
+    Tuning t;
+    t.spb = spb;
+    for (const auto& f : fusedCands_) {
+      t.path = 1;
+      t.fusedRows = f.first;
+      t.fusedThreads = f.second;
+      t.cpb = t.rpb = 0;
+      out.push_back(t);
+    }
+    for (const auto& sp : splitCands_) {
+      t.path = 2;
+      t.fusedRows = t.fusedThreads = 0;
+      t.cpb = sp.first;
+      t.rpb = sp.second;
+      out.push_back(t);
+    }
+    if (fusedCands_.empty() && splitCands_.empty()) {
+      t.path = 0;
+      t.fusedRows = t.fusedThreads = t.cpb = t.rpb = 0;
+      out.push_back(t);
+    }
+  }
+  return out;
+}
+
+template <typename T>
+void GpuPlan<T>::set_tuning(const Tuning& t) {
+  bool ok = false;
+  for (const Tuning& c : candidates()) {
+    ok |= c.spb == t.spb && c.path == t.path && c.fusedRows == t.fusedRows && c.fusedThreads == t.fusedThreads &&
+          c.cpb == t.cpb && c.rpb == t.rpb;
+  }
+  if (!ok) throw InvalidParameterError();
+  if (t.spb > 0) fastSpb_ = t.spb;
+  planePath_ = t.path == 1 ? PlanePath::Fused : t.path == 2 ? PlanePath::Split : PlanePath::Generic;
+  if (t.path == 1) {
+    fastRows_ = t.fusedRows;
+    fusedThreads_ = t.fusedThreads;
+  }
+  if (t.path == 2) {
+    splitCpb_ = t.cpb;
+    splitRpb_ = t.rpb;
+  }
+}
+
+template <typename T>
+float GpuPlan<T>::autotune(T* values, T* space, void* scratch, cudaStream_t stream, int reps) {
+  if (reps < 1) throw InvalidParameterError();
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  check_cuda(cudaEventCreate(&e0));
+  check_cuda(cudaEventCreate(&e1));
+  auto time_pair = [&](const Tuning& t) {
+    set_tuning(t);
+    backward(values, space, scratch, stream);  // warm-up
+    forward(space, values, true, scratch, stream);
+    check_cuda(cudaEventRecord(e0, stream));
+    for (int r = 0; r < reps; ++r) {
+      backward(values, space, scratch, stream);
+      forward(space, values, true, scratch, stream);
+    }
+    check_cuda(cudaEventRecord(e1, stream));
+    check_cuda(cudaEventSynchronize(e1));
+    float ms = 0.0f;
+    check_cuda(cudaEventElapsedTime(&ms, e0, e1));
+    return ms / reps;
+  };
+  const Tuning initial = tuning();
+  Tuning best = initial;
+  float bestMs = 0.0f;
+  try {
+    bestMs = time_pair(best);
+    // z shapes with the current plane strategy, then plane strategies with the best z shape
+    for (int pass = 0; pass < 2; ++pass) {
+      const Tuning base = best;
+      for (const Tuning& c : candidates()) {
+        const bool zOnly = c.path == base.path && c.fusedRows == base.fusedRows &&
+                           c.fusedThreads == base.fusedThreads && c.cpb == base.cpb && c.rpb == base.rpb;
+        const bool planeOnly = c.spb == base.spb;
+        if ((pass == 0 && !zOnly) || (pass == 1 && !planeOnly)) continue;
+        const float ms = time_pair(c);
+        if (ms < bestMs) {
+          bestMs = ms;
+          best = c;
+        }
+      }
+    }
+  } catch (...) {
+    (void)cudaEventDestroy(e0);
+    (void)cudaEventDestroy(e1);
+    set_tuning(initial);
+    throw;
+  }
+  (void)cudaEventDestroy(e0);
+  (void)cudaEventDestroy(e1);
+  set_tuning(best);
+  return bestMs;
 }
 
 size_t smem_optin(int device) { return static_cast<size_t>(max_smem_optin(device)); }

@@ -7,6 +7,8 @@
 #include <cuda_runtime.h>
 
 #include <memory>
+#include <utility>
+#include <vector>
 
 #include "kernels.hpp"
 #include "planner.hpp"
@@ -61,6 +63,26 @@ public:
     return (fastZ_ ? 1 : 0) | (planePath_ == PlanePath::Fused ? 2 : 0) | (planePath_ == PlanePath::Split ? 4 : 0);
   }
 
+  // Tile shapes and plane strategy the kernels run with.
+  struct Tuning {
+    int spb = 0;           // sticks per z block (0: generic z kernels)
+    int path = 0;          // 0 generic, 1 fused plane, 2 split y and x
+    int fusedRows = 0;     // fused: half of the x chunk buffer rows
+    int fusedThreads = 0;  // fused: threads per block (256: two blocks per SM, 512: one)
+    int cpb = 0, rpb = 0;  // split: columns per y block, rows per x block
+  };
+  Tuning tuning() const;
+  // Every tuning this plan can run (all combinations of the valid z, fused and split shapes).
+  std::vector<Tuning> candidates() const;
+  // Throws InvalidParameterError for a tuning that is not among candidates().
+  void set_tuning(const Tuning& t);
+  // Autotuner: times `reps` backward + scaled forward pairs per candidate on `values` / `space`
+  // (device buffers of this plan's sizes, overwritten) on `stream`, first over the z shapes with
+  // the current plane strategy, then over the plane strategies and tile shapes with the best z
+  // shape, and keeps the fastest. Returns its time per pair in milliseconds. No other work of
+  // this plan may run meanwhile.
+  float autotune(T* values, T* space, void* scratch, cudaStream_t stream, int reps);
+
   // Device view of this plan with its intermediates in `scratch` (used by batched execution).
   PlanView<T> device_view(void* scratch) const { return view(scratch); }
   T forward_scale() const { return scale_; }
@@ -79,6 +101,10 @@ private:
   LaunchConfig config_{};
   bool fastZ_ = false;
   PlanePath planePath_ = PlanePath::Generic;
+  // valid shapes, for the autotuner
+  std::vector<int> zCands_;
+  std::vector<std::pair<int, int>> fusedCands_;  // (rows, threads)
+  std::vector<std::pair<int, int>> splitCands_;  // (cpb, rpb)
   int fastSpb_ = 0, fastRows_ = 0, splitCpb_ = 0, splitRpb_ = 0, fusedThreads_ = 512;
   ScratchLayout layout_{};
   T scale_ = T(1);

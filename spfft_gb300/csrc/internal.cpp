@@ -282,6 +282,21 @@ void TransformInternal<T>::forward_device(const T* space, T* values, bool scaled
 }
 
 template <typename T>
+float TransformInternal<T>::autotune(int reps) {
+  DeviceGuard guard(grid_->device_id());
+  cudaStream_t s = begin();
+  void* scratch = grid_->scratch();
+  T* values = gpu_->staging(scratch);
+  T* space = grid_->space_device();
+  // zero data: finite everywhere, so every candidate runs its ordinary arithmetic
+  if (plan_->numValues > 0) check_cuda(cudaMemsetAsync(values, 0, sizeof(T) * 2 * plan_->numValues, s));
+  check_cuda(cudaMemsetAsync(space, 0, sizeof(T) * space_elements(), s));
+  const float ms = gpu_->autotune(values, space, scratch, s, reps);
+  check_cuda(cudaStreamSynchronize(s));
+  return ms;
+}
+
+template <typename T>
 void TransformInternal<T>::stage_times(int direction, const T* in, T* out, bool scaled,
                                        cudaStream_t stream, float ms[3]) {
   DeviceGuard guard(grid_->device_id());

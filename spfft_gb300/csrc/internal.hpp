@@ -122,6 +122,9 @@ public:
     gb300::DeviceGuard guard(grid_->device_id());
     gpu_->adjoint_forward(gradValues, gradSpace, scaled, grid_->scratch(), stream);
   }
+  // Autotuner over the plan's tile shapes on the grid's own buffers (see GpuPlan::autotune); on
+  // the user stream if one is set, else the internal stream; synchronous.
+  float autotune(int reps);
   // One pass in `direction` (0 backward, 1 forward) on device pointers with events between the
   // three kernels; waits for completion and returns the kernel times in milliseconds.
   void stage_times(int direction, const T* in, T* out, bool scaled, cudaStream_t stream,

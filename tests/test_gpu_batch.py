@@ -145,3 +145,30 @@ def test_batch_plane_pass_modes(lib, dtype, mode, monkeypatch):
         assert rel_l2(it["vals"].cpu().numpy(), want) <= TOL[dtype], it["dims"]
     ms_b = batch.stage_times(0, sp.SPFFT_NO_SCALING, stream)
     assert len(ms_b) == 3 and all(t >= 0 for t in ms_b)
+
+
+@pytest.mark.parametrize("dtype", ["float64", "float32"])
+def test_batch_autotune_then_graph(lib, dtype):
+    """Autotuning a bound batch (per group: plane strategy and z block size), then a captured pair
+    with new data against the oracle."""
+    rng = np.random.default_rng(6)
+    items = _make(dtype, [(64, 16, 0), (64, 16, 0), (60, 15, 1), (48, 12, 1), ((13, 12, 11), 0, 0)], rng)
+    batch = sp.Batch([it["tr"] for it in items])
+    batch.bind([it["vals"] for it in items], [it["space"] for it in items])
+    stream = torch.cuda.Stream()
+    batch.pair_graph(sp.SPFFT_FULL_SCALING, stream)  # a graph captured before tuning is dropped
+    stream.synchronize()
+    assert batch.autotune(2, stream) > 0
+    host_vals = []
+    for it in items:
+        v = rng.uniform(-1, 1, len(it["idx"])) + 1j * rng.uniform(-1, 1, len(it["idx"]))
+        if it["ttype"] == 1:
+            v[(it["idx"] == 0).all(axis=1)] = v[(it["idx"] == 0).all(axis=1)].real
+        host_vals.append(v)
+        it["vals"].copy_(torch.from_numpy(v).to(it["vals"].dtype))
+    torch.cuda.synchronize()
+    batch.pair_graph(sp.SPFFT_FULL_SCALING, stream)
+    stream.synchronize()
+    for it, v in zip(items, host_vals):
+        o = it["oracle"]
+        assert rel_l2(it["vals"].cpu().numpy(), o.forward(o.backward(v), scaled=True)) <= 10 * TOL[dtype], it["dims"]

@@ -390,3 +390,30 @@ def test_every_specialised_length(lib, dtype):
     stream.synchronize()
     for tr, v, space, oracle, vals in items:
         assert rel_l2(space.cpu().numpy(), oracle.backward(vals)) <= TOL[dtype]
+
+
+@pytest.mark.parametrize("dtype", ["float64", "float32"])
+def test_autotune_keeps_results(lib, dtype):
+    """The autotuner picks one of the valid tile shapes and plane strategies; results after tuning
+    still match the oracle."""
+    rng = np.random.default_rng(43)
+    for n, radius, ttype in [(64, 16, 0), (192, 48, 1)]:
+        idx = sphere_indices(n, radius, r2c=(ttype == 1))
+        tr = _transform(dtype, ttype, (n, n, n), idx)
+        before = tr.tuning()
+        ms = tr.autotune(2)
+        after = tr.tuning()
+        assert ms > 0 and after["plane"] in ("fused", "split"), (before, after)
+        assert after["sticks_per_z_block"] in (8, 12, 16, 24, 32)
+        vals = _values(rng, idx.shape[0])
+        if ttype == 1:
+            vals[(idx == 0).all(axis=1)] = vals[(idx == 0).all(axis=1)].real
+        oracle = pipeline.HostPipeline(ttype, n, n, n, idx)
+        v = torch.from_numpy(vals).to(CT[dtype]).cuda()
+        out = torch.empty((n, n, n), dtype=CT[dtype] if ttype == 0 else RT[dtype], device="cuda")
+        tr.backward(v, out)
+        want = oracle.backward(vals)
+        assert rel_l2(out.cpu().numpy(), want) <= TOL[dtype], (n, after)
+        f = torch.empty_like(v)
+        tr.forward(out, f)
+        assert rel_l2(f.cpu().numpy(), oracle.forward(want)) <= TOL[dtype], (n, after)
