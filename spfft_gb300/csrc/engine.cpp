@@ -683,6 +683,16 @@ float GpuPlan<T>::autotune(T* values, T* space, void* scratch, cudaStream_t stre
   return bestMs;
 }
 
+namespace fast {
+bool pdl_enabled() {
+  static const bool on = [] {
+    const char* e = std::getenv("SPFFT_GB300_PDL");
+    return !(e && e[0] == '0');
+  }();
+  return on;
+}
+}  // namespace fast
+
 size_t smem_optin(int device) { return static_cast<size_t>(max_smem_optin(device)); }
 template <typename T>
 bool fast_prepare(int device, int n) {

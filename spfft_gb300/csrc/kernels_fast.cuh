@@ -101,6 +101,15 @@ __device__ __forceinline__ int max_exponent(double2 v) {
 // Zero, subnormal-only and non-finite blocks use k = 0.
 __device__ __forceinline__ int block_scale(int e) { return (e == 0 || e == 2047) ? 0 : 1023 - e; }
 
+// Programmatic dependent launch (sm_90+): kernels of the same transform are launched so that the
+// next kernel's blocks may start while the previous kernel finishes. Each kernel loads only its
+// constant plan tables (twiddles, index maps) before pdl_wait(), which returns once the previous
+// kernel of the stream has completed and its writes are visible; every read of data another
+// kernel produces and every global write comes after it. pdl_trigger() lets the next kernel launch
+// once every block of this one has passed it. Both are no-ops for an ordinary launch.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 // Division by a block-uniform runtime divisor d in [1, 2^16) for numerators n in [0, 2^16): one
 // high multiply by m = floor(2^32 / d) + 1 instead of the division sequence. Exact because
 // n * (m - 2^32 / d) < n * 1 < 2^32 / d, i.e. the error stays below one step of n / d.
@@ -200,6 +209,8 @@ __device__ __forceinline__ void z_backward_body(const PlanView<S>& p, const S* _
   load_twiddles<S, A>(tw, p.twz, NZ);
   for (int i = threadIdx.x; i < nsb * PZ; i += blockDim.x) buf[i] = czero<A>();
   __syncthreads();
+  pdl_wait();
+  pdl_trigger();
 
   const CS* vals = reinterpret_cast<const CS*>(values);
   const int e0 = p.stickEntryStart[s0], e1 = p.stickEntryStart[s0 + nsb];
@@ -268,6 +279,8 @@ __device__ __forceinline__ void z_forward_body(const PlanView<S>& p, S* __restri
   const FastDiv dns(nsb);
 
   load_twiddles<S, A>(tw, p.twz, NZ);
+  pdl_wait();
+  pdl_trigger();
   const CS* sticks = reinterpret_cast<const CS*>(p.sticks) + s0;
   for (int i = threadIdx.x; i < NZ * nsb; i += blockDim.x) {
     const int z = dns.div(i), sl = i - z * nsb;
@@ -414,6 +427,8 @@ __device__ __forceinline__ void plane_backward_body(const PlanView<S>& p, S* __r
   plane_load_tables<S, A, NX, NY, R2C>(p, s);
   for (int i = threadIdx.x; i < NY * nc; i += blockDim.x) s.P[i] = czero<A>();
   __syncthreads();
+  pdl_wait();
+  pdl_trigger();
 
   // sticks of this plane -> compact columns, all copies in flight at once
   // (slot loads four at a time, so their latencies overlap)
@@ -539,6 +554,8 @@ __device__ __forceinline__ void plane_forward_body(const PlanView<S>& p, const S
     }
     cp_async_commit();
   };
+  pdl_wait();
+  pdl_trigger();
   issue_chunk(0);
 
   // Block scale (double-float only): the largest exponent of the whole plane, read once up front
@@ -666,6 +683,25 @@ cudaError_t allow_dynamic_smem(K kernel, size_t maxSmem) {
   const size_t avail = maxSmem > attr.sharedSizeBytes ? maxSmem - attr.sharedSizeBytes : 0;
   return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(avail));
 }
+// Launch with programmatic stream serialization (see pdl_wait); SPFFT_GB300_PDL=0 at the first
+// launch turns it off for the process. Errors are left for cudaGetLastError like <<<>>> launches.
+bool pdl_enabled();
+template <typename... KArgs, typename... Args>
+inline void launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                       Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = pdl_enabled() ? 1 : 0;
+  (void)cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
+
 template <typename S, typename A, int NZ>
 struct ZKernels {
   using CA = typename Types<S, A>::CA;
@@ -677,11 +713,11 @@ struct ZKernels {
   }
   static void backward(const PlanView<S>& p, int spb, const S* values, cudaStream_t st) {
     const int g = (p.numSticks + spb - 1) / spb;
-    z_backward<S, A, NZ><<<g, kThreads, smem(spb), st>>>(p, values, spb);
+    launch_pdl(z_backward<S, A, NZ>, g, kThreads, smem(spb), st, p, values, spb);
   }
   static void forward(const PlanView<S>& p, int spb, S* values, S scale, cudaStream_t st) {
     const int g = (p.numSticks + spb - 1) / spb;
-    z_forward<S, A, NZ><<<g, kThreads, smem(spb), st>>>(p, values, scale, spb);
+    launch_pdl(z_forward<S, A, NZ>, g, kThreads, smem(spb), st, p, values, scale, spb);
   }
 };
 
@@ -698,10 +734,10 @@ struct PlaneKernels {
   // `half`: the shared memory holds 2 * half rows of x chunk buffer, which both directions use as
   // one chunk of 2 * half rows (single-buffered, like the batched plane passes).
   static void backward(const PlanView<S>& p, int half, S* space, cudaStream_t st, int threads) {
-    plane_backward<S, A, NX, NY, R2C><<<p.dimZ, threads, smem(p.numColumns, half), st>>>(p, space, 2 * half);
+    launch_pdl(plane_backward<S, A, NX, NY, R2C>, p.dimZ, threads, smem(p.numColumns, half), st, p, space, 2 * half);
   }
   static void forward(const PlanView<S>& p, int half, const S* space, cudaStream_t st, int threads) {
-    plane_forward<S, A, NX, NY, R2C><<<p.dimZ, threads, smem(p.numColumns, half), st>>>(p, space, 2 * half);
+    launch_pdl(plane_forward<S, A, NX, NY, R2C>, p.dimZ, threads, smem(p.numColumns, half), st, p, space, 2 * half);
   }
 };
 
@@ -726,6 +762,8 @@ __device__ __forceinline__ void y_backward_body(const PlanView<S>& p, int cpb, i
   load_twiddles<S, A>(tw, p.twy, NY);
   for (int i = threadIdx.x; i < NY * ncb; i += blockDim.x) buf[i] = czero<A>();
   __syncthreads();
+  pdl_wait();
+  pdl_trigger();
   const CS* sticks = reinterpret_cast<const CS*>(p.sticks) + static_cast<size_t>(z) * p.numSticks;
   const int sBegin = p.columnStickStart[c0], sEnd = p.columnStickStart[c0 + ncb];
   for (int st0 = sBegin + threadIdx.x; st0 < sEnd; st0 += 4 * blockDim.x) {
@@ -783,6 +821,8 @@ __device__ __forceinline__ void y_forward_body(const PlanView<S>& p, int cpb, in
   const int c0 = bx * cpb, ncb = min(cpb, nc - c0);
   const FastDiv dncb(ncb), dnc(nc);
   load_twiddles<S, A>(tw, p.twy, NY);
+  pdl_wait();
+  pdl_trigger();
   const CS* planes = reinterpret_cast<const CS*>(p.planes) + static_cast<size_t>(z) * NY * nc + c0;
   for (int i = threadIdx.x; i < NY * ncb; i += blockDim.x) {
     const int y = dncb.div(i), c = i - y * ncb;
@@ -891,6 +931,8 @@ __device__ __forceinline__ void x_backward_body(const PlanView<S>& p, S* __restr
   const int y0 = bx * rpb, nr = min(rpb, ny - y0);
   RowSmem<CA, NX, R2C> s(nc, rpb);
   row_load_tables<S, A, NX, R2C>(p, s);
+  pdl_wait();
+  pdl_trigger();
   const CS* planes = reinterpret_cast<const CS*>(p.planes) + (static_cast<size_t>(z) * ny + y0) * nc;
   for (int i = threadIdx.x; i < nr * nc; i += blockDim.x) cp_async_c(s.P + i, planes + i);
   cp_async_commit();
@@ -962,6 +1004,8 @@ __device__ __forceinline__ void x_forward_body(const PlanView<S>& p, const S* __
   RowSmem<CA, NX, R2C> s(nc, rpb, !R2C);
   if (TT::kScaled && threadIdx.x == 0) sExp = 0;
   row_load_tables<S, A, NX, R2C>(p, s);
+  pdl_wait();
+  pdl_trigger();
   const CS* rows = reinterpret_cast<const CS*>(space + (static_cast<size_t>(z) * ny + y0) * NX * (R2C ? 1 : 2));
   for (int i = threadIdx.x; i < nr * L::LX; i += blockDim.x) {
     const int rl = i / L::LX, e = i - rl * L::LX;
@@ -1047,11 +1091,11 @@ struct YSplitKernels {
   }
   static void backward(const PlanView<S>& p, int cpb, cudaStream_t st) {
     const dim3 g((p.numColumns + cpb - 1) / cpb, p.dimZ);
-    y_backward_split<S, A, NY><<<g, kThreads, smem(cpb), st>>>(p, cpb);
+    launch_pdl(y_backward_split<S, A, NY>, g, kThreads, smem(cpb), st, p, cpb);
   }
   static void forward(const PlanView<S>& p, int cpb, cudaStream_t st) {
     const dim3 g((p.numColumns + cpb - 1) / cpb, p.dimZ);
-    y_forward_split<S, A, NY><<<g, kThreads, smem(cpb), st>>>(p, cpb);
+    launch_pdl(y_forward_split<S, A, NY>, g, kThreads, smem(cpb), st, p, cpb);
   }
 };
 
@@ -1072,11 +1116,11 @@ struct XSplitKernels {
   // planes [z0, z0 + nz) (nz < 0: all planes from z0)
   static void backward(const PlanView<S>& p, int rpb, S* space, cudaStream_t st, int z0, int nz) {
     const dim3 g((p.dimY + rpb - 1) / rpb, nz < 0 ? p.dimZ - z0 : nz);
-    x_backward_split<S, A, NX, R2C><<<g, kThreads, smem(p.numColumns, rpb), st>>>(p, space, rpb, z0);
+    launch_pdl(x_backward_split<S, A, NX, R2C>, g, kThreads, smem(p.numColumns, rpb), st, p, space, rpb, z0);
   }
   static void forward(const PlanView<S>& p, int rpb, const S* space, cudaStream_t st, int z0, int nz) {
     const dim3 g((p.dimY + rpb - 1) / rpb, nz < 0 ? p.dimZ - z0 : nz);
-    x_forward_split<S, A, NX, R2C><<<g, kThreads, smem_forward(p.numColumns, rpb), st>>>(p, space, rpb, z0);
+    launch_pdl(x_forward_split<S, A, NX, R2C>, g, kThreads, smem_forward(p.numColumns, rpb), st, p, space, rpb, z0);
   }
 };
 
