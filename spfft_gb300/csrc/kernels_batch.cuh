@@ -77,14 +77,14 @@ __global__ void __launch_bounds__(kThreads) x_forward_batch(const BatchView<S> b
 
 // Fused y + x passes, one block per plane (cubic planes): starts count planes.
 template <typename S, typename A, int N, bool R2C>
-__global__ void __launch_bounds__(kPlaneThreads) plane_backward_batch(const BatchView<S> bv, int rows) {
+__global__ void __launch_bounds__(BatchPlaneThreads<A>::value, 2) plane_backward_batch(const BatchView<S> bv, int rows) {
   __shared__ int sExp;
   const int t = find_transform(bv.starts, bv.count, blockIdx.x);
   plane_backward_body<S, A, N, N, R2C>(bv.views[t], bv.out[t], rows, blockIdx.x - bv.starts[t], &sExp);
 }
 
 template <typename S, typename A, int N, bool R2C>
-__global__ void __launch_bounds__(kPlaneThreads) plane_forward_batch(const BatchView<S> bv, int rows, int wRows) {
+__global__ void __launch_bounds__(BatchPlaneThreads<A>::value, 2) plane_forward_batch(const BatchView<S> bv, int rows, int wRows) {
   __shared__ int sExp;
   const int t = find_transform(bv.starts, bv.count, blockIdx.x);
   plane_forward_body<S, A, N, N, R2C>(bv.views[t], bv.in[t], rows, wRows, blockIdx.x - bv.starts[t], &sExp);

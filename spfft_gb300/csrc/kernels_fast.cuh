@@ -35,7 +35,12 @@ namespace fast {
 
 constexpr int kThreads = 256;       // z-pass blocks
 constexpr int kPlaneThreads = 512;  // plane blocks (one plane per block, so more warps per SM)
-constexpr int kBatchPlaneThreads = 256;  // batched plane blocks (two blocks per SM)
+// Batched plane blocks (two per SM): 384 threads in FP32 (80 registers), 256 in double-float
+// (whose register demand would spill at 384).
+template <typename A>
+struct BatchPlaneThreads {
+  static constexpr int value = 384;
+};
 // Minimum resident blocks per SM asked of the compiler for the split y kernels and the split x
 // forward kernel: double-float kernels are capped at 80 registers so that three 256-thread
 // blocks share an SM (24 warps to hide the FP32 pipe latencies of the dd dependency chains;
@@ -48,6 +53,10 @@ struct YMinBlocks {
 template <>
 struct YMinBlocks<dd> {
   static constexpr int value = 3;
+};
+template <>
+struct BatchPlaneThreads<dd> {
+  static constexpr int value = 256;
 };
 
 extern __shared__ __align__(16) unsigned char g_fast_smem[];
