@@ -420,6 +420,36 @@ __device__ __forceinline__ void plane_load_tables(const PlanView<S>& p,
   }
 }
 
+// C2R half-length packing of nr compact rows into the x-FFT rows of W (natural order, slot
+// L::wpos(k)): Z[k] = (X[k] + conj X[M-k]) + i e^{+2 pi i k/N} (X[k] - conj X[M-k]) with only the
+// real parts of X[0] and X[M] (the C2R convention). One work item per pair (k, M - k): with
+// s = X[k] + conj X[M-k], d = X[k] - conj X[M-k] and u = d e^{+2 pi i k/N},
+// Z[k] = s + i u and Z[M-k] = conj(s) + i conj(u), so the loads, sums and the product serve both.
+// Pairs j = 0 .. floor(M/2) cover every k (for even M the middle pair is k = M/2 alone).
+// `row(rl)` gives compact row rl.
+template <typename L, typename CA, typename RowFn>
+__device__ __forceinline__ void c2r_pack_rows(RowFn row, int nr, CA* W, const int* colOf, const CA* twx) {
+  using A = decltype(CA{}.x);
+  constexpr int M = L::M, H = M / 2;
+  for (int i = threadIdx.x; i < nr * (H + 1); i += blockDim.x) {
+    const int rl = i / (H + 1), j = i - rl * (H + 1);
+    const CA* prow = row(rl);
+    CA* wrow = W + rl * L::WP;
+    const int ck = colOf[j], cm = colOf[M - j];
+    const CA xk = ck >= 0 ? prow[ck] : make_c(A(0), A(0));
+    const CA xm = cm >= 0 ? prow[cm] : make_c(A(0), A(0));
+    if (j == 0) {
+      wrow[L::wpos(0)] = make_c(xk.x + xm.x, xk.x - xm.x);
+    } else {
+      const CA sum = make_c(xk.x + xm.x, xk.y - xm.y);
+      const CA dif = make_c(xk.x - xm.x, xk.y + xm.y);
+      const CA u = cmulc(dif, twx[j]);
+      wrow[L::wpos(j)] = make_c(sum.x - u.y, sum.y + u.x);
+      if (2 * j != M) wrow[L::wpos(M - j)] = make_c(sum.x + u.y, u.x - sum.y);  // M - j = j only for even M
+    }
+  }
+}
+
 template <typename S, typename A, int NX, int NY, bool R2C>
 __device__ __forceinline__ void plane_backward_body(const PlanView<S>& p, S* __restrict__ space, int rows,
                                                     int z, int* sExpPtr) {
@@ -480,9 +510,14 @@ __device__ __forceinline__ void plane_backward_body(const PlanView<S>& p, S* __r
   const CA* twl = R2C ? s.twm : s.twx;
   for (int r0 = 0; r0 < NY; r0 += rows) {
     const int nr = min(rows, NY - r0);
+    if (R2C) {
+      c2r_pack_rows<L>([&](int rl) { return s.P + transposed_pos<NY>(r0 + rl) * nc; }, nr, s.W, s.colOf, s.twx);
+      __syncthreads();
+    }
     for (int i = threadIdx.x; i < nr * Bx; i += blockDim.x) {
       const int rl = i / Bx, b = i - rl * Bx;
       const CA* prow = s.P + transposed_pos<NY>(r0 + rl) * nc;
+      CA* wrow = s.W + rl * L::WP;
       CA v[Ax];
 #pragma unroll
       for (int a = 0; a < Ax; ++a) {
@@ -491,23 +526,10 @@ __device__ __forceinline__ void plane_backward_body(const PlanView<S>& p, S* __r
           const int col = s.colOf[kk];
           v[a] = col >= 0 ? prow[col] : czero<A>();
         } else {
-          // Half-length C2R: Z'[k] = (X[k] + conj X[M-k]) + i e^{+2 pi i k/N} (X[k] - conj X[M-k]),
-          // with only the real parts of X[0] and X[M] (the C2R convention).
-          const int ck = s.colOf[kk], cm = s.colOf[L::M - kk];
-          const CA xk = ck >= 0 ? prow[ck] : czero<A>();
-          const CA xm = cm >= 0 ? prow[cm] : czero<A>();
-          if (kk == 0) {
-            v[a] = make_c(xk.x + xm.x, xk.x - xm.x);
-          } else {
-            const CA sum = make_c(xk.x + xm.x, xk.y - xm.y);
-            const CA dif = make_c(xk.x - xm.x, xk.y + xm.y);
-            const CA u = cmulc(dif, s.twx[kk]);
-            v[a] = make_c(sum.x - u.y, sum.y + u.x);
-          }
+          v[a] = wrow[L::wpos(kk)];
         }
       }
       fft_pass1_regs<L::LX, +1>(v, b, twl);
-      CA* wrow = s.W + rl * L::WP;
 #pragma unroll
       for (int k1 = 0; k1 < Ax; ++k1) wrow[L::wpos(k1 * Bx + b)] = v[k1];
     }
@@ -949,9 +971,14 @@ __device__ __forceinline__ void x_backward_body(const PlanView<S>& p, S* __restr
   __syncthreads();
   const int k = convert_block<S, A>(s.P, nr * nc, &sExp);
   const CA* twl = R2C ? s.twm : s.twx;
+  if (R2C) {
+    c2r_pack_rows<L>([&](int rl) { return s.P + rl * nc; }, nr, s.W, s.colOf, s.twx);
+    __syncthreads();
+  }
   for (int i = threadIdx.x; i < nr * Bx; i += blockDim.x) {
     const int rl = i / Bx, b = i - rl * Bx;
     const CA* prow = s.P + rl * nc;
+    CA* wrow = s.W + rl * L::WP;
     CA v[Ax];
 #pragma unroll
     for (int a = 0; a < Ax; ++a) {
@@ -960,21 +987,10 @@ __device__ __forceinline__ void x_backward_body(const PlanView<S>& p, S* __restr
         const int col = s.colOf[kk];
         v[a] = col >= 0 ? prow[col] : czero<A>();
       } else {
-        const int ck = s.colOf[kk], cm = s.colOf[L::M - kk];
-        const CA xk = ck >= 0 ? prow[ck] : czero<A>();
-        const CA xm = cm >= 0 ? prow[cm] : czero<A>();
-        if (kk == 0) {
-          v[a] = make_c(xk.x + xm.x, xk.x - xm.x);
-        } else {
-          const CA sum = make_c(xk.x + xm.x, xk.y - xm.y);
-          const CA dif = make_c(xk.x - xm.x, xk.y + xm.y);
-          const CA u = cmulc(dif, s.twx[kk]);
-          v[a] = make_c(sum.x - u.y, sum.y + u.x);
-        }
+        v[a] = wrow[L::wpos(kk)];
       }
     }
     fft_pass1_regs<L::LX, +1>(v, b, twl);
-    CA* wrow = s.W + rl * L::WP;
 #pragma unroll
     for (int k1 = 0; k1 < Ax; ++k1) wrow[L::wpos(k1 * Bx + b)] = v[k1];
   }
