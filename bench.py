@@ -165,7 +165,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.QUERY}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "50"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
@@ -203,6 +203,15 @@ class ClockSampler:
                     reasons.add(name)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
                 "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def load_window(step, stream, seconds: float = 0.2) -> None:
+    """Run `step` untimed until about `seconds` of GPU work has passed (clock samples under load)."""
+    t0 = time.perf_counter()
+    while time.perf_counter() - t0 < seconds:
+        for _ in range(8):
+            step()
+        stream.synchronize()
 
 
 # ---------------------------------------------------------------------------------------------
@@ -294,6 +303,10 @@ def measure_gpu(args, rank: int, world: int) -> dict:
         dist.barrier()
     torch.cuda.synchronize()
     with ClockSampler(dev) as clocks:
+        # the sampler's first readings come from this untimed load window (about 0.2 s of the same
+        # pairs), so a short timed region still has clock samples taken under load around it
+        with torch.cuda.stream(stream):
+            load_window(pair, stream)
         wall0 = time.perf_counter()
         with torch.cuda.stream(stream):
             for k in range(args.steps):
@@ -560,6 +573,7 @@ def measure_batch_workload(args, rank: int, world: int) -> dict:
         dist.barrier()
     torch.cuda.synchronize()
     with ClockSampler(dev) as clocks:
+        load_window(lambda: bt.pair_graph(sp.SPFFT_FULL_SCALING, stream), stream)
         for k in range(args.steps):
             starts[k].record(stream)
             bt.pair_graph(sp.SPFFT_FULL_SCALING, stream)
