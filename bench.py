@@ -400,6 +400,9 @@ def measure_gpu(args, rank: int, world: int) -> dict:
         e2e["staged_copies_value"] = round(e2e_steps / (time.perf_counter() - t0) * world, 3)
         del tr2
 
+    # ---- comparison point: the same pair through dense 3D cuFFT (torch.fft) on the full grid ----
+    cufft = measure_cufft_dense(args, idx, vals_h, n, r2c, ct, stream)
+
     # correctness guard on the timed output: forward(backward(v)) = N * v on C2C, and on R2C for
     # the values that are not on the x = 0 plane (those are folded by the hermitian fill)
     got = out_vals.cpu().numpy()
@@ -413,10 +416,55 @@ def measure_gpu(args, rank: int, world: int) -> dict:
         "batched": batched,
         "pairs_per_s": pairs_per_s, "ms_per_step": total_ms / args.steps, "wall_s": wall,
         "clocks": clocks.summary(), "roofline": roofline, "e2e": e2e,
-        "pair_gbs": pair_gbs, "roundtrip_rel_l2": err,
+        "pair_gbs": pair_gbs, "roundtrip_rel_l2": err, "cufft_dense": cufft,
         "launches_per_step": 6 if tr.path_info()["split_plane"] else 4, "npts": npts, "nsticks": nsticks,
         "ncols": ncols, "tuning": tuned or tr.tuning(),
     }
+
+
+def measure_cufft_dense(args, idx: np.ndarray, vals_h: np.ndarray, n: int, r2c: bool, ct, stream) -> dict:
+    """Pairs/s of the dense formulation with cuFFT (torch.fft): zero the full (half-)spectrum grid,
+    scatter the values, inverse 3D FFT without scaling, forward 3D FFT, gather the values. Device
+    buffers, CUDA events, L2 flushed between steps like the main measurement. A comparison point
+    for the sparse kernels; its hermitian handling of the x = 0 plane is cuFFT's, not the
+    reference's."""
+    import torch
+
+    nx = n // 2 + 1 if r2c else n
+    wrapped = np.mod(idx.astype(np.int64), n)
+    lin = torch.from_numpy((wrapped[:, 2] * n + wrapped[:, 1]) * nx + wrapped[:, 0]).cuda()
+    values = torch.from_numpy(vals_h).to(ct).cuda()
+    grid = torch.zeros((n, n, nx), dtype=ct, device="cuda")
+    out = torch.empty_like(values)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def pair():
+        grid.zero_()
+        grid.view(-1)[lin] = values
+        if r2c:
+            space = torch.fft.irfftn(grid, s=(n, n, n), norm="forward")
+            spec = torch.fft.rfftn(space, norm="backward")
+        else:
+            space = torch.fft.ifftn(grid, norm="forward")
+            spec = torch.fft.fftn(space, norm="backward")
+        out.copy_(spec.reshape(-1)[lin])
+
+    with torch.cuda.stream(stream):
+        for _ in range(max(3, args.warmup)):
+            pair()
+        stream.synchronize()
+        steps = max(3, min(args.steps, 20))
+        ms = 0.0
+        for _ in range(steps):
+            flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            pair()
+            b.record(stream)
+            b.synchronize()
+            ms += a.elapsed_time(b)
+    return {"value": round(steps / (ms / 1e3), 2), "unit": UNIT, "library": "cuFFT through torch.fft",
+            "form": "dense 3D grid: zero, scatter, inverse FFT, forward FFT, gather"}
 
 
 def measure_batched(args, workload: str, batch: int, dtype: str, radii=None) -> dict:
@@ -497,8 +545,28 @@ def measure_batched(args, workload: str, batch: int, dtype: str, radii=None) -> 
         got = vals[b].cpu().numpy().astype(np.complex128)
         sel = idxs[b][:, 0] != 0 if r2c else slice(None)
         errs.append(float(np.linalg.norm(got[sel] - hosts[b][sel]) / np.linalg.norm(hosts[b][sel])))
+    # FP32 against FP64: backward of the first and the last transform against the FP64 transform
+    fp64_err = {}
+    if dtype == "float32":
+        for b in range(batch):
+            vals[b].copy_(torch.from_numpy(hosts[b]).to(ct))
+        bt.backward(stream)
+        stream.synchronize()
+        rl2, mab = [], []
+        for b in sorted({0, batch - 1}):
+            t64 = sp.Transform(1, sp.SPFFT_PU_GPU, ttype, n, n, n, len(idxs[b]), sp.SPFFT_INDEX_TRIPLETS, idxs[b],
+                               dtype="float64")
+            s64 = torch.empty((n, n, n), dtype=torch.float64 if r2c else torch.complex128, device="cuda")
+            t64.backward(torch.from_numpy(hosts[b]).cuda(), s64)
+            d = (spaces[b].to(s64.dtype) - s64).flatten()
+            rl2.append(float(torch.linalg.vector_norm(d) / torch.linalg.vector_norm(s64.flatten())))
+            mab.append(float(d.abs().max() / s64.abs().max()))
+            del t64, s64
+        fp64_err = {"backward_space_rel_l2_max": max(rl2), "backward_space_rel_maxabs_max": max(mab),
+                    "transforms_checked": len(rl2)}
     info = bt.info()
     return {"value": round(batch * args.steps / (ms / 1e3), 2), "unit": UNIT, "dtype": dtype,
+            "fp32_vs_fp64": fp64_err,
             "transforms_per_step": batch, "ms_per_step": round(ms / args.steps, 4),
             "graph_launches_per_step": 1, "kernel_launches_per_step": info["launches_per_pair"],
             "shape_groups": info["groups"], "roundtrip_rel_l2_max": max(errs),
@@ -644,18 +712,23 @@ def measure_batch_workload(args, rank: int, world: int) -> dict:
         d.copy_(torch.from_numpy(h).to(ct32))
     bt.backward(stream)
     stream.synchronize()
-    sample = sorted(set(list(range(min(4, len(mine)))) + list(range(max(0, len(mine) - 4), len(mine)))))
-    errs_b, errs_f = [], []
+    # every transform of this rank: relative L2 and relative max-abs error of the FP32 backward
+    # (space) and of the FP32 forward of that space (values), each against the FP64 path
+    sample = list(range(len(mine)))
+    errs_b, errs_f, maxabs_b, maxabs_f = [], [], [], []
     out32 = [torch.empty_like(vals32[i]) for i in range(len(mine))]
     for i in sample:
         trs64[i].backward(vals64[i], spaces64[i])
-        errs_b.append(float(torch.linalg.vector_norm((spaces32[i].to(spaces64[i].dtype) - spaces64[i]).flatten())
-                            / torch.linalg.vector_norm(spaces64[i].flatten())))
+        d = (spaces32[i].to(spaces64[i].dtype) - spaces64[i]).flatten()
+        ref = spaces64[i].flatten()
+        errs_b.append(float(torch.linalg.vector_norm(d) / torch.linalg.vector_norm(ref)))
+        maxabs_b.append(float(d.abs().max() / ref.abs().max()))
         f64 = torch.empty_like(vals64[i])
         trs64[i].forward(spaces64[i], f64, sp.SPFFT_FULL_SCALING)
         trs32[i].forward(spaces32[i], out32[i], sp.SPFFT_FULL_SCALING)
-        errs_f.append(float(torch.linalg.vector_norm((out32[i].to(ct64) - f64).flatten())
-                            / torch.linalg.vector_norm(f64.flatten())))
+        d = (out32[i].to(ct64) - f64).flatten()
+        errs_f.append(float(torch.linalg.vector_norm(d) / torch.linalg.vector_norm(f64.flatten())))
+        maxabs_f.append(float(d.abs().max() / f64.abs().max()))
 
     # ---- FP64 plain: the drop-in API, one transform after another ------------------------------
     for t in trs64:
@@ -686,6 +759,11 @@ def measure_batch_workload(args, rank: int, world: int) -> dict:
             "launches_per_step": info["launches_per_pair"], "groups": info["groups"],
             "unbatched": info["unbatched"], "fp64_plain": plain,
             "err_backward": max(errs_b), "err_forward": max(errs_f), "sampled": len(sample),
+            "err_stats": {"backward_space_rel_l2": {"max": max(errs_b), "median": statistics.median(errs_b)},
+                          "backward_space_rel_maxabs": {"max": max(maxabs_b), "median": statistics.median(maxabs_b)},
+                          "forward_values_rel_l2": {"max": max(errs_f), "median": statistics.median(errs_f)},
+                          "forward_values_rel_maxabs": {"max": max(maxabs_f), "median": statistics.median(maxabs_f)},
+                          "per_transform_backward_rel_l2": [float(f"{e:.3g}") for e in errs_b]},
             "transforms": len(specs_all)}
 
 
@@ -792,6 +870,7 @@ def main() -> int:
         "e2e": res["e2e"], "clocks": res["clocks"],
         "gpu_launches": res["launches_per_step"] * args.steps,
         "roundtrip_rel_l2": res["roundtrip_rel_l2"], "tuning": res["tuning"],
+        "cufft_dense_comparison": res["cufft_dense"],
     }
     if res["batched"]:
         line["fp32_batched"] = res["batched"]
@@ -849,6 +928,7 @@ def batch_main(args, rank: int, world: int) -> int:
         "shape_groups": res["groups"], "unbatched_transforms": res["unbatched"],
         "fp64_plain": {"value": round(res["fp64_plain"], 2), "unit": UNIT,
                        "ratio_fp32_batched_vs_fp64_plain": round(res["value"] / res["fp64_plain"], 2)},
+        "fp32_vs_fp64_errors": res["err_stats"],
         "fp32_vs_fp64_rel_l2_max": {"backward_space": res["err_backward"], "forward_values": res["err_forward"],
                                     "transforms_checked": res["sampled"]},
     }
