@@ -205,6 +205,28 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+# ---------------------------------------------------------------------------------------------
+# multi-rank host logic (one process per GPU; covered by gloo tests on the CPU)
+# ---------------------------------------------------------------------------------------------
+def shard(count: int, rank: int, world: int) -> list:
+    """Transforms of a batch owned by `rank`: round robin, so every transform has exactly one
+    owner and the ranks' shares differ by at most one (no collective on the data path)."""
+    return list(range(rank, count, world))
+
+
+def max_over_ranks(value: float, world: int) -> float:
+    """The largest `value` over all ranks (the job's time is its slowest rank's)."""
+    if world <= 1:
+        return value
+    import torch
+    import torch.distributed as dist
+
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([value], device=dev, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def load_window(step, stream, seconds: float = 0.2) -> None:
     """Run `step` untimed until about `seconds` of GPU work has passed (clock samples under load)."""
     t0 = time.perf_counter()
@@ -320,10 +342,7 @@ def measure_gpu(args, rank: int, world: int) -> dict:
         dist.barrier()
     step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
     total_ms = sum(step_ms)
-    if world > 1:
-        t = torch.tensor([total_ms], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(total_ms, world)
     pairs_per_s = world * args.steps / (total_ms / 1e3)
 
     # ---- per-kernel times (stage events on the launching stream) ------------------------------
@@ -599,7 +618,7 @@ def measure_batch_workload(args, rank: int, world: int) -> dict:
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(dev)
     specs_all = batch_specs(args.workload)
-    mine = list(range(rank, len(specs_all), world))
+    mine = shard(len(specs_all), rank, world)
     idxs, hosts, geo = [], [], []
     for j in mine:
         n, radius, r2c = specs_all[j]
@@ -650,10 +669,7 @@ def measure_batch_workload(args, rank: int, world: int) -> dict:
     if world > 1:
         dist.barrier()
     total_ms = sum(a.elapsed_time(b) for a, b in zip(starts, ends))
-    if world > 1:
-        t = torch.tensor([total_ms], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(total_ms, world)
     value = len(specs_all) * args.steps / (total_ms / 1e3)
 
     # per-pass roofline (groups run pass by pass for the events)
