@@ -294,7 +294,11 @@ def measure_gpu(args, rank: int, world: int) -> dict:
     rt = torch.float64 if dtype == "float64" else torch.float32
     tsize = 8 if dtype == "float64" else 4
 
+    sp.Transform(1, sp.SPFFT_PU_GPU, ttype, n, n, n, npts, sp.SPFFT_INDEX_TRIPLETS, idx, dtype=dtype)  # warm
+    torch.cuda.synchronize()
+    t_plan = time.perf_counter()
     tr = sp.Transform(1, sp.SPFFT_PU_GPU, ttype, n, n, n, npts, sp.SPFFT_INDEX_TRIPLETS, idx, dtype=dtype)
+    plan_ms = (time.perf_counter() - t_plan) * 1e3
     vals_h = make_values(idx, r2c)
     values = torch.from_numpy(vals_h).to(ct).cuda()
     out_vals = torch.empty_like(values)
@@ -437,7 +441,7 @@ def measure_gpu(args, rank: int, world: int) -> dict:
         "clocks": clocks.summary(), "roofline": roofline, "e2e": e2e,
         "pair_gbs": pair_gbs, "roundtrip_rel_l2": err, "cufft_dense": cufft,
         "launches_per_step": 6 if tr.path_info()["split_plane"] else 4, "npts": npts, "nsticks": nsticks,
-        "ncols": ncols, "tuning": tuned or tr.tuning(),
+        "ncols": ncols, "tuning": tuned or tr.tuning(), "plan_ms": plan_ms,
     }
 
 
@@ -887,6 +891,7 @@ def main() -> int:
         "gpu_launches": res["launches_per_step"] * args.steps,
         "roundtrip_rel_l2": res["roundtrip_rel_l2"], "tuning": res["tuning"],
         "cufft_dense_comparison": res["cufft_dense"],
+        "transform_creation_ms": round(res["plan_ms"], 2),
     }
     if res["batched"]:
         line["fp32_batched"] = res["batched"]

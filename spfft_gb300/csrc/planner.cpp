@@ -62,24 +62,42 @@ IndexPlan make_index_plan(SpfftTransformType type, int dimX, int dimY, int dimZ,
   }
 
   // Unique stick keys x*dimY + y in ascending order; a stick's index is its rank in that order
-  // (indices.hpp:151-165). A sort + unique gives the same order as the reference's ordered map.
+  // (indices.hpp:151-165). Keys are bounded by dimX * dimY, so a presence table gives the same
+  // order as the reference's ordered map in O(values + keys); very large xy planes fall back to a
+  // sort + unique.
   std::vector<int> keyOfValue(numValues);
   for (int i = 0; i < numValues; ++i) {
     keyOfValue[i] = storage_index(dimX, triplets[3 * i]) * dimY +
                     storage_index(dimY, triplets[3 * i + 1]);
   }
-  p.stickKeys = keyOfValue;
-  std::sort(p.stickKeys.begin(), p.stickKeys.end());
-  p.stickKeys.erase(std::unique(p.stickKeys.begin(), p.stickKeys.end()), p.stickKeys.end());
+  const long long keyRange = static_cast<long long>(dimX) * dimY;
+  constexpr long long kTableLimit = 1LL << 24;
+  std::vector<int> rankOfKey;  // key -> stick index (-1: no stick), when the table is used
+  if (keyRange <= kTableLimit) {
+    rankOfKey.assign(static_cast<size_t>(keyRange), -1);
+    for (int key : keyOfValue) rankOfKey[key] = 0;
+    int rank = 0;
+    for (long long key = 0; key < keyRange; ++key) {
+      if (rankOfKey[key] == 0) {
+        rankOfKey[key] = rank++;
+        p.stickKeys.push_back(static_cast<int>(key));
+      }
+    }
+  } else {
+    p.stickKeys = keyOfValue;
+    std::sort(p.stickKeys.begin(), p.stickKeys.end());
+    p.stickKeys.erase(std::unique(p.stickKeys.begin(), p.stickKeys.end()), p.stickKeys.end());
+  }
   const int numSticks = static_cast<int>(p.stickKeys.size());
   if (static_cast<long long>(numSticks) * dimZ > INT_MAX) throw OverflowError();
 
   // Value index = stickIndex * dimZ + zStorage (indices.hpp:167-176).
   p.valueIndices.resize(numValues);
   for (int i = 0; i < numValues; ++i) {
-    const int stick = static_cast<int>(
-        std::lower_bound(p.stickKeys.begin(), p.stickKeys.end(), keyOfValue[i]) -
-        p.stickKeys.begin());
+    const int stick = !rankOfKey.empty()
+                          ? rankOfKey[keyOfValue[i]]
+                          : static_cast<int>(std::lower_bound(p.stickKeys.begin(), p.stickKeys.end(),
+                                                              keyOfValue[i]) - p.stickKeys.begin());
     p.valueIndices[i] = stick * dimZ + storage_index(dimZ, triplets[3 * i + 2]);
   }
 
@@ -105,11 +123,20 @@ IndexPlan make_index_plan(SpfftTransformType type, int dimX, int dimY, int dimZ,
   }
   p.columnStickStart.push_back(numSticks);
 
-  // Values grouped by stick and ordered by position; a stable sort keeps duplicates in user order.
+  // Values grouped by stick and ordered by position; duplicates keep user order (a counting sort
+  // over the value positions, or a stable sort when the position range is very large).
   std::vector<int> order(numValues);
-  std::iota(order.begin(), order.end(), 0);
-  std::stable_sort(order.begin(), order.end(),
-                   [&](int a, int b) { return p.valueIndices[a] < p.valueIndices[b]; });
+  const long long posRange = static_cast<long long>(numSticks) * dimZ;
+  if (posRange <= kTableLimit) {
+    std::vector<int> start(static_cast<size_t>(posRange) + 1, 0);
+    for (int i = 0; i < numValues; ++i) ++start[p.valueIndices[i] + 1];
+    for (long long q = 0; q < posRange; ++q) start[q + 1] += start[q];
+    for (int i = 0; i < numValues; ++i) order[start[p.valueIndices[i]]++] = i;
+  } else {
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int a, int b) { return p.valueIndices[a] < p.valueIndices[b]; });
+  }
   p.entryPos.resize(numValues);
   p.entryUser.resize(numValues);
   p.identityOrder = true;
