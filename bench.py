@@ -403,8 +403,9 @@ def measure_gpu(args, rank: int, world: int) -> dict:
            "h2d_bytes_per_step": int(hv.numel() * hv.element_size() + hspace.numel() * hspace.element_size()),
            "d2h_bytes_per_step": int(hspace.numel() * hspace.element_size() + hout.numel() * hout.element_size()),
            "host_access": os.environ.get("SPFFT_GB300_HOST_ACCESS", "direct"),
-           "host_path": "forward input: plane-chunk copies overlapped with the x pass; backward output: "
-                        "written by the x pass over the host link (copy mode: chunk copies both ways)",
+           "host_path": "space domain in host memory: plane-chunk copies overlapped with the chunks' y and x "
+                        "passes in both directions; values read / written by the z pass over the host link "
+                        "(copy mode: staged value copies)",
            "buffers": "pinned host (torch pin_memory), synchronous calls"}
     # the same pair with the reference's staged copies, for comparison
     if os.environ.get("SPFFT_GB300_HOST_ACCESS", "direct") != "copy":

@@ -492,6 +492,8 @@ bool GpuPlan<T>::forward_staged(const T* hostSpace, T* devSpace, T* values, bool
   a.stream = stream;
   a.param = splitRpb_;
   a.in = devSpace;
+  // each chunk's x and y passes run while the next chunk is copied (the y-FFT of plane z needs
+  // only plane z)
   for (int c = 0, z0 = 0; z0 < nz; ++c, z0 += per) {
     const int cnt = std::min(per, nz - z0);
     check_cuda(cudaMemcpyAsync(devSpace + z0 * plane, hostSpace + z0 * plane, cnt * plane * sizeof(T),
@@ -500,14 +502,15 @@ bool GpuPlan<T>::forward_staged(const T* hostSpace, T* devSpace, T* values, bool
     check_cuda(cudaStreamWaitEvent(stream, events[c], 0));
     a.zBegin = z0;
     a.zCount = cnt;
+    a.param = splitRpb_;
     fast_dispatch<T>(FastOp::XForward, base_.dimX, base_.r2c != 0, a);
+    check_launch(cudaGetLastError());
+    a.param = splitCpb_;
+    fast_dispatch<T>(FastOp::YForward, base_.dimY, base_.r2c != 0, a);
     check_launch(cudaGetLastError());
   }
   a.zBegin = 0;
   a.zCount = -1;
-  a.param = splitCpb_;
-  fast_dispatch<T>(FastOp::YForward, base_.dimY, base_.r2c != 0, a);
-  check_launch(cudaGetLastError());
   const T scale = scaled ? scale_ : T(0);
   if (fastZ_) {
     a.param = fastSpb_;
@@ -539,17 +542,18 @@ bool GpuPlan<T>::backward_staged(const T* values, T* devSpace, T* hostSpace, voi
     check_launch(launch_generic<T>(GenericPass::ZBackward, v, config_, values, nullptr, T(0), stream));
   }
   check_launch(cudaGetLastError());
-  a.param = splitCpb_;
-  fast_dispatch<T>(FastOp::YBackward, base_.dimY, base_.r2c != 0, a);
-  check_launch(cudaGetLastError());
   const size_t plane = static_cast<size_t>(base_.dimX) * base_.dimY * (base_.r2c ? 1 : 2);
   const int nz = base_.dimZ, per = (nz + kStagedChunks - 1) / kStagedChunks;
-  a.param = splitRpb_;
   a.out = devSpace;
+  // each chunk's y and x passes, then its copy back, which overlaps the next chunk's passes
   for (int c = 0, z0 = 0; z0 < nz; ++c, z0 += per) {
     const int cnt = std::min(per, nz - z0);
     a.zBegin = z0;
     a.zCount = cnt;
+    a.param = splitCpb_;
+    fast_dispatch<T>(FastOp::YBackward, base_.dimY, base_.r2c != 0, a);
+    check_launch(cudaGetLastError());
+    a.param = splitRpb_;
     fast_dispatch<T>(FastOp::XBackward, base_.dimX, base_.r2c != 0, a);
     check_launch(cudaGetLastError());
     check_cuda(cudaEventRecord(events[c], stream));

@@ -168,15 +168,9 @@ void TransformInternal<T>::backward_enqueue(const T* input, T* output) {
   cudaStream_t s = begin();
   auto in = gb300::split_pointer(input);
   auto out = gb300::split_pointer(output);
-  if (directHost_) {
-    // pinned host buffers: let the kernels read / write them over the coherent host link (the x
-    // pass writes the space domain at about the link's rate)
-    if (in.first) {
-      if (const T* d = gb300::mapped_host_alias(in.first)) in = {nullptr, d};
-    }
-    if (out.first) {
-      if (T* d = gb300::mapped_host_alias(out.first)) out = {nullptr, d};
-    }
+  // pinned host values: the z pass reads them over the coherent host link
+  if (directHost_ && in.first) {
+    if (const T* d = gb300::mapped_host_alias(in.first)) in = {nullptr, d};
   }
   void* scratch = grid_->scratch();
   const T* values = in.second;
@@ -188,12 +182,17 @@ void TransformInternal<T>::backward_enqueue(const T* input, T* output) {
     }
     values = staging;
   }
-  T* space = out.second ? out.second : grid_->space_device();
-  // host output: copies of plane chunks overlap the x pass of the next chunks
-  if (out.first &&
-      gpu_->backward_staged(values, space, out.first, scratch, s, copy_stream().get(), staged_events())) {
+  // host space domain: the y and x passes run in plane chunks into the grid's device buffer and
+  // each chunk is copied back while the next one is transformed
+  if (out.first && gpu_->backward_staged(values, grid_->space_device(), out.first, scratch, s,
+                                         copy_stream().get(), staged_events())) {
     return;
   }
+  // otherwise (no split passes) pinned memory is written by the x pass directly
+  if (directHost_ && out.first) {
+    if (T* d = gb300::mapped_host_alias(out.first)) out = {nullptr, d};
+  }
+  T* space = out.second ? out.second : grid_->space_device();
   gpu_->backward(values, space, scratch, s);
   if (out.first) {
     check_cuda(cudaMemcpyAsync(out.first, space, sizeof(T) * space_elements(),

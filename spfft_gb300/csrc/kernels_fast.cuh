@@ -833,9 +833,10 @@ __device__ __forceinline__ void y_backward_body(const PlanView<S>& p, int cpb, i
 }
 
 template <typename S, typename A, int NY>
-__global__ void __launch_bounds__(kThreads, YMinBlocks<A>::value) y_backward_split(const PlanView<S> p, int cpb) {
+__global__ void __launch_bounds__(kThreads, YMinBlocks<A>::value) y_backward_split(const PlanView<S> p, int cpb,
+                                                                                     int z0) {
   __shared__ int sExp;
-  y_backward_body<S, A, NY>(p, cpb, blockIdx.x, blockIdx.y, &sExp);
+  y_backward_body<S, A, NY>(p, cpb, blockIdx.x, z0 + blockIdx.y, &sExp);
 }
 
 // y forward: block (column group, z)
@@ -896,9 +897,10 @@ __device__ __forceinline__ void y_forward_body(const PlanView<S>& p, int cpb, in
 }
 
 template <typename S, typename A, int NY>
-__global__ void __launch_bounds__(kThreads, YMinBlocks<A>::value) y_forward_split(const PlanView<S> p, int cpb) {
+__global__ void __launch_bounds__(kThreads, YMinBlocks<A>::value) y_forward_split(const PlanView<S> p, int cpb,
+                                                                                    int z0) {
   __shared__ int sExp;
-  y_forward_body<S, A, NY>(p, cpb, blockIdx.x, blockIdx.y, &sExp);
+  y_forward_body<S, A, NY>(p, cpb, blockIdx.x, z0 + blockIdx.y, &sExp);
 }
 
 // Shared memory of the x kernels: twx[NX] | (R2C) twm[M] | colOf[NXF] | P[rows][numColumns] |
@@ -1114,13 +1116,14 @@ struct YSplitKernels {
     cudaError_t e2 = allow_dynamic_smem(y_forward_split<S, A, NY>, maxSmem);
     return e1 != cudaSuccess ? e1 : e2;
   }
-  static void backward(const PlanView<S>& p, int cpb, cudaStream_t st) {
-    const dim3 g((p.numColumns + cpb - 1) / cpb, p.dimZ);
-    launch_pdl(y_backward_split<S, A, NY>, g, kThreads, smem(cpb), st, p, cpb);
+  // planes [z0, z0 + nz) (nz < 0: all planes from z0)
+  static void backward(const PlanView<S>& p, int cpb, cudaStream_t st, int z0, int nz) {
+    const dim3 g((p.numColumns + cpb - 1) / cpb, nz < 0 ? p.dimZ - z0 : nz);
+    launch_pdl(y_backward_split<S, A, NY>, g, kThreads, smem(cpb), st, p, cpb, z0);
   }
-  static void forward(const PlanView<S>& p, int cpb, cudaStream_t st) {
-    const dim3 g((p.numColumns + cpb - 1) / cpb, p.dimZ);
-    launch_pdl(y_forward_split<S, A, NY>, g, kThreads, smem(cpb), st, p, cpb);
+  static void forward(const PlanView<S>& p, int cpb, cudaStream_t st, int z0, int nz) {
+    const dim3 g((p.numColumns + cpb - 1) / cpb, nz < 0 ? p.dimZ - z0 : nz);
+    launch_pdl(y_forward_split<S, A, NY>, g, kThreads, smem(cpb), st, p, cpb, z0);
   }
 };
 

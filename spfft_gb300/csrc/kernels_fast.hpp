@@ -43,7 +43,7 @@ struct FastArgs {
   const PlanView<T>* plan = nullptr;
   int param = 0;  // sticks per block (z) or rows per chunk (plane)
   int param2 = 0;  // batched plane forward: rows of the chunk buffer (2 * param double-buffers)
-  int zBegin = 0, zCount = -1;  // split x passes: plane range (zCount < 0: to the last plane)
+  int zBegin = 0, zCount = -1;  // split y and x passes: plane range (zCount < 0: to the last plane)
   const T* in = nullptr;
   T* out = nullptr;
   T scale = T(0);
