@@ -110,8 +110,10 @@ GpuPlan<T>::GpuPlan(const IndexPlan& p, int device) {
   // Scratch: sticks, then compact planes, then the value staging area.
   layout_.sticksOffset = 0;
   layout_.planesOffset = align_up(static_cast<size_t>(ns) * p.dimZ * c);
+  layout_.expOffset = layout_.planesOffset + align_up(static_cast<size_t>(p.dimZ) * p.dimY * ncol * c);
+  // per-plane column or row exponents of the double-float compact planes
   layout_.valuesOffset =
-      layout_.planesOffset + align_up(static_cast<size_t>(p.dimZ) * p.dimY * ncol * c);
+      layout_.expOffset + align_up(static_cast<size_t>(p.dimZ) * std::max(ncol, p.dimY) * sizeof(int));
   layout_.total = layout_.valuesOffset + align_up(static_cast<size_t>(nv) * c);
 
   // One allocation for every table: twiddles (T) then int arrays.
@@ -337,6 +339,8 @@ PlanView<T> GpuPlan<T>::view(void* scratch) const {
   char* s = static_cast<char*>(scratch);
   v.sticks = reinterpret_cast<T*>(s + layout_.sticksOffset);
   v.planes = reinterpret_cast<T*>(s + layout_.planesOffset);
+  v.planeExp = reinterpret_cast<int*>(s + layout_.expOffset);
+  v.planesRaw = sizeof(T) == sizeof(double) ? 1 : 0;
   return v;
 }
 

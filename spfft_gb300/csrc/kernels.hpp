@@ -37,6 +37,11 @@ struct PlanView {
   const unsigned char* hermitianWeight;  // R2C: per user value, 1 or 2; null for C2C
   T* sticks;
   T* planes;
+  // Double precision: the split y and x kernels keep the compact planes in double-float form
+  // (hi, lo floats in the 16 bytes of a complex double, scaled by a power of two per column or
+  // per row) instead of converting them to binary64 and back; planeExp holds those exponents.
+  int* planeExp;
+  int planesRaw;
 };
 
 // Device tables of one shape group of a batch for one pass (all device pointers); read by the

@@ -110,6 +110,19 @@ __device__ __forceinline__ int max_exponent(double2 v) {
 // Zero, subnormal-only and non-finite blocks use k = 0.
 __device__ __forceinline__ int block_scale(int e) { return (e == 0 || e == 2047) ? 0 : 1023 - e; }
 
+// Double-float compact planes (PlanView::planesRaw): each producing block stores its scaled values
+// as they are and records its scale exponent k per column (y pass) or per row (x forward); a
+// block of zeros records kZeroExp, which never wins the minimum. A consumer takes the smallest
+// exponent of its inputs (the largest magnitude) as its own scale and multiplies every other input
+// by 2^(k - k_input) <= 1, exactly (or to zero far below the block maximum).
+constexpr int kZeroExp = 1 << 20;
+__device__ __forceinline__ int produced_exp(int maxExponentField, int k) { return maxExponentField == 0 ? kZeroExp : k; }
+__device__ __forceinline__ float2 scale_pow2(float2 v, int) { return v; }
+__device__ __forceinline__ ddc scale_pow2(ddc v, int d) {
+  const float f = d < -126 ? 0.0f : __uint_as_float(static_cast<unsigned>(d + 127) << 23);
+  return make_c(dd(v.x.hi * f, v.x.lo * f), dd(v.y.hi * f, v.y.lo * f));
+}
+
 // Programmatic dependent launch (sm_90+): kernels of the same transform are launched so that the
 // next kernel's blocks may start while the previous kernel finishes. Each kernel loads only its
 // constant plan tables (twiddles, index maps) before pdl_wait(), which returns once the previous
@@ -366,12 +379,12 @@ struct PlaneLayout {
     b += 2 * static_cast<size_t>(rows) * WP * c;
     return b;
   }
-  // colOf[NXF] (int, padded to 16 bytes) then colInfo[NXF] (int4). The tables start on a 16-byte
+  // colOf[NXF] (int, padded to 16 bytes), colInfo[NXF] (int4), colExp[NXF] (int, padded). The tables start on a 16-byte
   // boundary (the twiddle tables before them are padded to one), so colInfo and the buffers after
   // it are 16-byte aligned for every length (20 * N bytes of FP32 twiddles are not, for N = 90).
   __host__ __device__ static constexpr size_t round16(size_t b) { return (b + 15) / 16 * 16; }
   __host__ __device__ static constexpr size_t col_table_bytes() {
-    return round16(NXF * sizeof(int)) + NXF * 16;
+    return round16(NXF * sizeof(int)) + NXF * 16 + round16(NXF * sizeof(int));
   }
   // R2C forward: W slots of Z[k] and Z[M-k] for the output column with x = k, and k itself
   __host__ __device__ static int4 col_info(int kk) {
@@ -823,13 +836,21 @@ __device__ __forceinline__ void y_backward_body(const PlanView<S>& p, int cpb, i
   }
   __syncthreads();
   CS* planes = reinterpret_cast<CS*>(p.planes) + static_cast<size_t>(z) * NY * nc + c0;
+  const bool raw = TT::kScaled && p.planesRaw;
   for (int i = threadIdx.x; i < ncb * Ay; i += blockDim.x) {
     const int k1 = dncb.div(i), c = i - k1 * ncb;
     CA v[By];
     fft_pass2<NY, +1>(buf + c, ncb, k1, v);
+    if (raw) {
+      CA* rp = reinterpret_cast<CA*>(planes);
 #pragma unroll
-    for (int k2 = 0; k2 < By; ++k2) planes[static_cast<size_t>(k1 + Ay * k2) * nc + c] = to_storage(v[k2], k);
+      for (int k2 = 0; k2 < By; ++k2) rp[static_cast<size_t>(k1 + Ay * k2) * nc + c] = v[k2];
+    } else {
+#pragma unroll
+      for (int k2 = 0; k2 < By; ++k2) planes[static_cast<size_t>(k1 + Ay * k2) * nc + c] = to_storage(v[k2], k);
+    }
   }
+  if (raw && threadIdx.x < ncb) p.planeExp[z * nc + c0 + threadIdx.x] = produced_exp(sExp, k);
 }
 
 template <typename S, typename A, int NY>
@@ -861,9 +882,31 @@ __device__ __forceinline__ void y_forward_body(const PlanView<S>& p, int cpb, in
     cp_async_c(buf + i, planes + static_cast<size_t>(y) * nc + c);
   }
   cp_async_commit();
-  cp_async_wait<0>();
-  __syncthreads();
-  const int k = convert_block<S, A>(buf, NY * ncb, &sExp);
+  int k = 0;
+  if (TT::kScaled && p.planesRaw) {
+    // double-float rows from the x pass: scale of the block = smallest row exponent
+    int* rowExp = reinterpret_cast<int*>(buf + NY * cpb);
+    if (threadIdx.x == 0) sExp = kZeroExp;
+    __syncthreads();
+    int e = kZeroExp;
+    for (int y = threadIdx.x; y < NY; y += blockDim.x) {
+      rowExp[y] = p.planeExp[z * NY + y];
+      e = min(e, rowExp[y]);
+    }
+    atomicMin(&sExp, e);
+    cp_async_wait<0>();
+    __syncthreads();
+    k = sExp == kZeroExp ? 0 : sExp;
+    for (int i = threadIdx.x; i < NY * ncb; i += blockDim.x) {
+      const int y = dncb.div(i);
+      buf[i] = scale_pow2(buf[i], k - rowExp[y]);
+    }
+    __syncthreads();
+  } else {
+    cp_async_wait<0>();
+    __syncthreads();
+    k = convert_block<S, A>(buf, NY * ncb, &sExp);
+  }
   for (int i = threadIdx.x; i < ncb * By; i += blockDim.x) {
     const int b = dncb.div(i), c = i - b * ncb;
     fft_pass1<NY, -1>(buf + c, ncb, b, tw);
@@ -912,6 +955,7 @@ struct RowSmem {
   CA* twm;
   int* colOf;
   int4* colInfo;
+  int* colExp;
   CA* P;
   CA* W;
   // withP = false: no compact-row buffer (the R2C forward stores its output columns straight to
@@ -921,6 +965,7 @@ struct RowSmem {
     twm = twx + NX;
     colOf = reinterpret_cast<int*>(g_fast_smem + L::round16((NX + (R2C ? L::M : 0)) * sizeof(CA)));
     colInfo = reinterpret_cast<int4*>(reinterpret_cast<unsigned char*>(colOf) + L::round16(L::NXF * sizeof(int)));
+    colExp = reinterpret_cast<int*>(colInfo + L::NXF);
     P = reinterpret_cast<CA*>(reinterpret_cast<unsigned char*>(colOf) + L::col_table_bytes());
     W = P + (withP ? rows * numColumns : 0);
   }
@@ -969,9 +1014,31 @@ __device__ __forceinline__ void x_backward_body(const PlanView<S>& p, S* __restr
   const CS* planes = reinterpret_cast<const CS*>(p.planes) + (static_cast<size_t>(z) * ny + y0) * nc;
   for (int i = threadIdx.x; i < nr * nc; i += blockDim.x) cp_async_c(s.P + i, planes + i);
   cp_async_commit();
-  cp_async_wait<0>();
-  __syncthreads();
-  const int k = convert_block<S, A>(s.P, nr * nc, &sExp);
+  int k = 0;
+  if (TT::kScaled && p.planesRaw) {
+    // double-float columns from the y pass: scale of the block = smallest column exponent
+    if (threadIdx.x == 0) sExp = kZeroExp;
+    __syncthreads();
+    int e = kZeroExp;
+    for (int c = threadIdx.x; c < nc; c += blockDim.x) {
+      s.colExp[c] = p.planeExp[z * nc + c];
+      e = min(e, s.colExp[c]);
+    }
+    atomicMin(&sExp, e);
+    cp_async_wait<0>();
+    __syncthreads();
+    k = sExp == kZeroExp ? 0 : sExp;
+    const FastDiv dnc(nc);
+    for (int i = threadIdx.x; i < nr * nc; i += blockDim.x) {
+      const int rl = dnc.div(i), c = i - rl * nc;
+      s.P[i] = scale_pow2(s.P[i], k - s.colExp[c]);
+    }
+    __syncthreads();
+  } else {
+    cp_async_wait<0>();
+    __syncthreads();
+    k = convert_block<S, A>(s.P, nr * nc, &sExp);
+  }
   const CA* twl = R2C ? s.twm : s.twx;
   if (R2C) {
     c2r_pack_rows<L>([&](int rl) { return s.P + rl * nc; }, nr, s.W, s.colOf, s.twx);
@@ -1083,6 +1150,8 @@ __device__ __forceinline__ void x_forward_body(const PlanView<S>& p, const S* __
   }
   __syncthreads();
   CS* planes = reinterpret_cast<CS*>(p.planes) + (static_cast<size_t>(z) * ny + y0) * nc;
+  const bool raw = TT::kScaled && p.planesRaw;
+  CA* rawPlanes = reinterpret_cast<CA*>(planes);
   if (R2C) {
     // output columns straight to the compact plane rows (consecutive threads, consecutive columns)
     for (int i = threadIdx.x; i < nr * nc; i += blockDim.x) {
@@ -1093,11 +1162,17 @@ __device__ __forceinline__ void x_forward_body(const PlanView<S>& p, const S* __
       const CA zm = wrow[ci.y];
       const CA dif = make_c(zk.x - zm.x, zk.y + zm.y);
       const CA u = cmul(dif, s.twx[ci.z]);
-      planes[i] = to_storage(make_c(half_of(zk.x + zm.x + u.y), half_of(zk.y - zm.y - u.x)), k);
+      const CA xv = make_c(half_of(zk.x + zm.x + u.y), half_of(zk.y - zm.y - u.x));
+      if (raw) rawPlanes[i] = xv;
+      else planes[i] = to_storage(xv, k);
     }
   } else {
-    for (int i = threadIdx.x; i < nr * nc; i += blockDim.x) planes[i] = to_storage(s.P[i], k);
+    for (int i = threadIdx.x; i < nr * nc; i += blockDim.x) {
+      if (raw) rawPlanes[i] = s.P[i];
+      else planes[i] = to_storage(s.P[i], k);
+    }
   }
+  if (raw && threadIdx.x < nr) p.planeExp[z * ny + y0 + threadIdx.x] = produced_exp(sExp, k);
 }
 
 template <typename S, typename A, int NX, bool R2C>
@@ -1110,7 +1185,8 @@ __global__ void __launch_bounds__(kThreads, YMinBlocks<A>::value) x_forward_spli
 template <typename S, typename A, int NY>
 struct YSplitKernels {
   using CA = typename Types<S, A>::CA;
-  static size_t smem(int cpb) { return (NY + static_cast<size_t>(NY) * cpb) * sizeof(CA); }
+  // twiddles, the column group, and (forward, double-float planes) the row exponents
+  static size_t smem(int cpb) { return (NY + static_cast<size_t>(NY) * cpb) * sizeof(CA) + NY * sizeof(int); }
   static cudaError_t prepare(size_t maxSmem) {
     cudaError_t e1 = allow_dynamic_smem(y_backward_split<S, A, NY>, maxSmem);
     cudaError_t e2 = allow_dynamic_smem(y_forward_split<S, A, NY>, maxSmem);
