@@ -260,7 +260,9 @@ void BatchPlan<T>::upload_views() {
     Group& g = *gp;
     std::vector<PlanView<T>> views;
     for (int t : g.members) {
-      views.push_back(tp_[t]->gpu_plan().device_view(tp_[t]->grid().scratch()));
+      PlanView<T> v = tp_[t]->gpu_plan().device_view(tp_[t]->grid().scratch());
+      v.sticksRaw = 0;  // binary64 sticks: a group may run the fused plane kernel
+      views.push_back(v);
     }
     check_cuda(cudaMemcpy(static_cast<char*>(g.dev.get()) + g.offViews, views.data(),
                           views.size() * sizeof(PlanView<T>), cudaMemcpyHostToDevice));

@@ -112,8 +112,10 @@ GpuPlan<T>::GpuPlan(const IndexPlan& p, int device) {
   layout_.planesOffset = align_up(static_cast<size_t>(ns) * p.dimZ * c);
   layout_.expOffset = layout_.planesOffset + align_up(static_cast<size_t>(p.dimZ) * p.dimY * ncol * c);
   // per-plane column or row exponents of the double-float compact planes
-  layout_.valuesOffset =
+  layout_.stickExpOffset =
       layout_.expOffset + align_up(static_cast<size_t>(p.dimZ) * std::max(ncol, p.dimY) * sizeof(int));
+  layout_.valuesOffset =
+      layout_.stickExpOffset + align_up(std::max(static_cast<size_t>(ns), static_cast<size_t>(p.dimZ) * ncol) * sizeof(int));
   layout_.total = layout_.valuesOffset + align_up(static_cast<size_t>(nv) * c);
 
   // One allocation for every table: twiddles (T) then int arrays.
@@ -341,6 +343,8 @@ PlanView<T> GpuPlan<T>::view(void* scratch) const {
   v.planes = reinterpret_cast<T*>(s + layout_.planesOffset);
   v.planeExp = reinterpret_cast<int*>(s + layout_.expOffset);
   v.planesRaw = sizeof(T) == sizeof(double) ? 1 : 0;
+  v.stickExp = reinterpret_cast<int*>(s + layout_.stickExpOffset);
+  v.sticksRaw = (sizeof(T) == sizeof(double) && fastZ_ && planePath_ == PlanePath::Split) ? 1 : 0;
   return v;
 }
 
@@ -369,7 +373,10 @@ void GpuPlan<T>::backward(const T* values, T* space, void* scratch, cudaStream_t
                           const StageEvents* events) const {
   bool aligned = true;
   check_alignment(values, space, &aligned);
-  const PlanView<T> v = view(scratch);
+  PlanView<T> v = view(scratch);
+  // double-float sticks only between the fast z and the split y kernels (an unaligned R2C space
+  // buffer sends this call through the generic plane passes, which exchange binary64 sticks)
+  if (!(planePath_ == PlanePath::Split && aligned)) v.sticksRaw = 0;
   FastArgs<T> a;
   a.plan = &v;
   a.stream = stream;
@@ -439,7 +446,10 @@ void GpuPlan<T>::forward(const T* space, T* values, bool scaled, void* scratch,
                          cudaStream_t stream, const StageEvents* events) const {
   bool aligned = true;
   check_alignment(values, space, &aligned);
-  const PlanView<T> v = view(scratch);
+  PlanView<T> v = view(scratch);
+  // double-float sticks only between the fast z and the split y kernels (an unaligned R2C space
+  // buffer sends this call through the generic plane passes, which exchange binary64 sticks)
+  if (!(planePath_ == PlanePath::Split && aligned)) v.sticksRaw = 0;
   FastArgs<T> a;
   a.plan = &v;
   a.stream = stream;

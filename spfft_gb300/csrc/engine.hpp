@@ -19,7 +19,7 @@ namespace gb300 {
 
 // Bytes of scratch one transform needs, and where each part starts inside it.
 struct ScratchLayout {
-  size_t sticksOffset = 0, planesOffset = 0, expOffset = 0, valuesOffset = 0, total = 0;
+  size_t sticksOffset = 0, planesOffset = 0, expOffset = 0, stickExpOffset = 0, valuesOffset = 0, total = 0;
 };
 
 template <typename T>

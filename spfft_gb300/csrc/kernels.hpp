@@ -42,6 +42,11 @@ struct PlanView {
   // per row) instead of converting them to binary64 and back; planeExp holds those exponents.
   int* planeExp;
   int planesRaw;
+  // The same for the sticks between the z and the split y kernels (single transforms on the
+  // split path): per-stick exponents from the z pass (backward), per-(plane, column) exponents
+  // from the y pass (forward).
+  int* stickExp;
+  int sticksRaw;
 };
 
 // Device tables of one shape group of a batch for one pass (all device pointers); read by the

@@ -268,15 +268,23 @@ __device__ __forceinline__ void z_backward_body(const PlanView<S>& p, const S* _
   }
   __syncthreads();
   CS* sticks = reinterpret_cast<CS*>(p.sticks) + s0;
+  const bool raw = TT::kScaled && p.sticksRaw;
   for (int i = threadIdx.x; i < nsb * Az; i += blockDim.x) {
     const int k1 = dns.div(i), sl = i - k1 * nsb;
     CA v[Bz];
     fft_pass2<NZ, +1>(buf + sl * PZ, 1, k1, v);
+    if (raw) {
+      CA* rs = reinterpret_cast<CA*>(sticks);
 #pragma unroll
-    for (int k2 = 0; k2 < Bz; ++k2) {
-      sticks[static_cast<size_t>(k1 + Az * k2) * p.numSticks + sl] = to_storage(v[k2], k);
+      for (int k2 = 0; k2 < Bz; ++k2) rs[static_cast<size_t>(k1 + Az * k2) * p.numSticks + sl] = v[k2];
+    } else {
+#pragma unroll
+      for (int k2 = 0; k2 < Bz; ++k2) {
+        sticks[static_cast<size_t>(k1 + Az * k2) * p.numSticks + sl] = to_storage(v[k2], k);
+      }
     }
   }
+  if (raw && threadIdx.x < nsb) p.stickExp[s0 + threadIdx.x] = produced_exp(sExp, k);
 }
 
 template <typename S, typename A, int NZ>
@@ -313,9 +321,33 @@ __device__ __forceinline__ void z_forward_body(const PlanView<S>& p, S* __restri
     if (PZ > NZ) buf[i * PZ + NZ] = czero<A>();
   }
   cp_async_commit();
-  cp_async_wait<0>();
-  __syncthreads();
-  const int k = convert_block<S, A>(buf, nsb * PZ, &sExp);
+  int k = 0;
+  if (TT::kScaled && p.sticksRaw) {
+    // double-float sticks from the y pass, one exponent per (plane, column): block scale = the
+    // smallest of them, every value brought to it
+    if (threadIdx.x == 0) sExp = kZeroExp;
+    __syncthreads();
+    const int nc = p.numColumns;
+    int e = kZeroExp;
+    for (int i = threadIdx.x; i < NZ * nsb; i += blockDim.x) {
+      const int z = dns.div(i), sl = i - z * nsb;
+      e = min(e, p.stickExp[z * nc + p.stickColumn[s0 + sl]]);
+    }
+    atomicMin(&sExp, e);
+    cp_async_wait<0>();
+    __syncthreads();
+    k = sExp == kZeroExp ? 0 : sExp;
+    for (int i = threadIdx.x; i < NZ * nsb; i += blockDim.x) {
+      const int z = dns.div(i), sl = i - z * nsb;
+      CA& v = buf[sl * PZ + z];
+      v = scale_pow2(v, k - p.stickExp[z * nc + p.stickColumn[s0 + sl]]);
+    }
+    __syncthreads();
+  } else {
+    cp_async_wait<0>();
+    __syncthreads();
+    k = convert_block<S, A>(buf, nsb * PZ, &sExp);
+  }
   for (int i = threadIdx.x; i < nsb * Bz; i += blockDim.x) {
     const int sl = i / Bz, b = i - sl * Bz;
     fft_pass1<NZ, -1>(buf + sl * PZ, 1, b, tw);
@@ -810,25 +842,58 @@ __device__ __forceinline__ void y_backward_body(const PlanView<S>& p, int cpb, i
   pdl_trigger();
   const CS* sticks = reinterpret_cast<const CS*>(p.sticks) + static_cast<size_t>(z) * p.numSticks;
   const int sBegin = p.columnStickStart[c0], sEnd = p.columnStickStart[c0 + ncb];
-  for (int st0 = sBegin + threadIdx.x; st0 < sEnd; st0 += 4 * blockDim.x) {
-    int pos[4];
+  int k = 0;
+  if (TT::kScaled && p.sticksRaw) {
+    // double-float sticks from the z pass: block scale = smallest stick exponent; each value is
+    // brought to it as it is gathered
+    if (threadIdx.x == 0) sExp = kZeroExp;
+    __syncthreads();
+    int e = kZeroExp;
+    for (int st = sBegin + threadIdx.x; st < sEnd; st += blockDim.x) e = min(e, p.stickExp[st]);
+    atomicMin(&sExp, e);
+    __syncthreads();
+    k = sExp == kZeroExp ? 0 : sExp;
+    const CA* rs = reinterpret_cast<const CA*>(sticks);
+    for (int st0 = sBegin + threadIdx.x; st0 < sEnd; st0 += 4 * blockDim.x) {
+      int pos[4], ex[4];
+      CA val[4];
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      const int st = st0 + u * blockDim.x;
-      pos[u] = st < sEnd ? __ldg(p.stickPlanePos + st) : -1;
-    }
+      for (int u = 0; u < 4; ++u) {
+        const int st = st0 + u * blockDim.x;
+        pos[u] = st < sEnd ? __ldg(p.stickPlanePos + st) : -1;
+        ex[u] = st < sEnd ? p.stickExp[st] : 0;
+        if (st < sEnd) val[u] = rs[st];
+      }
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      if (pos[u] >= 0) {
-        const int y = dnc.div(pos[u]), c = pos[u] - y * nc;
-        cp_async_c(buf + y * ncb + (c - c0), sticks + st0 + u * blockDim.x);
+      for (int u = 0; u < 4; ++u) {
+        if (pos[u] >= 0) {
+          const int y = dnc.div(pos[u]), c = pos[u] - y * nc;
+          buf[y * ncb + (c - c0)] = scale_pow2(val[u], k - ex[u]);
+        }
       }
     }
+    __syncthreads();
+  } else {
+    for (int st0 = sBegin + threadIdx.x; st0 < sEnd; st0 += 4 * blockDim.x) {
+      int pos[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int st = st0 + u * blockDim.x;
+        pos[u] = st < sEnd ? __ldg(p.stickPlanePos + st) : -1;
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        if (pos[u] >= 0) {
+          const int y = dnc.div(pos[u]), c = pos[u] - y * nc;
+          cp_async_c(buf + y * ncb + (c - c0), sticks + st0 + u * blockDim.x);
+        }
+      }
+    }
+    cp_async_commit();
+    cp_async_wait<0>();
+    __syncthreads();
+    k = convert_block<S, A>(buf, NY * ncb, &sExp);
   }
-  cp_async_commit();
-  cp_async_wait<0>();
-  __syncthreads();
-  const int k = convert_block<S, A>(buf, NY * ncb, &sExp);
   if (p.r2c && c0 == 0 && p.columnX[0] == 0) line_fill(buf, NY, ncb);
   for (int i = threadIdx.x; i < ncb * By; i += blockDim.x) {
     const int b = dncb.div(i), c = i - b * ncb;
@@ -922,6 +987,7 @@ __device__ __forceinline__ void y_forward_body(const PlanView<S>& p, int cpb, in
   __syncthreads();
   CS* sticks = reinterpret_cast<CS*>(p.sticks) + static_cast<size_t>(z) * p.numSticks;
   const int sBegin = p.columnStickStart[c0], sEnd = p.columnStickStart[c0 + ncb];
+  const bool raw = TT::kScaled && p.sticksRaw;
   for (int st0 = sBegin + threadIdx.x; st0 < sEnd; st0 += 4 * blockDim.x) {
     int pos[4];
 #pragma unroll
@@ -933,10 +999,14 @@ __device__ __forceinline__ void y_forward_body(const PlanView<S>& p, int cpb, in
     for (int u = 0; u < 4; ++u) {
       if (pos[u] >= 0) {
         const int y = dnc.div(pos[u]), c = pos[u] - y * nc;
-        sticks[st0 + u * blockDim.x] = to_storage(buf[transposed_pos<NY>(y) * ncb + (c - c0)], k);
+        const CA v = buf[transposed_pos<NY>(y) * ncb + (c - c0)];
+        if (raw) reinterpret_cast<CA*>(sticks)[st0 + u * blockDim.x] = v;
+        else sticks[st0 + u * blockDim.x] = to_storage(v, k);
       }
     }
   }
+  // exponent of this block's sticks of plane z, per column (the z forward reads them per stick)
+  if (raw && threadIdx.x < ncb) p.stickExp[z * nc + c0 + threadIdx.x] = sExp == kZeroExp ? kZeroExp : k;
 }
 
 template <typename S, typename A, int NY>
