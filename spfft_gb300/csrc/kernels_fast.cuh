@@ -833,7 +833,9 @@ __device__ __forceinline__ void y_backward_body(const PlanView<S>& p, int cpb, i
   CA* tw = reinterpret_cast<CA*>(g_fast_smem);
   CA* buf = tw + NY;
   const int nc = p.numColumns;
-  const int c0 = bx * cpb, ncb = min(cpb, nc - c0);
+  // ceil(nc / cpb) column groups of balanced sizes (at most cpb columns each)
+  const int groups = (nc + cpb - 1) / cpb;
+  const int c0 = bx * nc / groups, ncb = (bx + 1) * nc / groups - c0;
   const FastDiv dncb(ncb), dnc(nc);
   load_twiddles<S, A>(tw, p.twy, NY);
   for (int i = threadIdx.x; i < NY * ncb; i += blockDim.x) buf[i] = czero<A>();
@@ -936,7 +938,9 @@ __device__ __forceinline__ void y_forward_body(const PlanView<S>& p, int cpb, in
   CA* tw = reinterpret_cast<CA*>(g_fast_smem);
   CA* buf = tw + NY;
   const int nc = p.numColumns;
-  const int c0 = bx * cpb, ncb = min(cpb, nc - c0);
+  // ceil(nc / cpb) column groups of balanced sizes (at most cpb columns each)
+  const int groups = (nc + cpb - 1) / cpb;
+  const int c0 = bx * nc / groups, ncb = (bx + 1) * nc / groups - c0;
   const FastDiv dncb(ncb), dnc(nc);
   load_twiddles<S, A>(tw, p.twy, NY);
   pdl_wait();
