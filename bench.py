@@ -296,6 +296,12 @@ def measure_gpu(args, rank: int, world: int) -> dict:
 
     sp.Transform(1, sp.SPFFT_PU_GPU, ttype, n, n, n, npts, sp.SPFFT_INDEX_TRIPLETS, idx, dtype=dtype)  # warm
     torch.cuda.synchronize()
+    # creation time with the host planner, then with the default (device) planner
+    os.environ["SPFFT_GB300_PLANNER"] = "host"
+    t_plan = time.perf_counter()
+    sp.Transform(1, sp.SPFFT_PU_GPU, ttype, n, n, n, npts, sp.SPFFT_INDEX_TRIPLETS, idx, dtype=dtype)
+    plan_host_ms = (time.perf_counter() - t_plan) * 1e3
+    del os.environ["SPFFT_GB300_PLANNER"]
     t_plan = time.perf_counter()
     tr = sp.Transform(1, sp.SPFFT_PU_GPU, ttype, n, n, n, npts, sp.SPFFT_INDEX_TRIPLETS, idx, dtype=dtype)
     plan_ms = (time.perf_counter() - t_plan) * 1e3
@@ -443,6 +449,7 @@ def measure_gpu(args, rank: int, world: int) -> dict:
         "pair_gbs": pair_gbs, "roundtrip_rel_l2": err, "cufft_dense": cufft,
         "launches_per_step": 6 if tr.path_info()["split_plane"] else 4, "npts": npts, "nsticks": nsticks,
         "ncols": ncols, "tuning": tuned or tr.tuning(), "plan_ms": plan_ms,
+        "plan_host_ms": plan_host_ms,
     }
 
 
@@ -506,13 +513,17 @@ def measure_batched(args, workload: str, batch: int, dtype: str, radii=None) -> 
     ttype = sp.SPFFT_TRANS_R2C if r2c else sp.SPFFT_TRANS_C2C
     trs, vals, spaces, hosts, idxs = [], [], [], [], []
     cache = {}
+    create_s = 0.0
+    plans_before = sp.plan_cache_size()
     for b in range(batch):
         r = radii[b]
         if r not in cache:
             cache[r] = sphere_indices(n, r, r2c)
         idx = cache[r]
         idxs.append(idx)
+        t0 = time.perf_counter()
         trs.append(sp.Transform(1, sp.SPFFT_PU_GPU, ttype, n, n, n, len(idx), sp.SPFFT_INDEX_TRIPLETS, idx, dtype=dtype))
+        create_s += time.perf_counter() - t0
         v = make_values(idx, r2c, seed=100 + b)
         if not r2c:
             v = v / np.sqrt(len(idx))
@@ -598,7 +609,9 @@ def measure_batched(args, workload: str, batch: int, dtype: str, radii=None) -> 
             "pass_ms": {k: round(v, 4) for k, v in pass_ms.items()}, "pass_gbs": pass_gbs,
             "roofline": batch_roof,
             "hbm_gbs_per_pair_accounting": round(pb["pair"] / (ms / args.steps * 1e-3) / 1e9, 1),
-            "workload": workload, "l2": "batch working set > L2 (no flush)"}
+            "workload": workload, "l2": "batch working set > L2 (no flush)",
+            "creation": {"ms_total": round(create_s * 1e3, 2), "transforms": batch,
+                         "index_plans": sp.plan_cache_size() - plans_before}}
 
 
 def batch_values(idx: np.ndarray, r2c: bool, seed: int) -> np.ndarray:
@@ -648,7 +661,19 @@ def measure_batch_workload(args, rank: int, world: int) -> dict:
 
     stream = torch.cuda.Stream()
     # ---- FP32 batched -------------------------------------------------------------------------
+    # creation of the whole set with the host planner (discarded), then with the default planner
+    os.environ["SPFFT_GB300_PLANNER"] = "host"
+    t0 = time.perf_counter()
+    discard = make("float32")
+    create_host_s = time.perf_counter() - t0
+    del os.environ["SPFFT_GB300_PLANNER"], discard
+    plans_before = sp.plan_cache_size()
+    t0 = time.perf_counter()
     trs32, vals32, spaces32, ct32 = make("float32")
+    create_s = time.perf_counter() - t0
+    creation = {"ms_total": round(create_s * 1e3, 1), "ms_total_host_planner": round(create_host_s * 1e3, 1),
+                "transforms": len(trs32), "index_plans": sp.plan_cache_size() - plans_before,
+                "includes": "index planning, device tables, grid buffers, value and space buffers"}
     bt = sp.Batch(trs32)
     bt.bind(vals32, spaces32)
     if not args.no_autotune:
@@ -778,6 +803,7 @@ def measure_batch_workload(args, rank: int, world: int) -> dict:
     return {"value": value, "ms_per_step": total_ms / args.steps, "clocks": clocks.summary(),
             "roofline": roofline, "e2e": e2e, "pair_bytes": pair_bytes,
             "launches_per_step": info["launches_per_pair"], "groups": info["groups"],
+            "creation": creation,
             "unbatched": info["unbatched"], "fp64_plain": plain,
             "err_backward": max(errs_b), "err_forward": max(errs_f), "sampled": len(sample),
             "err_stats": {"backward_space_rel_l2": {"max": max(errs_b), "median": statistics.median(errs_b)},
@@ -892,7 +918,8 @@ def main() -> int:
         "gpu_launches": res["launches_per_step"] * args.steps,
         "roundtrip_rel_l2": res["roundtrip_rel_l2"], "tuning": res["tuning"],
         "cufft_dense_comparison": res["cufft_dense"],
-        "transform_creation_ms": round(res["plan_ms"], 2),
+        "transform_creation_ms": {"device_planner": round(res["plan_ms"], 2),
+                                  "host_planner": round(res["plan_host_ms"], 2)},
     }
     if res["batched"]:
         line["fp32_batched"] = res["batched"]
@@ -948,6 +975,7 @@ def batch_main(args, rank: int, world: int) -> int:
         "e2e": res["e2e"], "clocks": res["clocks"],
         "gpu_launches": res["launches_per_step"] * args.steps,
         "shape_groups": res["groups"], "unbatched_transforms": res["unbatched"],
+        "transform_creation": res["creation"],
         "fp64_plain": {"value": round(res["fp64_plain"], 2), "unit": UNIT,
                        "ratio_fp32_batched_vs_fp64_plain": round(res["value"] / res["fp64_plain"], 2)},
         "fp32_vs_fp64_errors": res["err_stats"],

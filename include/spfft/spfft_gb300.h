@@ -24,6 +24,27 @@ SPFFT_EXPORT SpfftError spfft_gb300_plan_indices(SpfftTransformType transformTyp
                                                  int* stickKeys, int maxSticks, int* numSticks,
                                                  int* zeroZeroStick);
 
+/* Every table of the index plan a transform of these parameters uses, for verification: from the
+ * host planner (planner 0) or from the device planner on the current device (planner 1; where it
+ * declines -- duplicate triplets, very large key or position ranges -- the host planner runs and
+ * *usedDevice is 0). `tables` receives, back to back: numSticks, numColumns, zeroZeroStick,
+ * identityOrder, valueIndices[numLocalElements], stickKeys[numSticks], stickColumn[numSticks],
+ * stickY[numSticks], stickPlanePos[numSticks], columnX[numColumns],
+ * columnStickStart[numColumns + 1], entryPos[numLocalElements], entryUser[numLocalElements],
+ * stickEntryStart[numSticks + 1] and, for R2C, hermitianWeight[numLocalElements]. *size receives
+ * the number of ints; nothing is written to `tables` when it is NULL or `capacity` is smaller.
+ * Errors are those of transform creation. */
+SPFFT_EXPORT SpfftError spfft_gb300_plan_tables(int planner, SpfftTransformType transformType,
+                                                int dimX, int dimY, int dimZ,
+                                                int numLocalElements, const int* indices,
+                                                int* tables, long long capacity, long long* size,
+                                                int* usedDevice);
+
+/* Number of live index plans that transform creation can share (transforms created with the same
+ * type, sizes and index triplets on the same device share one plan and its device tables;
+ * SPFFT_GB300_PLAN_CACHE=0 turns the sharing off). */
+SPFFT_EXPORT SpfftError spfft_gb300_plan_cache_size(int* count);
+
 /* Attach a CUDA stream (a cudaStream_t passed as void*). Afterwards every call of the transform is
  * enqueued on that stream only: no internal stream and no ordering against the legacy default
  * stream. In SPFFT_EXEC_ASYNCHRONOUS mode calls then return without waiting, which makes them

@@ -138,6 +138,9 @@ def _declare(lib: ctypes.CDLL) -> None:
         getattr(lib, prefix + "transform_stage_times").argtypes = [_vp, _i, _vp, _vp, _i, _vp,
                                                                    ctypes.POINTER(ctypes.c_float)]
     lib.spfft_gb300_plan_indices.argtypes = [_i, _i, _i, _i, _i, _vp, _vp, _vp, _i, _ip, _ip]
+    lib.spfft_gb300_plan_tables.argtypes = [_i, _i, _i, _i, _i, _i, _vp, _vp, ctypes.c_longlong,
+                                            ctypes.POINTER(ctypes.c_longlong), _ip]
+    lib.spfft_gb300_plan_cache_size.argtypes = [_ip]
     lib.spfft_gb300_batch_create.argtypes = [ctypes.POINTER(_vp), _i, ctypes.POINTER(_vp)]
     lib.spfft_gb300_float_batch_create.argtypes = [ctypes.POINTER(_vp), _i, ctypes.POINTER(_vp)]
     lib.spfft_gb300_batch_destroy.argtypes = [_vp]
@@ -207,6 +210,46 @@ def plan_indices(transform_type: int, dim_x: int, dim_y: int, dim_z: int, indice
           int(values.ctypes.data), int(sticks.ctypes.data), int(sticks.size), ctypes.byref(ns),
           ctypes.byref(zz))
     return values[:n].copy(), sticks[: ns.value].copy(), zz.value
+
+
+PLAN_TABLE_FIELDS = ("value_indices", "stick_keys", "stick_column", "stick_y", "stick_plane_pos",
+                     "column_x", "column_stick_start", "entry_pos", "entry_user", "stick_entry_start",
+                     "hermitian_weight")
+
+
+def plan_tables(planner: int, transform_type: int, dim_x: int, dim_y: int, dim_z: int,
+                indices: Any) -> dict:
+    """Every table of the index plan from the host planner (0) or the device planner on the
+    current device (1): a dict of int32 arrays named by PLAN_TABLE_FIELDS plus the scalars
+    num_sticks, num_columns, zero_zero_stick, identity_order and used_device (0 where the device
+    planner declined and the host planner ran)."""
+    import numpy as np
+
+    owner, ptr = _indices_arg(indices)
+    n = 0 if owner is None else owner.size // 3
+    size = ctypes.c_longlong(0)
+    used = ctypes.c_int(0)
+    args = (planner, transform_type, dim_x, dim_y, dim_z, n, ptr or None)
+    _call("spfft_gb300_plan_tables", *args, None, 0, ctypes.byref(size), ctypes.byref(used))
+    buf = np.zeros(max(size.value, 1), dtype=np.int32)
+    _call("spfft_gb300_plan_tables", *args, int(buf.ctypes.data), int(buf.size), ctypes.byref(size),
+          ctypes.byref(used))
+    ns, nc, zz, ident = (int(v) for v in buf[:4])
+    lengths = (n, ns, ns, ns, ns, nc, nc + 1, n, n, ns + 1, n if transform_type == SPFFT_TRANS_R2C else 0)
+    out: dict = {"num_sticks": ns, "num_columns": nc, "zero_zero_stick": zz, "identity_order": ident,
+                 "used_device": used.value}
+    pos = 4
+    for name, length in zip(PLAN_TABLE_FIELDS, lengths):
+        out[name] = buf[pos:pos + length].copy()
+        pos += length
+    return out
+
+
+def plan_cache_size() -> int:
+    """Live index plans that transform creation can share."""
+    v = ctypes.c_int(0)
+    _call("spfft_gb300_plan_cache_size", ctypes.byref(v))
+    return v.value
 
 
 # ---- handles ------------------------------------------------------------------------------------

@@ -1,10 +1,12 @@
 // The C interface: every function converts exceptions into SpfftError codes, like the reference's
 // src/spfft/{grid,transform,multi_transform}{,_float}.cpp C sections (e.g. transform.cpp:179-562).
+#include <algorithm>
 #include <vector>
 
 #include "access.hpp"
 #include "internal.hpp"
 #include "planner.hpp"
+#include "planner_gpu.hpp"
 #include "spfft/spfft.h"
 #include "spfft/spfft.hpp"
 #include "spfft/spfft_gb300.h"
@@ -336,6 +338,60 @@ SpfftError spfft_gb300_plan_indices(SpfftTransformType transformType, int dimX, 
     }
     if (numSticks) *numSticks = plan.num_sticks();
     if (zeroZeroStick) *zeroZeroStick = plan.zeroZeroStick;
+  });
+}
+
+// Every table of the index plan, from the host or the device planner (for verification).
+SpfftError spfft_gb300_plan_tables(int planner, SpfftTransformType transformType, int dimX, int dimY,
+                                   int dimZ, int numLocalElements, const int* indices, int* tables,
+                                   long long capacity, long long* size, int* usedDevice) {
+  return guarded([&] {
+    if (numLocalElements < 0 || (!indices && numLocalElements > 0) || !size) {
+      throw spfft::InvalidParameterError();
+    }
+    if (planner != 0 && planner != 1) throw spfft::InvalidParameterError();
+    spfft::gb300::IndexPlan plan;
+    bool device = false;
+    if (planner == 1) {
+      device = spfft::gb300::make_index_plan_device(transformType, dimX, dimY, dimZ,
+                                                    numLocalElements, indices, &plan);
+    }
+    if (!device) {
+      plan = spfft::gb300::make_index_plan(transformType, dimX, dimY, dimZ, numLocalElements, indices);
+    }
+    const spfft::gb300::IndexPlan h = spfft::gb300::download_index_plan(plan);
+    const long long ns = h.numSticks, ncol = h.numColumns, nv = h.numValues;
+    const long long need = 4 + nv + 5 * ns + ncol + (ncol + 1) + 2 * nv + (ns + 1) +
+                           static_cast<long long>(h.hermitianWeight.size());
+    *size = need;
+    if (usedDevice) *usedDevice = device ? 1 : 0;
+    if (!tables || capacity < need) return;
+    int* o = tables;
+    *o++ = h.numSticks;
+    *o++ = h.numColumns;
+    *o++ = h.zeroZeroStick;
+    *o++ = h.identityOrder ? 1 : 0;
+    auto put = [&o](const std::vector<int>& v) { o = std::copy(v.begin(), v.end(), o); };
+    put(h.valueIndices);
+    put(h.stickKeys);
+    put(h.stickColumn);
+    put(h.stickY);
+    std::vector<int> planePos(ns);
+    for (long long st = 0; st < ns; ++st) planePos[st] = h.stickY[st] * h.numColumns + h.stickColumn[st];
+    put(planePos);
+    put(h.columnX);
+    put(h.columnStickStart);
+    put(h.entryPos);
+    put(h.entryUser);
+    put(h.stickEntryStart);
+    for (unsigned char w : h.hermitianWeight) *o++ = w;
+  });
+}
+
+SpfftError spfft_gb300_plan_cache_size(int* count) {
+  return guarded([&] {
+    if (!count) throw spfft::InvalidParameterError();
+    *count = spfft::gb300::index_plan_cache_size();
   });
 }
 

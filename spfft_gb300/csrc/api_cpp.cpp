@@ -8,6 +8,7 @@
 #include "internal.hpp"
 #include "multi_batch.hpp"
 #include "planner.hpp"
+#include "planner_gpu.hpp"
 #include "spfft/grid.hpp"
 #include "spfft/grid_float.hpp"
 #include "spfft/multi_transform.hpp"
@@ -28,14 +29,23 @@ void check_transform_args(int dimX, int dimY, int dimZ, int localZLength, int nu
   }
 }
 
+// The plan of a transform: shared with a live transform of the same index set on the same device,
+// else made by the device planner (large sets of GPU transforms) or the host planner. `device` is
+// the grid's device, or -1 for the current one.
 std::shared_ptr<const gb300::IndexPlan> make_plan(SpfftTransformType type, int dimX, int dimY,
                                                   int dimZ, int numLocalElements,
                                                   SpfftIndexFormatType indexFormat,
-                                                  const int* indices) {
+                                                  const int* indices,
+                                                  SpfftProcessingUnitType processingUnit,
+                                                  int device) {
   // Only index triplets are defined (parameters.cpp:159-162 raises InternalError otherwise).
   if (indexFormat != SPFFT_INDEX_TRIPLETS) throw InternalError();
-  return std::make_shared<const gb300::IndexPlan>(
-      gb300::make_index_plan(type, dimX, dimY, dimZ, numLocalElements, indices));
+  const bool gpu = processingUnit == SPFFT_PU_GPU;
+  if (gpu && device >= 0) {
+    gb300::DeviceGuard guard(device);
+    return gb300::shared_index_plan(type, dimX, dimY, dimZ, numLocalElements, indices, true);
+  }
+  return gb300::shared_index_plan(type, dimX, dimY, dimZ, numLocalElements, indices, gpu);
 }
 
 template <typename TransformType, typename ValueType>
@@ -118,8 +128,9 @@ void multi_backward(int n, TransformType* transforms, const ValueType* const* in
                        int dimX, int dimY, int dimZ, int localZLength, int numLocalElements,      \
                        SpfftIndexFormatType indexFormat, const int* indices) {                    \
     check_transform_args(dimX, dimY, dimZ, localZLength, numLocalElements, indices);             \
+    const int device = grid && (grid->processing_unit() & SPFFT_PU_GPU) ? grid->device_id() : -1; \
     auto plan = make_plan(transformType, dimX, dimY, dimZ, numLocalElements, indexFormat,        \
-                          indices);                                                              \
+                          indices, processingUnit, device);                                      \
     transform_ = std::make_shared<TransformInternal<T>>(processingUnit, grid, std::move(plan));  \
   }                                                                                              \
   TRANSFORM::TRANSFORM(int maxNumThreads, SpfftProcessingUnitType processingUnit,                \
@@ -128,7 +139,7 @@ void multi_backward(int n, TransformType* transforms, const ValueType* const* in
                        const int* indices) {                                                      \
     check_transform_args(dimX, dimY, dimZ, 0, numLocalElements, indices);                        \
     auto plan = make_plan(transformType, dimX, dimY, dimZ, numLocalElements, indexFormat,        \
-                          indices);                                                              \
+                          indices, processingUnit, -1);                                          \
     std::shared_ptr<GridInternal<T>> grid(new GridInternal<T>(                                   \
         dimX, dimY, dimZ, plan->num_sticks(), processingUnit, maxNumThreads));                   \
     transform_ = std::make_shared<TransformInternal<T>>(processingUnit, std::move(grid),         \

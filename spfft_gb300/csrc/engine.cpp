@@ -1,6 +1,7 @@
 // GpuPlan: uploads the planner's tables and the twiddles once, picks tile shapes, and issues the
 // kernel sequence of each transform.
 #include "engine.hpp"
+#include "planner_gpu.hpp"
 
 #include <algorithm>
 #include <cstdlib>
@@ -127,22 +128,41 @@ GpuPlan<T>::GpuPlan(const IndexPlan& p, int device) {
     size_t offset;
   };
   std::vector<T> tz(twz.begin(), twz.end()), ty(twy.begin(), twy.end()), tx(twx.begin(), twx.end());
-  std::vector<int> planePos(ns);
-  for (int st = 0; st < ns; ++st) planePos[st] = p.stickY[st] * ncol + p.stickColumn[st];
+  // Index tables: a plan made by the device planner on this device is read where it lies (and
+  // kept alive with this plan); other plans upload their host tables, downloaded first when the
+  // plan was made on another device.
+  const DeviceIndexTables* dt =
+      (p.deviceTables && p.deviceTables->device == device) ? p.deviceTables.get() : nullptr;
+  IndexPlan downloaded;
+  const IndexPlan* hp = &p;
+  if (p.deviceTables && !dt) {
+    downloaded = download_index_plan(p);
+    hp = &downloaded;
+  }
+  if (dt) sharedTables_ = p.deviceTables;
+  std::vector<int> planePos;
+  if (!dt) {
+    planePos.resize(ns);
+    for (int st = 0; st < ns; ++st) planePos[st] = hp->stickY[st] * ncol + hp->stickColumn[st];
+  }
   std::vector<Part> parts = {
       {tz.data(), tz.size() * sizeof(T), 0},
       {ty.data(), ty.size() * sizeof(T), 0},
       {tx.data(), tx.size() * sizeof(T), 0},
-      {p.stickColumn.data(), p.stickColumn.size() * sizeof(int), 0},
-      {p.stickY.data(), p.stickY.size() * sizeof(int), 0},
-      {p.columnX.data(), p.columnX.size() * sizeof(int), 0},
-      {p.columnStickStart.data(), p.columnStickStart.size() * sizeof(int), 0},
-      {p.entryPos.data(), p.entryPos.size() * sizeof(int), 0},
-      {p.entryUser.data(), p.entryUser.size() * sizeof(int), 0},
-      {p.stickEntryStart.data(), p.stickEntryStart.size() * sizeof(int), 0},
-      {p.hermitianWeight.data(), p.hermitianWeight.size(), 0},
-      {planePos.data(), planePos.size() * sizeof(int), 0},
   };
+  if (!dt) {
+    parts.insert(parts.end(), {
+        {hp->stickColumn.data(), hp->stickColumn.size() * sizeof(int), 0},
+        {hp->stickY.data(), hp->stickY.size() * sizeof(int), 0},
+        {hp->columnX.data(), hp->columnX.size() * sizeof(int), 0},
+        {hp->columnStickStart.data(), hp->columnStickStart.size() * sizeof(int), 0},
+        {hp->entryPos.data(), hp->entryPos.size() * sizeof(int), 0},
+        {hp->entryUser.data(), hp->entryUser.size() * sizeof(int), 0},
+        {hp->stickEntryStart.data(), hp->stickEntryStart.size() * sizeof(int), 0},
+        {hp->hermitianWeight.data(), hp->hermitianWeight.size(), 0},
+        {planePos.data(), planePos.size() * sizeof(int), 0},
+    });
+  }
   size_t total = 0;
   for (auto& part : parts) {
     part.offset = total;
@@ -319,16 +339,29 @@ GpuPlan<T>::GpuPlan(const IndexPlan& p, int device) {
   base_.twz = reinterpret_cast<const T*>(d + parts[0].offset);
   base_.twy = reinterpret_cast<const T*>(d + parts[1].offset);
   base_.twx = reinterpret_cast<const T*>(d + parts[2].offset);
-  base_.stickColumn = reinterpret_cast<const int*>(d + parts[3].offset);
-  base_.stickY = reinterpret_cast<const int*>(d + parts[4].offset);
-  base_.stickPlanePos = reinterpret_cast<const int*>(d + parts[11].offset);
-  base_.columnX = reinterpret_cast<const int*>(d + parts[5].offset);
-  base_.columnStickStart = reinterpret_cast<const int*>(d + parts[6].offset);
-  base_.entryPos = reinterpret_cast<const int*>(d + parts[7].offset);
-  base_.entryUser = reinterpret_cast<const int*>(d + parts[8].offset);
-  base_.stickEntryStart = reinterpret_cast<const int*>(d + parts[9].offset);
-  base_.hermitianWeight =
-      p.hermitianWeight.empty() ? nullptr : reinterpret_cast<const unsigned char*>(d + parts[10].offset);
+  if (dt) {
+    base_.stickColumn = dt->stickColumn;
+    base_.stickY = dt->stickY;
+    base_.stickPlanePos = dt->stickPlanePos;
+    base_.columnX = dt->columnX;
+    base_.columnStickStart = dt->columnStickStart;
+    base_.entryPos = dt->entryPos;
+    base_.entryUser = dt->entryUser;
+    base_.stickEntryStart = dt->stickEntryStart;
+    base_.hermitianWeight = dt->hermitianWeight;
+  } else {
+    base_.stickColumn = reinterpret_cast<const int*>(d + parts[3].offset);
+    base_.stickY = reinterpret_cast<const int*>(d + parts[4].offset);
+    base_.stickPlanePos = reinterpret_cast<const int*>(d + parts[11].offset);
+    base_.columnX = reinterpret_cast<const int*>(d + parts[5].offset);
+    base_.columnStickStart = reinterpret_cast<const int*>(d + parts[6].offset);
+    base_.entryPos = reinterpret_cast<const int*>(d + parts[7].offset);
+    base_.entryUser = reinterpret_cast<const int*>(d + parts[8].offset);
+    base_.stickEntryStart = reinterpret_cast<const int*>(d + parts[9].offset);
+    base_.hermitianWeight = hp->hermitianWeight.empty()
+                                ? nullptr
+                                : reinterpret_cast<const unsigned char*>(d + parts[10].offset);
+  }
   numValues_ = nv;
 
   // Forward scaling factor T(1 / (Nx Ny Nz)) computed in double (execution_gpu.cpp:58-59).

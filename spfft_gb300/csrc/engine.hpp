@@ -110,6 +110,7 @@ private:
   T scale_ = T(1);
   int numValues_ = 0;
   DeviceBuffer tables_;
+  std::shared_ptr<const DeviceIndexTables> sharedTables_;  // device-planned index tables
 };
 
 // Opt-in shared memory per block of `device`, and one-time attribute setup of the specialised

@@ -89,6 +89,7 @@ IndexPlan make_index_plan(SpfftTransformType type, int dimX, int dimY, int dimZ,
     p.stickKeys.erase(std::unique(p.stickKeys.begin(), p.stickKeys.end()), p.stickKeys.end());
   }
   const int numSticks = static_cast<int>(p.stickKeys.size());
+  p.numSticks = numSticks;
   if (static_cast<long long>(numSticks) * dimZ > INT_MAX) throw OverflowError();
 
   // Value index = stickIndex * dimZ + zStorage (indices.hpp:167-176).
@@ -122,6 +123,7 @@ IndexPlan make_index_plan(SpfftTransformType type, int dimX, int dimY, int dimZ,
     p.stickColumn[s] = static_cast<int>(p.columnX.size()) - 1;
   }
   p.columnStickStart.push_back(numSticks);
+  p.numColumns = static_cast<int>(p.columnX.size());
 
   // Values grouped by stick and ordered by position; duplicates keep user order (a counting sort
   // over the value positions, or a stable sort when the position range is very large).

@@ -10,6 +10,7 @@
 #pragma once
 
 #include <cstdint>
+#include <memory>
 #include <vector>
 
 #include "spfft/types.h"
@@ -17,11 +18,14 @@
 namespace spfft {
 namespace gb300 {
 
+struct DeviceIndexTables;  // planner_gpu.hpp
+
 struct IndexPlan {
   SpfftTransformType type = SPFFT_TRANS_C2C;
   int dimX = 0, dimY = 0, dimZ = 0;
   int dimXFreq = 0;  // dimX/2+1 for R2C, dimX for C2C (parameters.cpp:148)
   int numValues = 0;
+  int numSticks = 0, numColumns = 0;
   bool centered = false;
 
   // --- reference-compatible part -------------------------------------------------------------
@@ -54,8 +58,13 @@ struct IndexPlan {
   // row of the x = 0 plane (where the plane fill conjugates in place). Used by the adjoints.
   std::vector<unsigned char> hermitianWeight;
 
-  int num_sticks() const { return static_cast<int>(stickKeys.size()); }
-  int num_columns() const { return static_cast<int>(columnX.size()); }
+  // Set when the plan was made by the device planner: the derived tables (stickColumn ..
+  // hermitianWeight, plus the stick plane positions) live on that device only, and the host
+  // vectors above are empty (download_index_plan() in planner_gpu.hpp brings them back).
+  std::shared_ptr<const DeviceIndexTables> deviceTables;
+
+  int num_sticks() const { return numSticks; }
+  int num_columns() const { return numColumns; }
 };
 
 // Throws the same exception types as the reference for the same inputs:

@@ -78,3 +78,30 @@ def test_null_handles_and_bad_arguments(lib):
     # grid limits are validated first (grid_internal.cpp:61-67)
     assert lib.spfft_grid_create(ctypes.byref(h), 0, 4, 4, 1, 2, 1) == E.SPFFT_INVALID_PARAMETER_ERROR
     assert lib.spfft_grid_create(ctypes.byref(h), 4, 4, 4, 1, 4, 1) == E.SPFFT_INVALID_PARAMETER_ERROR
+
+
+def test_plan_tables_are_consistent(lib):
+    """The derived tables of the host planner (the ones the device planner must reproduce) agree
+    with the reference-compatible value indices and stick keys."""
+    rng = np.random.default_rng(8)
+    for t, dims, centered in [(0, (12, 11, 13), False), (1, (16, 12, 10), True), (0, (20, 3, 7), True)]:
+        idx = random_indices(rng, *dims, r2c=(t == 1), centered=centered)
+        idx = np.ascontiguousarray(idx[rng.permutation(idx.shape[0])])
+        tb = sp.plan_tables(0, t, *dims, idx)
+        vi, sk, zz = sp.plan_indices(t, *dims, idx)
+        assert tb["used_device"] == 0
+        np.testing.assert_array_equal(tb["value_indices"], vi)
+        np.testing.assert_array_equal(tb["stick_keys"], sk)
+        assert tb["zero_zero_stick"] == zz and tb["num_sticks"] == len(sk)
+        dy, dz = dims[1], dims[2]
+        np.testing.assert_array_equal(tb["column_x"][tb["stick_column"]] * dy + tb["stick_y"], sk)
+        np.testing.assert_array_equal(tb["stick_plane_pos"], tb["stick_y"] * tb["num_columns"] + tb["stick_column"])
+        starts = tb["column_stick_start"]
+        assert starts[0] == 0 and starts[-1] == len(sk) and np.all(np.diff(starts) > 0)
+        assert np.all(np.diff(tb["entry_pos"]) > 0)
+        np.testing.assert_array_equal(np.sort(tb["entry_user"]), np.arange(len(vi)))
+        np.testing.assert_array_equal(vi[tb["entry_user"]], tb["entry_pos"])
+        np.testing.assert_array_equal(
+            tb["stick_entry_start"], np.searchsorted(tb["entry_pos"], np.arange(len(sk) + 1) * dz))
+        assert len(tb["hermitian_weight"]) == (len(vi) if t == 1 else 0)
+    assert sp.plan_cache_size() >= 0
