@@ -606,6 +606,7 @@ def measure_batched(args, workload: str, batch: int, dtype: str, radii=None) -> 
             "graph_launches_per_step": 1, "kernel_launches_per_step": info["launches_per_pair"],
             "shape_groups": info["groups"], "roundtrip_rel_l2_max": max(errs),
             "plane_pass": "fused" if bt.transform_path(0) == 2 else "split",
+            "row_groups": bt.row_groups(0),
             "pass_ms": {k: round(v, 4) for k, v in pass_ms.items()}, "pass_gbs": pass_gbs,
             "roofline": batch_roof,
             "hbm_gbs_per_pair_accounting": round(pb["pair"] / (ms / args.steps * 1e-3) / 1e9, 1),

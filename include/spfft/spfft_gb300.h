@@ -180,6 +180,12 @@ SPFFT_EXPORT SpfftError spfft_gb300_batch_autotune(SpfftGb300Batch batch, int re
  * plane with the compact plane on chip; chosen for cubic planes that fit two blocks per SM, or
  * forced with SPFFT_GB300_BATCH_PLANE=fused|split at batch creation). */
 SPFFT_EXPORT SpfftError spfft_gb300_batch_transform_path(SpfftGb300Batch batch, int index, int* path);
+/* Row groups of the fused plane passes of transform `index`: the x pass of each plane block is
+ * split into this many independent groups of warps that synchronise only among themselves (0 when
+ * the transform's plane passes are not fused). Chosen by spfft_gb300_batch_autotune, or set at
+ * batch creation with SPFFT_GB300_BATCH_ROW_GROUPS=1|2|3|4 where valid; by default 4 in FP32
+ * (where valid) and 1 in FP64. */
+SPFFT_EXPORT SpfftError spfft_gb300_batch_row_groups(SpfftGb300Batch batch, int index, int* groups);
 /* One direction (0 backward, 1 forward) of the bound batch with the groups run pass by pass on
  * `stream` and events between the three passes (z, y, x in backward order; a fused group runs its
  * plane pass in the y slot and nothing in the x slot); waits and writes the pass times in

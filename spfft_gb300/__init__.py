@@ -150,6 +150,7 @@ def _declare(lib: ctypes.CDLL) -> None:
     lib.spfft_gb300_batch_pair_graph.argtypes = [_vp, _i, _vp]
     lib.spfft_gb300_batch_info.argtypes = [_vp, _ip, _ip, _ip]
     lib.spfft_gb300_batch_transform_path.argtypes = [_vp, _i, _ip]
+    lib.spfft_gb300_batch_row_groups.argtypes = [_vp, _i, _ip]
     lib.spfft_gb300_batch_autotune.argtypes = [_vp, _i, _vp, ctypes.POINTER(ctypes.c_float)]
     lib.spfft_gb300_multi_batched_calls.argtypes = [ctypes.POINTER(ctypes.c_longlong)]
     lib.spfft_gb300_batch_stage_times.argtypes = [_vp, _i, _i, _vp, ctypes.POINTER(ctypes.c_float)]
@@ -568,4 +569,10 @@ class Batch:
         """0 unbatched, 1 batched with split y and x passes, 2 batched with the fused plane pass."""
         v = ctypes.c_int()
         _call("spfft_gb300_batch_transform_path", self._h, int(index), ctypes.byref(v))
+        return v.value
+
+    def row_groups(self, index: int) -> int:
+        """Row groups of the fused plane passes of transform `index` (0 when not fused)."""
+        v = ctypes.c_int()
+        _call("spfft_gb300_batch_row_groups", self._h, int(index), ctypes.byref(v))
         return v.value

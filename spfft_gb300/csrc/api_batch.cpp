@@ -141,6 +141,13 @@ SpfftError spfft_gb300_batch_transform_path(SpfftGb300Batch batch, int index, in
   });
 }
 
+SpfftError spfft_gb300_batch_row_groups(SpfftGb300Batch batch, int index, int* groups) {
+  if (!groups) return SPFFT_INVALID_PARAMETER_ERROR;
+  return with_batch(batch, [&](BatchHandle& h) {
+    *groups = h.d ? h.d->row_groups(index) : h.f->row_groups(index);
+  });
+}
+
 SpfftError spfft_gb300_multi_batched_calls(long long* count) {
   if (!count) return SPFFT_INVALID_PARAMETER_ERROR;
   *count = spfft::gb300::multi_batched_calls();

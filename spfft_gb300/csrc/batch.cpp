@@ -38,6 +38,8 @@ struct BatchPlan<T>::Group {
   bool fusedAvail = false, splitAvail = false;  // which plane strategies fit (for the autotuner)
   std::vector<int> zCands;                      // sticks per z block that fit (for the autotuner)
   int rowsF = 0, rowsB = 0, blocksP = 0;
+  int xGroups = 1;                // row groups of the fused plane passes' x pass
+  std::vector<int> groupCands;    // valid row-group counts
   size_t smemP = 0;
   T scale = T(0);
   DeviceBuffer dev;
@@ -155,6 +157,21 @@ BatchPlan<T>::BatchPlan(std::vector<std::shared_ptr<TransformInternal<T>>> trans
           g.rowsB = std::min(2 * rows, g.ny);
           g.rowsF = g.rowsB;
           g.smemP = sm;
+          // row groups of the x pass: whole warps per group, at least one row per group chunk
+          constexpr int threads = batch_plane_threads<T>();
+          for (int gr : {1, 2, 3, 4}) {
+            if (threads % gr == 0 && (threads / gr) % 32 == 0 && g.rowsB / gr >= 1) g.groupCands.push_back(gr);
+          }
+          // four groups in FP32 (192^3 R2C, 64 transforms: 26.2k against 25.3k pairs/s with one);
+          // SPFFT_GB300_BATCH_ROW_GROUPS=n starts with n row groups where n is valid
+          if (sizeof(T) == sizeof(float) &&
+              std::find(g.groupCands.begin(), g.groupCands.end(), 4) != g.groupCands.end()) {
+            g.xGroups = 4;
+          }
+          if (const char* env = std::getenv("SPFFT_GB300_BATCH_ROW_GROUPS")) {
+            const int want = std::atoi(env);
+            if (std::find(g.groupCands.begin(), g.groupCands.end(), want) != g.groupCands.end()) g.xGroups = want;
+          }
           break;
         }
       }
@@ -233,6 +250,15 @@ int BatchPlan<T>::transform_path(int t) const {
   if (t < 0 || t >= static_cast<int>(tp_.size())) throw InvalidParameterError();
   for (const auto& g : groups_) {
     if (std::find(g->members.begin(), g->members.end(), t) != g->members.end()) return g->fused ? 2 : 1;
+  }
+  return 0;
+}
+
+template <typename T>
+int BatchPlan<T>::row_groups(int t) const {
+  if (t < 0 || t >= static_cast<int>(tp_.size())) throw InvalidParameterError();
+  for (const auto& g : groups_) {
+    if (std::find(g->members.begin(), g->members.end(), t) != g->members.end()) return g->fused ? g->xGroups : 0;
   }
   return 0;
 }
@@ -328,7 +354,7 @@ void BatchPlan<T>::check_bound() const {
 namespace {
 template <typename T>
 void launch(FastOp op, int n, bool r2c, const BatchView<T>& bv, int blocks, size_t smem, int param,
-            cudaStream_t s, int param2 = 0) {
+            cudaStream_t s, int param2 = 0, int groups = 1) {
   if (blocks == 0) return;
   FastArgs<T> a;
   a.batch = &bv;
@@ -336,6 +362,7 @@ void launch(FastOp op, int n, bool r2c, const BatchView<T>& bv, int blocks, size
   a.smem = smem;
   a.param = param;
   a.param2 = param2;
+  a.groups = groups;
   a.stream = s;
   fast_dispatch<T>(op, n, r2c, a);
   check_launch(cudaGetLastError());
@@ -360,10 +387,10 @@ void BatchPlan<T>::run_pass(Group& g, int pass, int direction, bool scaled, cuda
     BatchView<T> bp = g.view(g.offStartsP, T(0));
     if (direction == 0) {
       bp.out = spacesOut;
-      launch(FastOp::BatchPlaneBackward, g.nx, g.r2c, bp, g.blocksP, g.smemP, g.rowsB, s);
+      launch(FastOp::BatchPlaneBackward, g.nx, g.r2c, bp, g.blocksP, g.smemP, g.rowsB, s, 0, g.xGroups);
     } else {
       bp.in = spaces;
-      launch(FastOp::BatchPlaneForward, g.nx, g.r2c, bp, g.blocksP, g.smemP, g.rowsF, s, g.rowsB);
+      launch(FastOp::BatchPlaneForward, g.nx, g.r2c, bp, g.blocksP, g.smemP, g.rowsF, s, g.rowsB, g.xGroups);
     }
   } else if (pass == 1) {
     launch(direction == 0 ? FastOp::BatchYBackward : FastOp::BatchYForward, g.ny, g.r2c, g.view(g.offStartsY, T(0)),
@@ -508,7 +535,7 @@ float BatchPlan<T>::autotune(cudaStream_t stream, int reps) {
         check_cuda(cudaEventElapsedTime(&ms, e0, e1));
         return ms / reps;
       };
-      int bestSpb = g.spb;
+      int bestSpb = g.spb, bestGroups = g.xGroups;
       bool bestFused = g.fused;
       float best = time_group();
       for (int f = 0; f < 2; ++f) {
@@ -527,6 +554,19 @@ float BatchPlan<T>::autotune(cudaStream_t stream, int reps) {
       }
       g.fused = bestFused;
       set_z_shape(g, bestSpb);
+      // row groups of the fused x pass, with the best z shape
+      if (g.fused) {
+        for (int gr : g.groupCands) {
+          if (gr == bestGroups) continue;
+          g.xGroups = gr;
+          const float ms = time_group();
+          if (ms < best) {
+            best = ms;
+            bestGroups = gr;
+          }
+        }
+        g.xGroups = bestGroups;
+      }
       total += best;
     }
   } catch (...) {

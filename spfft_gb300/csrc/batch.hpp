@@ -68,6 +68,8 @@ public:
   int num_fused_groups() const;
   // 0 unbatched, 1 batched with split y and x passes, 2 batched with the fused plane pass.
   int transform_path(int t) const;
+  // Row groups of the fused plane passes' x pass for transform t (0 when its passes are not fused).
+  int row_groups(int t) const;
   // Kernel launches of one backward + forward pair.
   int launches_per_pair() const;
 

@@ -75,19 +75,23 @@ __global__ void __launch_bounds__(kThreads) x_forward_batch(const BatchView<S> b
   x_forward_body<S, A, NX, R2C>(p, bv.in[t], rpb, lb % gx, lb / gx, &sExp);
 }
 
-// Fused y + x passes, one block per plane (cubic planes): starts count planes.
+// Fused y + x passes, one block per plane (cubic planes): starts count planes. `groups` row groups
+// share the x pass (RowGroups; blockDim.x / groups a multiple of 32, rows / groups >= 1).
 template <typename S, typename A, int N, bool R2C>
-__global__ void __launch_bounds__(BatchPlaneThreads<A>::value, 2) plane_backward_batch(const BatchView<S> bv, int rows) {
+__global__ void __launch_bounds__(BatchPlaneThreads<A>::value, 2)
+    plane_backward_batch(const BatchView<S> bv, int rows, int groups) {
   __shared__ int sExp;
   const int t = find_transform(bv.starts, bv.count, blockIdx.x);
-  plane_backward_body<S, A, N, N, R2C>(bv.views[t], bv.out[t], rows, blockIdx.x - bv.starts[t], &sExp);
+  plane_backward_body<S, A, N, N, R2C>(bv.views[t], bv.out[t], rows, blockIdx.x - bv.starts[t], &sExp, groups);
 }
 
 template <typename S, typename A, int N, bool R2C>
-__global__ void __launch_bounds__(BatchPlaneThreads<A>::value, 2) plane_forward_batch(const BatchView<S> bv, int rows, int wRows) {
+__global__ void __launch_bounds__(BatchPlaneThreads<A>::value, 2)
+    plane_forward_batch(const BatchView<S> bv, int rows, int wRows, int groups) {
   __shared__ int sExp;
   const int t = find_transform(bv.starts, bv.count, blockIdx.x);
-  plane_forward_body<S, A, N, N, R2C>(bv.views[t], bv.in[t], rows, wRows, blockIdx.x - bv.starts[t], &sExp);
+  plane_forward_body<S, A, N, N, R2C>(bv.views[t], bv.in[t], rows, wRows, blockIdx.x - bv.starts[t], &sExp,
+                                      groups);
 }
 
 template <typename S, typename A, int N>

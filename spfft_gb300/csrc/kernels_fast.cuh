@@ -28,6 +28,7 @@
 #include "dd.cuh"
 #include "dft.cuh"
 #include "kernels.hpp"
+#include "kernels_fast.hpp"
 
 namespace spfft {
 namespace gb300 {
@@ -35,11 +36,10 @@ namespace fast {
 
 constexpr int kThreads = 256;       // z-pass blocks
 constexpr int kPlaneThreads = 512;  // plane blocks (one plane per block, so more warps per SM)
-// Batched plane blocks (two per SM): 384 threads in FP32 (80 registers), 256 in double-float
-// (whose register demand would spill at 384).
+// Batched plane blocks (two per SM), by arithmetic type: batch_plane_threads() of the storage type.
 template <typename A>
 struct BatchPlaneThreads {
-  static constexpr int value = 384;
+  static constexpr int value = batch_plane_threads<float>();
 };
 // Minimum resident blocks per SM asked of the compiler for the split y kernels and the split x
 // forward kernel: double-float kernels are capped at 80 registers so that three 256-thread
@@ -56,7 +56,7 @@ struct YMinBlocks<dd> {
 };
 template <>
 struct BatchPlaneThreads<dd> {
-  static constexpr int value = 256;
+  static constexpr int value = batch_plane_threads<double>();
 };
 
 extern __shared__ __align__(16) unsigned char g_fast_smem[];
@@ -131,6 +131,24 @@ __device__ __forceinline__ ddc scale_pow2(ddc v, int d) {
 // once every block of this one has passed it. Both are no-ops for an ordinary launch.
 __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 __device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+// Thread groups of the plane kernels' x pass: the block splits into `groups` groups of whole warps
+// that each own a share of the rows and of the W buffer and synchronise only among themselves
+// (named barrier g + 1; barrier 0 is __syncthreads), so one group's barrier wait overlaps another
+// group's arithmetic. One group is the whole block.
+struct RowGroups {
+  int groups, threads, g, t;
+  __device__ __forceinline__ explicit RowGroups(int n)
+      : groups(n), threads(blockDim.x / n), g(threadIdx.x / (blockDim.x / n)),
+        t(threadIdx.x - (threadIdx.x / (blockDim.x / n)) * (blockDim.x / n)) {}
+  __device__ __forceinline__ void sync() const {
+    if (groups == 1) __syncthreads();
+    else asm volatile("bar.sync %0, %1;" ::"r"(g + 1), "r"(threads) : "memory");
+  }
+  // rows [begin, end) of this group out of n
+  __device__ __forceinline__ int begin(int n) const { return g * n / groups; }
+  __device__ __forceinline__ int end(int n) const { return (g + 1) * n / groups; }
+};
 
 // Division by a block-uniform runtime divisor d in [1, 2^16) for numerators n in [0, 2^16): one
 // high multiply by m = floor(2^32 / d) + 1 instead of the division sequence. Exact because
@@ -473,10 +491,11 @@ __device__ __forceinline__ void plane_load_tables(const PlanView<S>& p,
 // Pairs j = 0 .. floor(M/2) cover every k (for even M the middle pair is k = M/2 alone).
 // `row(rl)` gives compact row rl.
 template <typename L, typename CA, typename RowFn>
-__device__ __forceinline__ void c2r_pack_rows(RowFn row, int nr, CA* W, const int* colOf, const CA* twx) {
+__device__ __forceinline__ void c2r_pack_rows(RowFn row, int nr, CA* W, const int* colOf, const CA* twx,
+                                              int tid, int nthreads) {
   using A = decltype(CA{}.x);
   constexpr int M = L::M, H = M / 2;
-  for (int i = threadIdx.x; i < nr * (H + 1); i += blockDim.x) {
+  for (int i = tid; i < nr * (H + 1); i += nthreads) {
     const int rl = i / (H + 1), j = i - rl * (H + 1);
     const CA* prow = row(rl);
     CA* wrow = W + rl * L::WP;
@@ -497,7 +516,7 @@ __device__ __forceinline__ void c2r_pack_rows(RowFn row, int nr, CA* W, const in
 
 template <typename S, typename A, int NX, int NY, bool R2C>
 __device__ __forceinline__ void plane_backward_body(const PlanView<S>& p, S* __restrict__ space, int rows,
-                                                    int z, int* sExpPtr) {
+                                                    int z, int* sExpPtr, int groups = 1) {
   using TT = Types<S, A>;
   using CS = typename TT::CS;
   using CA = typename TT::CA;
@@ -551,18 +570,23 @@ __device__ __forceinline__ void plane_backward_body(const PlanView<S>& p, S* __r
   }
   __syncthreads();
 
-  // x-FFT of every row
+  // x-FFT of every row; each row group takes its own rows in chunks of `rows / groups`
   const CA* twl = R2C ? s.twm : s.twx;
-  for (int r0 = 0; r0 < NY; r0 += rows) {
-    const int nr = min(rows, NY - r0);
+  const RowGroups rg(groups);
+  const int gRows = rows / groups;
+  CA* W = s.W + rg.g * gRows * L::WP;
+  const int rEnd = rg.end(NY);
+  for (int r0 = rg.begin(NY); r0 < rEnd; r0 += gRows) {
+    const int nr = min(gRows, rEnd - r0);
     if (R2C) {
-      c2r_pack_rows<L>([&](int rl) { return s.P + transposed_pos<NY>(r0 + rl) * nc; }, nr, s.W, s.colOf, s.twx);
-      __syncthreads();
+      c2r_pack_rows<L>([&](int rl) { return s.P + transposed_pos<NY>(r0 + rl) * nc; }, nr, W, s.colOf, s.twx,
+                       rg.t, rg.threads);
+      rg.sync();
     }
-    for (int i = threadIdx.x; i < nr * Bx; i += blockDim.x) {
+    for (int i = rg.t; i < nr * Bx; i += rg.threads) {
       const int rl = i / Bx, b = i - rl * Bx;
       const CA* prow = s.P + transposed_pos<NY>(r0 + rl) * nc;
-      CA* wrow = s.W + rl * L::WP;
+      CA* wrow = W + rl * L::WP;
       CA v[Ax];
 #pragma unroll
       for (int a = 0; a < Ax; ++a) {
@@ -578,17 +602,17 @@ __device__ __forceinline__ void plane_backward_body(const PlanView<S>& p, S* __r
 #pragma unroll
       for (int k1 = 0; k1 < Ax; ++k1) wrow[L::wpos(k1 * Bx + b)] = v[k1];
     }
-    __syncthreads();
-    for (int i = threadIdx.x; i < nr * Ax; i += blockDim.x) {
+    rg.sync();
+    for (int i = rg.t; i < nr * Ax; i += rg.threads) {
       const int rl = i / Ax, k1 = i - rl * Ax;
       CA v[Bx];
-      fft_pass2<L::LX, +1>(s.W + rl * L::WP + k1 * L::PAD, 1, k1, v);
+      fft_pass2<L::LX, +1>(W + rl * L::WP + k1 * L::PAD, 1, k1, v);
       // C2C: complex x row; C2R: pairs (x[2m], x[2m+1]) of the real row
       CS* out = reinterpret_cast<CS*>(space + (static_cast<size_t>(z) * NY + r0 + rl) * NX * (R2C ? 1 : 2));
 #pragma unroll
       for (int k2 = 0; k2 < Bx; ++k2) out[k1 + Ax * k2] = to_storage(v[k2], k);
     }
-    __syncthreads();
+    rg.sync();
   }
 }
 
@@ -601,7 +625,7 @@ __global__ void __launch_bounds__(kPlaneThreads) plane_backward(const PlanView<S
 
 template <typename S, typename A, int NX, int NY, bool R2C>
 __device__ __forceinline__ void plane_forward_body(const PlanView<S>& p, const S* __restrict__ space, int rows,
-                                                   int wRows, int z, int* sExpPtr) {
+                                                   int wRows, int z, int* sExpPtr, int groups = 1) {
   using TT = Types<S, A>;
   using CS = typename TT::CS;
   using CA = typename TT::CA;
@@ -614,17 +638,22 @@ __device__ __forceinline__ void plane_forward_body(const PlanView<S>& p, const S
   PlaneSmem<CA, NX, NY, R2C> s(nc);
   plane_load_tables<S, A, NX, NY, R2C>(p, s);
 
-  // Row chunks of plane z are contiguous in the space buffer. When W holds two chunks (wRows >=
-  // 2 * rows) chunk i+1 streams into the other half while chunk i is transformed; otherwise each
-  // chunk is loaded after the previous one is done (the other blocks of the SM cover the wait).
+  // Row chunks of plane z are contiguous in the space buffer. Each row group (RowGroups) takes its
+  // own rows in chunks of rows / groups. With one group and W holding two chunks (wRows >= 2 *
+  // rows), chunk i+1 streams into the other half while chunk i is transformed; otherwise each
+  // chunk is loaded after the previous one is done (other groups and blocks cover the wait).
   const CS* plane = reinterpret_cast<const CS*>(space + static_cast<size_t>(z) * NY * NX * (R2C ? 1 : 2));
-  const int nchunks = (NY + rows - 1) / rows;
-  const bool dbuf = 2 * rows <= wRows;
+  const RowGroups rg(groups);
+  const int gRows = rows / groups;
+  const bool dbuf = groups == 1 && 2 * rows <= wRows;
+  CA* Wg = s.W + rg.g * gRows * L::WP;
+  const int gBegin = rg.begin(NY), gEnd = rg.end(NY);
+  const int nchunks = (gEnd - gBegin + gRows - 1) / gRows;
   auto issue_chunk = [&](int chunk) {
-    const int r0 = chunk * rows, nr = min(rows, NY - r0);
-    CA* dst = s.W + (dbuf ? (chunk & 1) : 0) * rows * L::WP;
+    const int r0 = gBegin + chunk * gRows, nr = min(gRows, gEnd - r0);
+    CA* dst = Wg + (dbuf ? (chunk & 1) : 0) * gRows * L::WP;
     const CS* src = plane + static_cast<size_t>(r0) * L::LX;
-    for (int i = threadIdx.x; i < nr * L::LX; i += blockDim.x) {
+    for (int i = rg.t; i < nr * L::LX; i += rg.threads) {
       const int rl = i / L::LX, e = i - rl * L::LX;
       cp_async_c(dst + rl * L::WP + L::wpos(e), src + i);
     }
@@ -649,8 +678,8 @@ __device__ __forceinline__ void plane_forward_body(const PlanView<S>& p, const S
 
   const CA* twl = R2C ? s.twm : s.twx;
   for (int chunk = 0; chunk < nchunks; ++chunk) {
-    const int r0 = chunk * rows, nr = min(rows, NY - r0);
-    CA* wbase = s.W + (dbuf ? (chunk & 1) : 0) * rows * L::WP;
+    const int r0 = gBegin + chunk * gRows, nr = min(gRows, gEnd - r0);
+    CA* wbase = Wg + (dbuf ? (chunk & 1) : 0) * gRows * L::WP;
     if (!dbuf && chunk > 0) issue_chunk(chunk);
     if (dbuf && chunk + 1 < nchunks) {
       issue_chunk(chunk + 1);
@@ -658,8 +687,8 @@ __device__ __forceinline__ void plane_forward_body(const PlanView<S>& p, const S
     } else {
       cp_async_wait<0>();
     }
-    __syncthreads();
-    for (int i = threadIdx.x; i < nr * Bx; i += blockDim.x) {
+    rg.sync();
+    for (int i = rg.t; i < nr * Bx; i += rg.threads) {
       const int rl = i / Bx, b = i - rl * Bx;
       // padded row: element a*Bx + b sits at a*(Bx + PAD) + b (raw storage values until here)
       CA* wrow = wbase + rl * L::WP;
@@ -672,8 +701,8 @@ __device__ __forceinline__ void plane_forward_body(const PlanView<S>& p, const S
 #pragma unroll
       for (int k1 = 0; k1 < Ax; ++k1) wrow[k1 * (Bx + L::PAD) + b] = v[k1];
     }
-    __syncthreads();
-    for (int i = threadIdx.x; i < nr * Ax; i += blockDim.x) {
+    rg.sync();
+    for (int i = rg.t; i < nr * Ax; i += rg.threads) {
       const int rl = i / Ax, k1 = i - rl * Ax;
       CA v[Bx];
       CA* wrow = wbase + rl * L::WP + k1 * L::PAD;
@@ -690,10 +719,10 @@ __device__ __forceinline__ void plane_forward_body(const PlanView<S>& p, const S
         for (int k2 = 0; k2 < Bx; ++k2) wrow[k1 * Bx + k2] = v[k2];  // wrow is offset by k1*PAD
       }
     }
-    __syncthreads();
+    rg.sync();
     if (R2C) {
       // X[k] = (Z[k] + conj Z[M-k]) / 2 - i/2 e^{-2 pi i k/N} (Z[k] - conj Z[M-k]), Z[M] = Z[0]
-      for (int i = threadIdx.x; i < nr * nc; i += blockDim.x) {
+      for (int i = rg.t; i < nr * nc; i += rg.threads) {
         const int rl = dnc.div(i), c = i - rl * nc;
         const int4 ci = s.colInfo[c];
         const CA* wrow = wbase + rl * L::WP;
@@ -703,9 +732,10 @@ __device__ __forceinline__ void plane_forward_body(const PlanView<S>& p, const S
         const CA u = cmul(dif, s.twx[ci.z]);
         s.P[(r0 + rl) * nc + c] = make_c(half_of(zk.x + zm.x + u.y), half_of(zk.y - zm.y - u.x));
       }
-      __syncthreads();
+      rg.sync();
     }
   }
+  if (groups > 1) __syncthreads();  // every group's rows are in P before the y pass
 
   for (int i = threadIdx.x; i < nc * By; i += blockDim.x) {
     const int b = dnc.div(i), c = i - b * nc;
@@ -1115,7 +1145,7 @@ __device__ __forceinline__ void x_backward_body(const PlanView<S>& p, S* __restr
   }
   const CA* twl = R2C ? s.twm : s.twx;
   if (R2C) {
-    c2r_pack_rows<L>([&](int rl) { return s.P + rl * nc; }, nr, s.W, s.colOf, s.twx);
+    c2r_pack_rows<L>([&](int rl) { return s.P + rl * nc; }, nr, s.W, s.colOf, s.twx, threadIdx.x, blockDim.x);
     __syncthreads();
   }
   for (int i = threadIdx.x; i < nr * Bx; i += blockDim.x) {

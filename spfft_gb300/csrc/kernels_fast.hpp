@@ -38,11 +38,19 @@ enum class FastOp {
   BatchPlaneForward
 };
 
+// Threads of a batched fused plane block (two blocks per SM): 384 in FP32 (80 registers), 256 in
+// double-float (T = double; its register demand would spill at 384).
+template <typename T>
+constexpr int batch_plane_threads() {
+  return sizeof(T) == sizeof(float) ? 384 : 256;
+}
+
 template <typename T>
 struct FastArgs {
   const PlanView<T>* plan = nullptr;
   int param = 0;  // sticks per block (z) or rows per chunk (plane)
   int param2 = 0;  // batched plane forward: rows of the chunk buffer (2 * param double-buffers)
+  int groups = 1;  // batched plane passes: independent row groups of the x pass
   int zBegin = 0, zCount = -1;  // split y and x passes: plane range (zCount < 0: to the last plane)
   const T* in = nullptr;
   T* out = nullptr;

@@ -148,6 +148,54 @@ def test_batch_plane_pass_modes(lib, dtype, mode, monkeypatch):
 
 
 @pytest.mark.parametrize("dtype", ["float64", "float32"])
+def test_batch_row_groups_give_identical_results(lib, dtype, monkeypatch):
+    """The fused plane passes with the x pass split into independent row groups compute exactly
+    what one group computes (same arithmetic per element), for every valid group count."""
+    monkeypatch.setenv("SPFFT_GB300_BATCH_PLANE", "fused")
+    specs = [(64, 16, 0), (60, 15, 1), (48, 12, 1), (64, 20, 0)]
+    if dtype == "float32":
+        specs.append((192, 48, 1))
+    results = {}
+    for groups in (1, 2, 3, 4):
+        monkeypatch.setenv("SPFFT_GB300_BATCH_ROW_GROUPS", str(groups))
+        rng = np.random.default_rng(7)
+        items = _make(dtype, specs, rng)
+        batch = sp.Batch([it["tr"] for it in items])
+        got = batch.row_groups(0)
+        if groups == 3 and dtype == "float64":
+            assert got == 1  # 256 threads do not split into three groups of whole warps
+            continue
+        assert got == groups
+        batch.bind([it["vals"] for it in items], [it["space"] for it in items])
+        host_vals = []
+        for it in items:
+            v = rng.uniform(-1, 1, len(it["idx"])) + 1j * rng.uniform(-1, 1, len(it["idx"]))
+            if it["ttype"] == 1:
+                v[(it["idx"] == 0).all(axis=1)] = v[(it["idx"] == 0).all(axis=1)].real
+            host_vals.append(v)
+            it["vals"].copy_(torch.from_numpy(v).to(it["vals"].dtype))
+        stream = torch.cuda.Stream()
+        torch.cuda.synchronize()
+        batch.backward(stream)
+        stream.synchronize()
+        spaces = [it["space"].cpu().numpy().copy() for it in items]
+        for it, v, sp_ in zip(items, host_vals, spaces):
+            assert rel_l2(sp_, it["oracle"].backward(v)) <= TOL[dtype], it["dims"]
+        batch.forward(sp.SPFFT_NO_SCALING, stream)
+        stream.synchronize()
+        vals = [it["vals"].cpu().numpy().copy() for it in items]
+        for it, sp_, got_v in zip(items, spaces, vals):
+            want = it["oracle"].forward(sp_.astype(np.complex128 if it["ttype"] == 0 else np.float64))
+            assert rel_l2(got_v, want) <= TOL[dtype], it["dims"]
+        results[groups] = (spaces, vals)
+    for groups, (spaces, vals) in results.items():
+        for a, b in zip(spaces, results[1][0]):
+            np.testing.assert_array_equal(a, b)
+        for a, b in zip(vals, results[1][1]):
+            np.testing.assert_array_equal(a, b)
+
+
+@pytest.mark.parametrize("dtype", ["float64", "float32"])
 def test_batch_autotune_then_graph(lib, dtype):
     """Autotuning a bound batch (per group: plane strategy and z block size), then a captured pair
     with new data against the oracle."""
