@@ -132,7 +132,7 @@ def batch_pass_bytes(bt, geo: list) -> dict:
 
 
 def algorithmic_bytes(n: int, npts: int, nsticks: int, ncols: int, r2c: bool, tsize: int) -> dict:
-    """Compulsory HBM bytes per launch of each kernel and per pair (SURVEY-style accounting:
+    """Compulsory HBM bytes per launch of each kernel and per pair (compulsory-traffic accounting:
     sparse values + int32 value map + intermediates + dense space grid, each read or written once)."""
     c = 2 * tsize
     s = tsize if r2c else c

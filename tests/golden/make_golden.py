@@ -51,7 +51,7 @@ def ref_cases() -> None:
 
 EDGES = [
     # (name, type, dx, dy, dz, triplets)
-    ("survey_probe", 0, 4, 4, 4, [0, 0, 0, 1, 0, -1, -1, 2, -1, 1, 0, 2]),
+    ("mixed_sign_probe", 0, 4, 4, 4, [0, 0, 0, 1, 0, -1, -1, 2, -1, 1, 0, 2]),
     ("plain_max", 0, 5, 4, 3, [4, 3, 2, 0, 0, 0]),
     ("plain_over", 0, 5, 4, 3, [5, 0, 0]),
     ("centered_bounds", 0, 5, 4, 3, [-2, -1, -1, 2, 2, 1]),
