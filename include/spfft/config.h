@@ -1,5 +1,5 @@
 /* Build configuration of the GB300 SpFFT library (hand-written; the reference generates this file
- * from CMake, include/spfft/config.h.in). This build always has the CUDA backend and the
+ * from CMake, include/spfft/config.h.in). This library always has the CUDA backend and the
  * single-precision API, and never MPI. */
 #ifndef SPFFT_CONFIG_H
 #define SPFFT_CONFIG_H

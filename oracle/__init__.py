@@ -1,7 +1,7 @@
 """CPU oracle for the GB300 SpFFT library -- TEST INFRASTRUCTURE ONLY.
 
 Nothing in the library imports this package. Only tests/, ``__graft_entry__.smoke()`` and the
-CPU-baseline legs of ``bench.py`` use it, and only as the checker or as the timed CPU baseline.
+CPU-baseline legs of ``bench.py`` use it, and only to produce expected results or as the timed CPU baseline.
 
 * ``indices``  -- numpy restatement of the reference's index conversion
   (src/compression/indices.hpp:120-186, src/parameters/parameters.cpp:143-180).

@@ -333,7 +333,7 @@ void BatchPlan<T>::bind(const T* const* values, T* const* spaces, cudaStream_t s
     }
     char* d = static_cast<char*>(g.dev.get());
     if (async) {
-      // pageable source: staged by the driver before the call returns, written in stream order
+      // pageable source: staged by the CUDA runtime before the call returns, written in stream order
       check_cuda(cudaMemcpyAsync(d + g.offValues, vp.data(), vp.size() * sizeof(T*), cudaMemcpyHostToDevice,
                                  stream));
       check_cuda(cudaMemcpyAsync(d + g.offSpaces, sp.data(), sp.size() * sizeof(T*), cudaMemcpyHostToDevice,
