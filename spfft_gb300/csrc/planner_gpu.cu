@@ -533,7 +533,13 @@ IndexPlan make_index_plan_auto(SpfftTransformType type, int dimX, int dimY, int 
   const int threshold = mode == "device" ? 1 : kDevicePlanMinValues;
   if (allowDevice && mode != "host" && numValues >= threshold && device_present()) {
     IndexPlan p;
-    if (make_index_plan_device(type, dimX, dimY, dimZ, numValues, triplets, &p)) return p;
+    try {
+      if (make_index_plan_device(type, dimX, dimY, dimZ, numValues, triplets, &p)) return p;
+    } catch (const GPUError&) {
+      // a device that cannot run the planner (no stream-ordered allocator, out of memory): plan on
+      // the host; index errors are not GPU errors and propagate
+      (void)cudaGetLastError();
+    }
   }
   return make_index_plan(type, dimX, dimY, dimZ, numValues, triplets);
 }

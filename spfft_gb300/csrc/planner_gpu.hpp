@@ -46,7 +46,7 @@ IndexPlan download_index_plan(const IndexPlan& p);
 // Planner choice of transform creation: the device planner when `allowDevice` (a GPU transform),
 // a device is present, the set has at least kDevicePlanMinValues values and SPFFT_GB300_PLANNER
 // is not "host" ("device" lowers the threshold to 1); otherwise, or where the device planner
-// declines, the host planner.
+// declines or fails with a GPU error, the host planner.
 constexpr int kDevicePlanMinValues = 16384;
 IndexPlan make_index_plan_auto(SpfftTransformType type, int dimX, int dimY, int dimZ, int numValues,
                                const int* triplets, bool allowDevice);
