@@ -40,6 +40,13 @@ SPFFT_EXPORT SpfftError spfft_gb300_plan_tables(int planner, SpfftTransformType 
                                                 int* tables, long long capacity, long long* size,
                                                 int* usedDevice);
 
+/* Fault injection for tests of the allocation-failure paths (no GPU fault involved): the next
+ * afterAllocations device or pinned host allocations of the library succeed and the one after fails
+ * once, as if the CUDA allocator had failed (SPFFT_GPU_ALLOCATION_ERROR for device memory,
+ * SPFFT_ALLOCATION_ERROR for pinned host memory). -1 turns it off. previous (may be NULL) receives
+ * the countdown before the call: -1 once an injected failure has fired. */
+SPFFT_EXPORT SpfftError spfft_gb300_inject_allocation_failure(int afterAllocations, int* previous);
+
 /* Number of live index plans that transform creation can share (transforms created with the same
  * type, sizes and index triplets on the same device share one plan and its device tables;
  * SPFFT_GB300_PLAN_CACHE=0 turns the sharing off). */

@@ -141,6 +141,7 @@ def _declare(lib: ctypes.CDLL) -> None:
     lib.spfft_gb300_plan_tables.argtypes = [_i, _i, _i, _i, _i, _i, _vp, _vp, ctypes.c_longlong,
                                             ctypes.POINTER(ctypes.c_longlong), _ip]
     lib.spfft_gb300_plan_cache_size.argtypes = [_ip]
+    lib.spfft_gb300_inject_allocation_failure.argtypes = [_i, _ip]
     lib.spfft_gb300_batch_create.argtypes = [ctypes.POINTER(_vp), _i, ctypes.POINTER(_vp)]
     lib.spfft_gb300_float_batch_create.argtypes = [ctypes.POINTER(_vp), _i, ctypes.POINTER(_vp)]
     lib.spfft_gb300_batch_destroy.argtypes = [_vp]
@@ -244,6 +245,14 @@ def plan_tables(planner: int, transform_type: int, dim_x: int, dim_y: int, dim_z
         out[name] = buf[pos:pos + length].copy()
         pos += length
     return out
+
+
+def inject_allocation_failure(after_allocations: int) -> int:
+    """Test hook: the allocation after `after_allocations` more successful ones fails once (-1 turns
+    it off). Returns the previous countdown (-1 once an injected failure has fired)."""
+    v = ctypes.c_int(0)
+    _call("spfft_gb300_inject_allocation_failure", int(after_allocations), ctypes.byref(v))
+    return v.value
 
 
 def plan_cache_size() -> int:

@@ -388,6 +388,13 @@ SpfftError spfft_gb300_plan_tables(int planner, SpfftTransformType transformType
   });
 }
 
+SpfftError spfft_gb300_inject_allocation_failure(int afterAllocations, int* previous) {
+  if (afterAllocations < -1) return SPFFT_INVALID_PARAMETER_ERROR;
+  const int old = spfft::gb300::allocation_countdown().exchange(afterAllocations);
+  if (previous) *previous = old;
+  return SPFFT_SUCCESS;
+}
+
 SpfftError spfft_gb300_plan_cache_size(int* count) {
   return guarded([&] {
     if (!count) throw spfft::InvalidParameterError();

@@ -296,7 +296,10 @@ __global__ void __launch_bounds__(kThreads)
 // Stream-ordered scratch, freed in stream order.
 class AsyncBuffer {
 public:
-  AsyncBuffer(size_t bytes, cudaStream_t s) : s_(s) { check_cuda(cudaMallocAsync(&p_, bytes, s)); }
+  AsyncBuffer(size_t bytes, cudaStream_t s) : s_(s) {
+    if (injected_allocation_failure()) throw GPUAllocationError();
+    check_cuda(cudaMallocAsync(&p_, bytes, s));
+  }
   ~AsyncBuffer() {
     if (p_) (void)cudaFreeAsync(p_, s_);
   }

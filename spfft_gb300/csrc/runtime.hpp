@@ -7,6 +7,7 @@
 
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstddef>
 #include <utility>
 
@@ -32,6 +33,21 @@ inline void check_launch(cudaError_t error) {
       error == cudaErrorInvalidDeviceFunction || error == cudaErrorNoKernelImageForDevice)
     throw GPULaunchError();
   check_cuda(error);
+}
+
+// Fault injection for the tests of the allocation-failure paths: with the countdown at n >= 0 the
+// next n device or pinned host allocations of the library succeed and the one after fails, once,
+// with the exception a failing CUDA allocator raises (without calling it). -1 turns it off.
+inline std::atomic<int>& allocation_countdown() {
+  static std::atomic<int> countdown{-1};
+  return countdown;
+}
+inline bool injected_allocation_failure() {
+  int c = allocation_countdown().load();
+  while (c >= 0) {
+    if (allocation_countdown().compare_exchange_weak(c, c - 1)) return c == 0;
+  }
+  return false;
 }
 
 class DeviceGuard {
@@ -78,6 +94,7 @@ private:
   void resize(size_t bytes) {
     release();
     if (bytes == 0) return;
+    if (injected_allocation_failure()) throw GPUAllocationError();
     check_cuda(cudaMalloc(&ptr_, bytes));
     bytes_ = bytes;
   }
@@ -107,6 +124,7 @@ public:
     if (ptr_) (void)cudaFreeHost(ptr_);
     ptr_ = nullptr;
     bytes_ = 0;
+    if (injected_allocation_failure()) throw HostAllocationError();
     if (cudaMallocHost(&ptr_, bytes) != cudaSuccess) {
       ptr_ = nullptr;
       throw HostAllocationError();

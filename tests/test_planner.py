@@ -105,3 +105,12 @@ def test_plan_tables_are_consistent(lib):
             tb["stick_entry_start"], np.searchsorted(tb["entry_pos"], np.arange(len(sk) + 1) * dz))
         assert len(tb["hermitian_weight"]) == (len(vi) if t == 1 else 0)
     assert sp.plan_cache_size() >= 0
+
+
+def test_allocation_failure_hook_countdown(lib):
+    """The fault-injection countdown arms and disarms without a GPU (nothing allocates here)."""
+    assert sp.inject_allocation_failure(5) == -1
+    assert sp.inject_allocation_failure(2) == 5
+    assert sp.inject_allocation_failure(-1) == 2
+    with pytest.raises(sp.SpfftError):
+        sp.inject_allocation_failure(-2)
