@@ -13,6 +13,12 @@ ref_edges.npz   Hand-made planner edge cases (bounds, centered switch, R2C x ran
                 empty input) with the reference planner's output or error code.
 dense_small.npz A few small transforms (inputs and unnormalised dense DFT outputs, numpy) used to
                 pin the floating-point results independently of the oracle pipeline code.
+ref_pipeline.npz The reference's OWN host transform path (oracle/_ref/libref_pipeline.so: its
+                execution_host.cpp and everything it calls, with FFTW replaced by the project's
+                FFTW-API shim) run on the inputs of its local test suite, FP64: C2C backward then
+                forward of the generated values; R2C forward then backward of the real space
+                domain the suite builds (a uniform(0,1) draw at each index position), as in
+                tests/test_util/test_transform.hpp:153-276.
 """
 from __future__ import annotations
 
@@ -116,11 +122,52 @@ def dense_small() -> None:
     np.savez_compressed(OUT / "dense_small.npz", **arrays)
 
 
+def r2c_space_of_test(dx: int, dy: int, dz: int, idx: np.ndarray, re: np.ndarray) -> np.ndarray:
+    """The real space domain the reference's R2C test builds: the value drawn for triplet i sits at
+    the triplet's own (storage) position (test_transform.hpp:232-237, 257-263)."""
+    t = idx.reshape(-1, 3)
+    space = np.zeros((dz, dy, dx))
+    space[t[:, 2] % dz, t[:, 1] % dy, t[:, 0] % dx] = re
+    return space
+
+
+PIPELINE_CASES = [(11, 12, 13), (13, 11, 12), (12, 12, 12), (2, 11, 13), (13, 1, 12), (11, 2, 1),
+                  (1, 1, 1), (12, 13, 2)]
+
+
+def ref_pipeline() -> None:
+    arrays = {}
+    names = []
+    for r2c, centered in itertools.product((False, True), (False, True)):
+        for dx, dy, dz in PIPELINE_CASES:
+            case = ref.test_case(dx, dy, dz, r2c, centered)
+            idx = case["indices"].astype(np.int32)
+            if idx.size == 0:
+                continue
+            name = f"{'r2c' if r2c else 'c2c'}_{'cen' if centered else 'pos'}_{dx}_{dy}_{dz}"
+            arrays[name + "/args"] = np.array([int(r2c), dx, dy, dz], dtype=np.int32)
+            arrays[name + "/indices"] = idx.astype(np.int8)
+            if r2c:
+                space_in = r2c_space_of_test(dx, dy, dz, idx, case["values"].real)
+                space, values = ref.pipeline_run(1, dx, dy, dz, idx, space=space_in)
+                arrays[name + "/space_in"] = space_in
+            else:
+                space, values = ref.pipeline_run(0, dx, dy, dz, idx, values=case["values"])
+                arrays[name + "/values_in"] = case["values"]
+            arrays[name + "/space_out"] = space
+            arrays[name + "/values_out"] = values
+            names.append(name)
+    arrays["names"] = np.array(names)
+    np.savez_compressed(OUT / "ref_pipeline.npz", **arrays)
+
+
 if __name__ == "__main__":
     if not ref.available():
         sys.exit("oracle/_ref/ref_indices missing: run `make -C oracle` where the reference exists")
     ref_cases()
     ref_edges()
     dense_small()
+    if ref.pipeline_available():
+        ref_pipeline()
     for f in sorted(OUT.glob("*.npz")):
         print(f.name, f.stat().st_size)

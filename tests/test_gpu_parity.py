@@ -417,3 +417,35 @@ def test_autotune_keeps_results(lib, dtype):
         f = torch.empty_like(v)
         tr.forward(out, f)
         assert rel_l2(f.cpu().numpy(), oracle.forward(want)) <= TOL[dtype], (n, after)
+
+
+@pytest.mark.parametrize("dtype", ["float64", "float32"])
+def test_reference_pipeline_golden(lib, dtype):
+    """The library against golden vectors of the reference's OWN host transform path (run on the
+    inputs of its local test suite, FP64; tests/golden/make_golden.py): C2C backward then forward,
+    R2C forward then backward, the order of the reference's tests."""
+    cases = load_npz_group("ref_pipeline.npz")
+    assert len(cases) >= 28
+    for name, c in cases.items():
+        t, dx, dy, dz = map(int, c["args"])
+        idx = np.ascontiguousarray(c["indices"].astype(np.int32).reshape(-1, 3))
+        tr = _transform(dtype, t, (dx, dy, dz), idx)
+        n = idx.shape[0]
+        vals = torch.empty(n, dtype=CT[dtype], device="cuda")
+        space = torch.empty((dz, dy, dx), dtype=CT[dtype] if t == 0 else RT[dtype], device="cuda")
+        if t == 0:
+            vals.copy_(torch.from_numpy(c["values_in"]).to(CT[dtype]))
+            tr.backward(vals, space)
+            torch.cuda.synchronize()
+            assert rel_l2(space.cpu().numpy(), c["space_out"]) <= TOL[dtype], name
+            tr.forward(space, vals)
+            torch.cuda.synchronize()
+            assert rel_l2(vals.cpu().numpy(), c["values_out"]) <= TOL[dtype], name
+        else:
+            space.copy_(torch.from_numpy(c["space_in"]).to(RT[dtype]))
+            tr.forward(space, vals)
+            torch.cuda.synchronize()
+            assert rel_l2(vals.cpu().numpy(), c["values_out"]) <= TOL[dtype], name
+            tr.backward(vals, space)
+            torch.cuda.synchronize()
+            assert rel_l2(space.cpu().numpy(), c["space_out"]) <= TOL[dtype], name

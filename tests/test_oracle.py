@@ -80,3 +80,47 @@ def test_oracle_indices_match_reference_binary_random():
         np.testing.assert_array_equal(p["value_indices"], r["value_indices"])
         np.testing.assert_array_equal(p["stick_keys"], r["stick_keys"])
         assert p["zero_zero_stick"] == r["zero_zero_stick"]
+
+
+def test_oracle_pipeline_matches_reference_pipeline_golden():
+    """The oracle against the reference's OWN host transform path (golden vectors it produced on
+    the inputs of its local test suite; tests/golden/make_golden.py)."""
+    cases = load_npz_group("ref_pipeline.npz")
+    assert len(cases) >= 28
+    for name, c in cases.items():
+        t, dx, dy, dz = map(int, c["args"])
+        p = pipeline.HostPipeline(t, dx, dy, dz, c["indices"].astype(np.int64))
+        if t == 0:
+            assert rel_l2(p.backward(c["values_in"]), c["space_out"]) < 1e-13, name
+            assert rel_l2(p.forward(c["space_out"]), c["values_out"]) < 1e-13, name
+        else:
+            assert rel_l2(p.forward(c["space_in"]), c["values_out"]) < 1e-13, name
+            assert rel_l2(p.backward(c["values_out"]), c["space_out"]) < 1e-13, name
+
+
+@pytest.mark.skipif(not ref.pipeline_available(), reason="reference pipeline not built here")
+@pytest.mark.parametrize("precision", ["float64", "float32"])
+def test_oracle_pipeline_matches_live_reference_pipeline(precision):
+    """Where the reference's host path is built (oracle/_ref), the oracle against it live: the whole
+    local suite of index sets, C2C and R2C, plain and centered, larger sphere sets, non-hermitian
+    R2C values, and scaled forwards."""
+    from util import sphere_indices
+
+    tol = 1e-13 if precision == "float64" else 2e-6
+    rng = np.random.default_rng(17)
+    cases = [(1 if k.startswith("r2c") else 0, tuple(int(v) for v in k.split("_")[2:]),
+              c["indices"].astype(np.int64)) for k, c in load_npz_group("ref_cases.npz").items()]
+    cases += [(0, (64, 64, 64), sphere_indices(64, 16)), (1, (48, 48, 48), sphere_indices(48, 12, True)),
+              (1, (30, 20, 18), sphere_indices(18, 6, True)), (0, (45, 50, 27), sphere_indices(27, 9))]
+    for k, (t, dims, idx) in enumerate(cases):
+        if idx.size == 0:
+            continue
+        n = idx.size // 3
+        vals = rng.uniform(-1, 1, n) + 1j * rng.uniform(-1, 1, n)  # non-hermitian for R2C too
+        scaling = k % 2
+        space, fwd = ref.pipeline_run(t, *dims, idx, values=vals, precision=precision, scaling=scaling)
+        p = pipeline.HostPipeline(t, *dims, idx.reshape(-1, 3))
+        want = p.backward(vals)
+        assert rel_l2(space, want) < tol, (dims, t)
+        want_f = p.forward(space.astype(np.complex128 if t == 0 else np.float64), scaled=bool(scaling))
+        assert rel_l2(fwd, want_f) < tol, (dims, t)
