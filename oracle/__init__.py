@@ -11,11 +11,14 @@ CPU-baseline legs of ``bench.py`` use it, and only to produce expected results o
   replaced by scipy.fft (pocketfft) transforms of the same direction and normalisation.
 * ``dense``    -- the dense 3D DFT oracle of the reference's tests
   (tests/test_util/test_transform.hpp:33-276).
-* ``ref``      -- runs ``_ref/ref_indices``, the reference's own index code compiled from its
-  sources by ``Makefile`` (only where the reference sources exist).
+* ``ref``      -- runs the reference's own code compiled from its sources by ``Makefile`` (only
+  where the reference sources exist): ``_ref/ref_indices`` (its index planner and test-input
+  generator) and ``_ref/libref_pipeline.so`` (its host transform path, src/execution/
+  execution_host.cpp and what it calls, with FFTW 3 -- absent here -- replaced by the FFTW-API
+  shim ``fftw_shim/``, a DFT written for this project).
 
 Parity pinning: index/layout results are pinned bit-exactly against ``_ref`` (fixtures under
-tests/golden/). Floating-point results are pinned against the dense DFT definition, which is the
-check the reference's own tests make; the reference ships no floating-point golden vectors and its
-FFT library (FFTW 3) is not available here.
+tests/golden/). Floating-point results are pinned against the reference's own host transform path
+(``ref_pipeline.npz``, produced by ``libref_pipeline.so`` on the inputs of the reference's local
+test suite) and against the dense DFT definition, the check the reference's own tests make.
 """
