@@ -172,6 +172,12 @@ BatchPlan<T>::BatchPlan(std::vector<std::shared_ptr<TransformInternal<T>>> trans
             const int want = std::atoi(env);
             if (std::find(g.groupCands.begin(), g.groupCands.end(), want) != g.groupCands.end()) g.xGroups = want;
           }
+          // SPFFT_GB300_BATCH_FWD_ROWS=r: forward chunks of r rows (r <= rowsB / 2 double-buffers
+          // them per row group)
+          if (const char* env = std::getenv("SPFFT_GB300_BATCH_FWD_ROWS")) {
+            const int want = std::atoi(env);
+            if (want >= g.xGroups && want <= g.rowsB) g.rowsF = want;
+          }
           break;
         }
       }

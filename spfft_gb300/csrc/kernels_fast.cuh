@@ -639,14 +639,14 @@ __device__ __forceinline__ void plane_forward_body(const PlanView<S>& p, const S
   plane_load_tables<S, A, NX, NY, R2C>(p, s);
 
   // Row chunks of plane z are contiguous in the space buffer. Each row group (RowGroups) takes its
-  // own rows in chunks of rows / groups. With one group and W holding two chunks (wRows >= 2 *
-  // rows), chunk i+1 streams into the other half while chunk i is transformed; otherwise each
-  // chunk is loaded after the previous one is done (other groups and blocks cover the wait).
+  // own rows in chunks of rows / groups. When W holds two chunks per group (wRows >= 2 * rows),
+  // each group streams its chunk i+1 into its other half while chunk i is transformed; otherwise
+  // each chunk is loaded after the previous one is done (other groups and blocks cover the wait).
   const CS* plane = reinterpret_cast<const CS*>(space + static_cast<size_t>(z) * NY * NX * (R2C ? 1 : 2));
   const RowGroups rg(groups);
   const int gRows = rows / groups;
-  const bool dbuf = groups == 1 && 2 * rows <= wRows;
-  CA* Wg = s.W + rg.g * gRows * L::WP;
+  const bool dbuf = 2 * rows <= wRows;
+  CA* Wg = s.W + rg.g * (dbuf ? 2 : 1) * gRows * L::WP;
   const int gBegin = rg.begin(NY), gEnd = rg.end(NY);
   const int nchunks = (gEnd - gBegin + gRows - 1) / gRows;
   auto issue_chunk = [&](int chunk) {
