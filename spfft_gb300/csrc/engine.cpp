@@ -364,6 +364,11 @@ GpuPlan<T>::GpuPlan(const IndexPlan& p, int device) {
   }
   numValues_ = nv;
 
+  if (const char* env = std::getenv("SPFFT_GB300_STAGED_CHUNKS")) {
+    const int want = std::atoi(env);
+    if (want >= 1 && want <= kMaxStagedChunks) stagedChunks_ = want;
+  }
+
   // Forward scaling factor T(1 / (Nx Ny Nz)) computed in double (execution_gpu.cpp:58-59).
   scale_ = static_cast<T>(1.0 / (static_cast<double>(p.dimX) * p.dimY * p.dimZ));
 }
@@ -530,10 +535,10 @@ bool GpuPlan<T>::forward_staged(const T* hostSpace, T* devSpace, T* values, bool
   if (planePath_ != PlanePath::Split || !aligned) return false;
   const PlanView<T> v = view(scratch);
   const size_t plane = static_cast<size_t>(base_.dimX) * base_.dimY * (base_.r2c ? 1 : 2);
-  const int nz = base_.dimZ, per = (nz + kStagedChunks - 1) / kStagedChunks;
+  const int nz = base_.dimZ, per = (nz + stagedChunks_ - 1) / stagedChunks_;
   // the copies overwrite devSpace: start them after the work already on `stream`
-  check_cuda(cudaEventRecord(events[kStagedChunks], stream));
-  check_cuda(cudaStreamWaitEvent(copyStream, events[kStagedChunks], 0));
+  check_cuda(cudaEventRecord(events[kMaxStagedChunks], stream));
+  check_cuda(cudaStreamWaitEvent(copyStream, events[kMaxStagedChunks], 0));
   FastArgs<T> a;
   a.plan = &v;
   a.stream = stream;
@@ -590,7 +595,7 @@ bool GpuPlan<T>::backward_staged(const T* values, T* devSpace, T* hostSpace, voi
   }
   check_launch(cudaGetLastError());
   const size_t plane = static_cast<size_t>(base_.dimX) * base_.dimY * (base_.r2c ? 1 : 2);
-  const int nz = base_.dimZ, per = (nz + kStagedChunks - 1) / kStagedChunks;
+  const int nz = base_.dimZ, per = (nz + stagedChunks_ - 1) / stagedChunks_;
   a.out = devSpace;
   // each chunk's y and x passes, then its copy back, which overlaps the next chunk's passes
   for (int c = 0, z0 = 0; z0 < nz; ++c, z0 += per) {
@@ -609,8 +614,8 @@ bool GpuPlan<T>::backward_staged(const T* values, T* devSpace, T* hostSpace, voi
                                cudaMemcpyDeviceToHost, copyStream));
   }
   // `stream` continues once every chunk is back in host memory
-  check_cuda(cudaEventRecord(events[kStagedChunks], copyStream));
-  check_cuda(cudaStreamWaitEvent(stream, events[kStagedChunks], 0));
+  check_cuda(cudaEventRecord(events[kMaxStagedChunks], copyStream));
+  check_cuda(cudaStreamWaitEvent(stream, events[kMaxStagedChunks], 0));
   return true;
 }
 

@@ -42,7 +42,10 @@ public:
   // chunk c back while the x pass of chunk c + 1 runs. `events` holds kStagedEvents events. Both
   // return false, doing nothing, when the plan has no split x pass (the caller then copies the
   // whole domain at once).
-  static constexpr int kStagedChunks = 8, kStagedEvents = kStagedChunks + 1;
+  // Chunks per staged transform: 8 by default, SPFFT_GB300_STAGED_CHUNKS=n (1 .. kMaxStagedChunks)
+  // at plan creation.
+  static constexpr int kMaxStagedChunks = 32, kStagedEvents = kMaxStagedChunks + 1;
+  int staged_chunks() const { return stagedChunks_; }
   bool forward_staged(const T* hostSpace, T* devSpace, T* values, bool scaled, void* scratch,
                       cudaStream_t stream, cudaStream_t copyStream, cudaEvent_t* events) const;
   bool backward_staged(const T* values, T* devSpace, T* hostSpace, void* scratch, cudaStream_t stream,
@@ -106,6 +109,7 @@ private:
   std::vector<std::pair<int, int>> fusedCands_;  // (rows, threads)
   std::vector<std::pair<int, int>> splitCands_;  // (cpb, rpb)
   int fastSpb_ = 0, fastRows_ = 0, splitCpb_ = 0, splitRpb_ = 0, fusedThreads_ = 512;
+  int stagedChunks_ = 8;
   ScratchLayout layout_{};
   T scale_ = T(1);
   int numValues_ = 0;
