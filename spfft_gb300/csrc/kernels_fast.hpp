@@ -80,14 +80,20 @@ template <typename T>
 bool fast_group_f(FastOp op, int n, bool r2c, const FastArgs<T>& args);
 template <typename T>
 bool fast_group_g(FastOp op, int n, bool r2c, const FastArgs<T>& args);
+template <typename T>
+bool fast_group_h(FastOp op, int n, bool r2c, const FastArgs<T>& args);
+template <typename T>
+bool fast_group_i(FastOp op, int n, bool r2c, const FastArgs<T>& args);
 
-// Lengths with specialised kernels: 12, 48, 60, 64, 72, 90, 96, 100, 108, 120, 128, 150, 160, 192.
+// Lengths with specialised kernels: 12, 48, 60, 64, 72, 90, 96, 100, 108, 120, 128, 144, 150, 160,
+// 180, 192, 240, 256.
 template <typename T>
 inline bool fast_dispatch(FastOp op, int n, bool r2c, const FastArgs<T>& args) {
   return fast_group_a<T>(op, n, r2c, args) || fast_group_b<T>(op, n, r2c, args) ||
          fast_group_c<T>(op, n, r2c, args) || fast_group_d<T>(op, n, r2c, args) ||
          fast_group_e<T>(op, n, r2c, args) || fast_group_f<T>(op, n, r2c, args) ||
-         fast_group_g<T>(op, n, r2c, args);
+         fast_group_g<T>(op, n, r2c, args) || fast_group_h<T>(op, n, r2c, args) ||
+         fast_group_i<T>(op, n, r2c, args);
 }
 
 }  // namespace gb300

@@ -78,7 +78,7 @@ def test_full_grids(lib, dtype, ttype, dims):
 @pytest.mark.parametrize("dtype", ["float64", "float32"])
 def test_largest_specialised_length(lib, dtype):
     """256^3 (the longest size-specialised length), R2C |k| <= 64 and C2C |k| <= 40, values in a
-    shuffled user order."""
+    shuffled user order, on the specialised kernels."""
     rng = np.random.default_rng(12)
     for ttype, radius in ((1, 64), (0, 40)):
         idx = sphere_indices(256, radius, r2c=(ttype == 1))
@@ -87,6 +87,11 @@ def test_largest_specialised_length(lib, dtype):
         if ttype == 1:
             vals[(idx == 0).all(axis=1)] = vals[(idx == 0).all(axis=1)].real
         oracle = pipeline.HostPipeline(ttype, 256, 256, 256, idx)
+        tr = sp.Transform(1, sp.SPFFT_PU_GPU, ttype, 256, 256, 256, len(idx), sp.SPFFT_INDEX_TRIPLETS, idx,
+                          dtype=dtype)
+        info = tr.path_info()
+        assert info["fast_z"] and (info["split_plane"] or info["fused_plane"]), info
+        del tr
         space, out = _run(dtype, ttype, (256, 256, 256), idx, vals)
         assert rel_l2(space, oracle.backward(vals)) <= TOL[dtype], ttype
         want = oracle.forward(space.astype(np.complex128 if ttype == 0 else np.float64))

@@ -365,7 +365,7 @@ def test_every_specialised_length(lib, dtype):
     (the FP32 R2C twiddle tables of N = 90 and 150 end on an 8-byte boundary)."""
     rng = np.random.default_rng(41)
     items = []
-    for n in (12, 48, 60, 64, 72, 90, 96, 100, 108, 120, 128, 150, 160, 192):
+    for n in (12, 48, 60, 64, 72, 90, 96, 100, 108, 120, 128, 144, 150, 160, 180, 192, 240, 256):
         for ttype in (0, 1):
             idx = sphere_indices(n, max(2, n // 6), r2c=(ttype == 1))
             vals = _values(rng, idx.shape[0])
