@@ -270,10 +270,10 @@ def test_kernel_paths_and_fallbacks(lib):
             fused = dtype == "float32" and dims == (192, 192, 192)
             assert info["fused_plane"] == fused and info["split_plane"] != fused, (dtype, dims, info)
             assert info["fast_z"] == (dims[2] in (12, 64, 100, 192)), (dtype, dims, info)
-    # 192^3 C2C |k| <= 48 FP64: 97 columns do not fit one block's shared memory -> generic planes
+    # 192^3 C2C |k| <= 48 FP64: 97 columns, a compact plane too large for a fused block -> split
     idx = sphere_indices(192, 48)
     tr = _transform("float64", 0, (192, 192, 192), idx)
-    assert tr.path_info()["fast_z"] and not tr.path_info()["fused_plane"]
+    assert tr.path_info()["fast_z"] and tr.path_info()["split_plane"], tr.path_info()
     vals = _values(rng, len(idx))
     oracle = pipeline.HostPipeline(0, 192, 192, 192, idx)
     out = torch.empty((192, 192, 192), dtype=torch.complex128, device="cuda")
