@@ -441,9 +441,10 @@ def measure_gpu(args, rank: int, world: int) -> dict:
     err = float(np.linalg.norm(got[sel] - want[sel]) / np.linalg.norm(want[sel]))
 
     batched = None if args.no_batched else measure_batched(args, args.workload, args.batch, "float32")
+    grad = None if args.no_batched else measure_grad(args)
 
     return {
-        "batched": batched,
+        "batched": batched, "grad": grad,
         "pairs_per_s": pairs_per_s, "ms_per_step": total_ms / args.steps, "wall_s": wall,
         "clocks": clocks.summary(), "roofline": roofline, "e2e": e2e,
         "pair_gbs": pair_gbs, "roundtrip_rel_l2": err, "cufft_dense": cufft,
@@ -496,6 +497,47 @@ def measure_cufft_dense(args, idx: np.ndarray, vals_h: np.ndarray, n: int, r2c: 
             ms += a.elapsed_time(b)
     return {"value": round(steps / (ms / 1e3), 2), "unit": UNIT, "library": "cuFFT through torch.fft",
             "form": "dense 3D grid: zero, scatter, inverse FFT, forward FFT, gather"}
+
+
+def measure_grad(args) -> dict:
+    """Differentiation leg: one gradient step of L = sum V |psi|^2 with psi = backward(c) on 96^3
+    C2C FP64 |k| <= 24 (c ~ N(0,1) complex, V ~ U(0,1) real), through the torch.autograd.Function
+    of spfft_gb300.autograd: the backward transform, the loss, and the gradient by the hand-written
+    adjoint (unnormalised forward transform + gather). Steps/s with CUDA events on the current
+    stream; inputs resident on the device."""
+    import torch
+
+    import spfft_gb300 as sp
+    from spfft_gb300 import autograd as ag
+
+    n, radius = 96, 24
+    idx = sphere_indices(n, radius, False)
+    tr = sp.Transform(1, sp.SPFFT_PU_GPU, sp.SPFFT_TRANS_C2C, n, n, n, len(idx), sp.SPFFT_INDEX_TRIPLETS, idx)
+    rng = np.random.default_rng(4)
+    c = torch.from_numpy(rng.standard_normal(len(idx)) + 1j * rng.standard_normal(len(idx))).cuda()
+    c.requires_grad_(True)
+    weight = torch.from_numpy(rng.uniform(0.0, 1.0, (n, n, n))).cuda()
+
+    def step():
+        psi = ag.backward(tr, c)
+        loss = (weight * (psi.real ** 2 + psi.imag ** 2)).sum()
+        (grad,) = torch.autograd.grad(loss, c)
+        return grad
+
+    for _ in range(max(3, args.warmup)):
+        step()
+    torch.cuda.synchronize()
+    steps = max(5, args.steps)
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    start.record()
+    for _ in range(steps):
+        step()
+    end.record()
+    torch.cuda.synchronize()
+    ms = start.elapsed_time(end) / steps
+    return {"workload": "c2c_96_sphere24 (57,777 values), L = sum V |backward(c)|^2, FP64",
+            "grad_steps_per_s": round(1e3 / ms, 1), "ms_per_step": round(ms, 4),
+            "step": "backward transform + loss + adjoint gradient (torch elementwise ops for the loss)"}
 
 
 def measure_batched(args, workload: str, batch: int, dtype: str, radii=None) -> dict:
@@ -925,6 +967,8 @@ def main() -> int:
     if res["batched"]:
         line["fp32_batched"] = res["batched"]
         line["fp32_batched"]["ratio_vs_value"] = round(res["batched"]["value"] / res["pairs_per_s"], 2)
+    if res["grad"]:
+        line["differentiation"] = res["grad"]
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_pairs_per_s(args.workload, args.cpu_seconds, 400)
         line["cpu_baseline"]["value"] = round(line["cpu_baseline"]["value"], 3)
