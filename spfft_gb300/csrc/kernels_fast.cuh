@@ -595,12 +595,12 @@ __device__ __forceinline__ void plane_backward_body(const PlanView<S>& p, S* __r
           const int col = s.colOf[kk];
           v[a] = col >= 0 ? prow[col] : czero<A>();
         } else {
-          v[a] = wrow[L::wpos(kk)];
+          v[a] = wrow[a * (Bx + L::PAD) + b];  // L::wpos(kk), b < Bx
         }
       }
       fft_pass1_regs<L::LX, +1>(v, b, twl);
 #pragma unroll
-      for (int k1 = 0; k1 < Ax; ++k1) wrow[L::wpos(k1 * Bx + b)] = v[k1];
+      for (int k1 = 0; k1 < Ax; ++k1) wrow[k1 * (Bx + L::PAD) + b] = v[k1];  // L::wpos(k1 * Bx + b)
     }
     rg.sync();
     for (int i = rg.t; i < nr * Ax; i += rg.threads) {
@@ -1165,7 +1165,7 @@ __device__ __forceinline__ void x_backward_body(const PlanView<S>& p, S* __restr
     }
     fft_pass1_regs<L::LX, +1>(v, b, twl);
 #pragma unroll
-    for (int k1 = 0; k1 < Ax; ++k1) wrow[L::wpos(k1 * Bx + b)] = v[k1];
+    for (int k1 = 0; k1 < Ax; ++k1) wrow[k1 * (Bx + L::PAD) + b] = v[k1];  // L::wpos(k1 * Bx + b)
   }
   __syncthreads();
   for (int i = threadIdx.x; i < nr * Ax; i += blockDim.x) {
