@@ -653,9 +653,15 @@ __device__ __forceinline__ void plane_forward_body(const PlanView<S>& p, const S
     const int r0 = gBegin + chunk * gRows, nr = min(gRows, gEnd - r0);
     CA* dst = Wg + (dbuf ? (chunk & 1) : 0) * gRows * L::WP;
     const CS* src = plane + static_cast<size_t>(r0) * L::LX;
-    for (int i = rg.t; i < nr * L::LX; i += rg.threads) {
-      const int rl = i / L::LX, e = i - rl * L::LX;
-      cp_async_c(dst + rl * L::WP + L::wpos(e), src + i);
+    if (rg.threads % L::LX == 0) {
+      // every thread keeps one row position: its padded slot is computed once
+      const int e = rg.t % L::LX, pe = L::wpos(e), step = rg.threads / L::LX;
+      for (int rl = rg.t / L::LX; rl < nr; rl += step) cp_async_c(dst + rl * L::WP + pe, src + rl * L::LX + e);
+    } else {
+      for (int i = rg.t; i < nr * L::LX; i += rg.threads) {
+        const int rl = i / L::LX, e = i - rl * L::LX;
+        cp_async_c(dst + rl * L::WP + L::wpos(e), src + i);
+      }
     }
     cp_async_commit();
   };
