@@ -150,6 +150,24 @@ struct RowGroups {
   __device__ __forceinline__ int end(int n) const { return (g + 1) * n / groups; }
 };
 
+// Walks the flat indices i = start, start + step, ... of a row-major [rows][len] range as (row r,
+// column c) pairs, one compare instead of one division per element.
+struct RowWalk {
+  int r, c;
+  int dr, dc, len;
+  __device__ __forceinline__ RowWalk(int start, int step, int len_)
+      : r(start / len_), c(start - (start / len_) * len_), dr(step / len_), dc(step - (step / len_) * len_),
+        len(len_) {}
+  __device__ __forceinline__ void next() {
+    r += dr;
+    c += dc;
+    if (c >= len) {
+      c -= len;
+      ++r;
+    }
+  }
+};
+
 // Division by a block-uniform runtime divisor d in [1, 2^16) for numerators n in [0, 2^16): one
 // high multiply by m = floor(2^32 / d) + 1 instead of the division sequence. Exact because
 // n * (m - 2^32 / d) < n * 1 < 2^32 / d, i.e. the error stays below one step of n / d.
@@ -1211,9 +1229,8 @@ __device__ __forceinline__ void x_forward_body(const PlanView<S>& p, const S* __
   pdl_wait();
   pdl_trigger();
   const CS* rows = reinterpret_cast<const CS*>(space + (static_cast<size_t>(z) * ny + y0) * NX * (R2C ? 1 : 2));
-  for (int i = threadIdx.x; i < nr * L::LX; i += blockDim.x) {
-    const int rl = i / L::LX, e = i - rl * L::LX;
-    cp_async_c(s.W + rl * L::WP + L::wpos(e), rows + i);
+  for (RowWalk w(threadIdx.x, blockDim.x, L::LX); w.r < nr; w.next()) {
+    cp_async_c(s.W + w.r * L::WP + L::wpos(w.c), rows + w.r * L::LX + w.c);
   }
   cp_async_commit();
   cp_async_wait<0>();
@@ -1221,9 +1238,8 @@ __device__ __forceinline__ void x_forward_body(const PlanView<S>& p, const S* __
   if (TT::kScaled) {
     // block scale from the thread's own copies, now in shared memory
     int e = 0;
-    for (int i = threadIdx.x; i < nr * L::LX; i += blockDim.x) {
-      const int rl = i / L::LX, el = i - rl * L::LX;
-      e = max(e, max_exponent(reinterpret_cast<const CS*>(s.W)[rl * L::WP + L::wpos(el)]));
+    for (RowWalk w(threadIdx.x, blockDim.x, L::LX); w.r < nr; w.next()) {
+      e = max(e, max_exponent(reinterpret_cast<const CS*>(s.W)[w.r * L::WP + L::wpos(w.c)]));
     }
     atomicMax(&sExp, e);
   }
