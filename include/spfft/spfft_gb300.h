@@ -146,6 +146,16 @@ SPFFT_EXPORT SpfftError spfft_gb300_float_transform_autotune(SpfftFloatTransform
 SPFFT_EXPORT SpfftError spfft_gb300_transform_tuning(SpfftTransform transform, int* tuning);
 SPFFT_EXPORT SpfftError spfft_gb300_float_transform_tuning(SpfftFloatTransform transform, int* tuning);
 
+/* The radix plans of the generic (runtime-radix) kernels for the z, y and x lengths: numStages[d]
+ * stages with radices radices[d * 24 + 0 .. numStages[d] - 1] (d = 0 z, 1 y, 2 x; 24 slots per
+ * length). The autotuner chooses among several plans for the lengths that run on the generic
+ * kernels (the default grouping of powers of two into radix 8, the reverse order, radix-4 and
+ * radix-2 stages); lengths with size-specialised kernels use a fixed two-pass split instead. */
+SPFFT_EXPORT SpfftError spfft_gb300_transform_radix_plans(SpfftTransform transform, int* numStages,
+                                                          int* radices);
+SPFFT_EXPORT SpfftError spfft_gb300_float_transform_radix_plans(SpfftFloatTransform transform,
+                                                                int* numStages, int* radices);
+
 /* ---- batched execution (no counterpart in the reference; the GB300 form of its multi-transform)
  * A batch holds many transforms (all double or all float, on distinct grids, same device). Each
  * pass of each group of equally shaped transforms runs as ONE kernel launch over all of them, so

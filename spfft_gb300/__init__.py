@@ -133,6 +133,7 @@ def _declare(lib: ctypes.CDLL) -> None:
         getattr(lib, prefix + "transform_path_info").argtypes = [_vp, _ip]
         getattr(lib, prefix + "transform_autotune").argtypes = [_vp, _i, ctypes.POINTER(ctypes.c_float)]
         getattr(lib, prefix + "transform_tuning").argtypes = [_vp, _ip]
+        getattr(lib, prefix + "transform_radix_plans").argtypes = [_vp, _ip, _ip]
         getattr(lib, prefix + "transform_adjoint_backward").argtypes = [_vp, _vp, _vp, _vp]
         getattr(lib, prefix + "transform_adjoint_forward").argtypes = [_vp, _vp, _vp, _i, _vp]
         getattr(lib, prefix + "transform_stage_times").argtypes = [_vp, _i, _vp, _vp, _i, _vp,
@@ -432,6 +433,12 @@ class Transform:
                 "fused_half_rows": v[2], "fused_threads": v[3], "columns_per_y_block": v[4],
                 "rows_per_x_block": v[5]}
 
+    def radix_plans(self) -> list:
+        """Radix stages of the generic kernels for the z, y and x lengths ([[...], [...], [...]])."""
+        stages = (ctypes.c_int * 3)()
+        radices = (ctypes.c_int * (3 * 24))()
+        _call("spfft_gb300_" + self._p[len("spfft_"):] + "transform_radix_plans", self._h, stages, radices)
+        return [[radices[d * 24 + i] for i in range(stages[d])] for d in range(3)]
     def set_stream(self, stream: Any) -> None:
         """Run every later call on this CUDA stream (torch.cuda.Stream, cudaStream_t int or None)."""
         ptr = None if stream is None else int(getattr(stream, "cuda_stream", stream))

@@ -261,6 +261,18 @@ SPFFT_GB300_GRID_C_API(spfft_float_grid_, GridFloat)
       tuning[5] = tu.rpb;                                                                         \
     });                                                                                           \
   }                                                                                               \
+  SpfftError GPREFIX##radix_plans(void* transform, int* numStages, int* radices) {                \
+    if (!numStages || !radices) return SPFFT_INVALID_PARAMETER_ERROR;                             \
+    return with_handle<spfft::TRANSFORM>(transform, [&](spfft::TRANSFORM& t) {                    \
+      const auto& plan = spfft::TransformAccess::get(t).gpu_plan();                               \
+      for (int d = 0; d < 3; ++d) {                                                               \
+        const spfft::gb300::RadixPlan r = plan.radix_plan(d);                                     \
+        numStages[d] = r.numStages;                                                               \
+        for (int i = 0; i < spfft::gb300::kMaxStages; ++i)                                        \
+          radices[d * spfft::gb300::kMaxStages + i] = i < r.numStages ? r.radix[i] : 0;           \
+      }                                                                                           \
+    });                                                                                           \
+  }                                                                                               \
   SpfftError GPREFIX##forward_device(void* transform, const T* space, T* values,                  \
                                      SpfftScalingType scaling, void* stream) {                    \
     return with_handle<spfft::TRANSFORM>(transform, [&](spfft::TRANSFORM& t) {                    \

@@ -333,9 +333,12 @@ GpuPlan<T>::GpuPlan(const IndexPlan& p, int device) {
     splitRpb_ = rpb;
   }
 
-  base_.fz = make_radix_plan(p.dimZ);
-  base_.fy = make_radix_plan(p.dimY);
-  base_.fx = make_radix_plan(p.dimX);
+  radixCands_[0] = radix_plan_candidates(p.dimZ);
+  radixCands_[1] = radix_plan_candidates(p.dimY);
+  radixCands_[2] = radix_plan_candidates(p.dimX);
+  base_.fz = radixCands_[0][0];
+  base_.fy = radixCands_[1][0];
+  base_.fx = radixCands_[2][0];
   base_.twz = reinterpret_cast<const T*>(d + parts[0].offset);
   base_.twy = reinterpret_cast<const T*>(d + parts[1].offset);
   base_.twx = reinterpret_cast<const T*>(d + parts[2].offset);
@@ -632,6 +635,7 @@ typename GpuPlan<T>::Tuning GpuPlan<T>::tuning() const {
     t.cpb = splitCpb_;
     t.rpb = splitRpb_;
   }
+  for (int d = 0; d < 3; ++d) t.radix[d] = radixChoice_[d];
   return t;
 }
 
@@ -673,7 +677,12 @@ void GpuPlan<T>::set_tuning(const Tuning& t) {
     ok |= c.spb == t.spb && c.path == t.path && c.fusedRows == t.fusedRows && c.fusedThreads == t.fusedThreads &&
           c.cpb == t.cpb && c.rpb == t.rpb;
   }
+  for (int d = 0; d < 3; ++d) ok &= t.radix[d] >= 0 && t.radix[d] < static_cast<int>(radixCands_[d].size());
   if (!ok) throw InvalidParameterError();
+  for (int d = 0; d < 3; ++d) radixChoice_[d] = t.radix[d];
+  base_.fz = radixCands_[0][t.radix[0]];
+  base_.fy = radixCands_[1][t.radix[1]];
+  base_.fx = radixCands_[2][t.radix[2]];
   if (t.spb > 0) fastSpb_ = t.spb;
   planePath_ = t.path == 1 ? PlanePath::Fused : t.path == 2 ? PlanePath::Split : PlanePath::Generic;
   if (t.path == 1) {
@@ -715,11 +724,29 @@ float GpuPlan<T>::autotune(T* values, T* space, void* scratch, cudaStream_t stre
     // z shapes with the current plane strategy, then plane strategies with the best z shape
     for (int pass = 0; pass < 2; ++pass) {
       const Tuning base = best;
-      for (const Tuning& c : candidates()) {
+      for (Tuning c : candidates()) {
         const bool zOnly = c.path == base.path && c.fusedRows == base.fusedRows &&
                            c.fusedThreads == base.fusedThreads && c.cpb == base.cpb && c.rpb == base.rpb;
         const bool planeOnly = c.spb == base.spb;
         if ((pass == 0 && !zOnly) || (pass == 1 && !planeOnly)) continue;
+        for (int d = 0; d < 3; ++d) c.radix[d] = base.radix[d];
+        const float ms = time_pair(c);
+        if (ms < bestMs) {
+          bestMs = ms;
+          best = c;
+        }
+      }
+    }
+    // radix plans of the lengths the generic kernels transform: z without specialised z kernels,
+    // y and x on the generic plane path
+    const bool generic[3] = {best.spb == 0, best.path == 0, best.path == 0};
+    for (int d = 0; d < 3; ++d) {
+      if (!generic[d]) continue;
+      const Tuning base = best;
+      for (int r = 0; r < static_cast<int>(radixCands_[d].size()); ++r) {
+        if (r == base.radix[d]) continue;
+        Tuning c = base;
+        c.radix[d] = r;
         const float ms = time_pair(c);
         if (ms < bestMs) {
           bestMs = ms;

@@ -73,7 +73,12 @@ public:
     int fusedRows = 0;     // fused: half of the x chunk buffer rows
     int fusedThreads = 0;  // fused: threads per block (256: two blocks per SM, 512: one)
     int cpb = 0, rpb = 0;  // split: columns per y block, rows per x block
+    int radix[3] = {0, 0, 0};  // generic kernels: radix plan of z, y, x (index into radix_plans())
   };
+  // Radix plans available to the generic kernels for the z, y and x lengths (dim 0, 1, 2), and
+  // the ones in use.
+  const std::vector<RadixPlan>& radix_plans(int dim) const { return radixCands_[dim]; }
+  RadixPlan radix_plan(int dim) const { return dim == 0 ? base_.fz : dim == 1 ? base_.fy : base_.fx; }
   Tuning tuning() const;
   // Every tuning this plan can run (all combinations of the valid z, fused and split shapes).
   std::vector<Tuning> candidates() const;
@@ -82,8 +87,9 @@ public:
   // Autotuner: times `reps` backward + scaled forward pairs per candidate on `values` / `space`
   // (device buffers of this plan's sizes, overwritten) on `stream`, first over the z shapes with
   // the current plane strategy, then over the plane strategies and tile shapes with the best z
-  // shape, and keeps the fastest. Returns its time per pair in milliseconds. No other work of
-  // this plan may run meanwhile.
+  // shape, then -- for the lengths that run on the generic kernels -- over their radix plans one
+  // length at a time, and keeps the fastest. Returns its time per pair in milliseconds. No other
+  // work of this plan may run meanwhile.
   float autotune(T* values, T* space, void* scratch, cudaStream_t stream, int reps);
 
   // Device view of this plan with its intermediates in `scratch` (used by batched execution).
@@ -110,6 +116,8 @@ private:
   std::vector<std::pair<int, int>> splitCands_;  // (cpb, rpb)
   int fastSpb_ = 0, fastRows_ = 0, splitCpb_ = 0, splitRpb_ = 0, fusedThreads_ = 512;
   int stagedChunks_ = 8;
+  std::vector<RadixPlan> radixCands_[3];
+  int radixChoice_[3] = {0, 0, 0};
   ScratchLayout layout_{};
   T scale_ = T(1);
   int numValues_ = 0;

@@ -69,6 +69,48 @@ inline RadixPlan make_radix_plan(int n) {
   return p;
 }
 
+// Radix plans the autotuner may choose from for the generic (runtime-radix) kernels, the default of
+// make_radix_plan first; then the same stages in reverse order, the powers of two as radix-4 stages
+// (and one radix 2), and for at most ten factors of two radix-2 stages only -- each followed by
+// the odd factors in the default order. Every plan's radices multiply to n; duplicates are dropped.
+inline std::vector<RadixPlan> radix_plan_candidates(int n) {
+  std::vector<RadixPlan> out;
+  auto add = [&](const std::vector<int>& r) {
+    if (static_cast<int>(r.size()) > kMaxStages) return;
+    RadixPlan p;
+    p.n = n;
+    p.numStages = static_cast<int>(r.size());
+    for (int i = 0; i < p.numStages; ++i) p.radix[i] = r[i];
+    for (const RadixPlan& q : out) {
+      bool same = q.numStages == p.numStages;
+      for (int i = 0; same && i < p.numStages; ++i) same = q.radix[i] == p.radix[i];
+      if (same) return;
+    }
+    out.push_back(p);
+  };
+  const RadixPlan d = make_radix_plan(n);
+  std::vector<int> def(d.radix, d.radix + d.numStages);
+  add(def);
+  add(std::vector<int>(def.rbegin(), def.rend()));
+  int twos = 0;
+  for (int m = n; m > 1 && m % 2 == 0; m /= 2) ++twos;
+  std::vector<int> odd;
+  for (int r : def)
+    if (r % 2 != 0) odd.push_back(r);
+  if (twos > 0) {
+    std::vector<int> fours(static_cast<size_t>(twos / 2), 4);
+    if (twos % 2) fours.push_back(2);
+    fours.insert(fours.end(), odd.begin(), odd.end());
+    add(fours);
+    if (twos <= 10) {
+      std::vector<int> pairs(static_cast<size_t>(twos), 2);
+      pairs.insert(pairs.end(), odd.begin(), odd.end());
+      add(pairs);
+    }
+  }
+  return out;
+}
+
 // exp(-2 pi i m / n) for m in [0, n), as (cos, sin) pairs in double precision.
 inline std::vector<double> make_twiddles(int n) {
   std::vector<double> w(2 * static_cast<size_t>(n > 0 ? n : 1));

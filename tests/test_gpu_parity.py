@@ -420,6 +420,34 @@ def test_autotune_keeps_results(lib, dtype):
 
 
 @pytest.mark.parametrize("dtype", ["float64", "float32"])
+def test_autotuned_radix_plans_on_generic_lengths(lib, dtype):
+    """Lengths without specialised kernels run the runtime-radix kernels; the autotuner picks one
+    of several radix plans per length (products equal the length) and the results stay those of
+    the oracle, for every plan of every length forced through the plane strategy 'generic'."""
+    rng = np.random.default_rng(47)
+    for dims, ttype in [((40, 54, 45), 0), ((32, 36, 50), 1), ((11, 13, 7), 0)]:
+        idx = random_indices(rng, *dims, r2c=(ttype == 1))
+        tr = _transform(dtype, ttype, dims, idx)
+        assert tr.tuning()["plane"] == "generic"
+        ms = tr.autotune(2)
+        plans = tr.radix_plans()
+        assert ms > 0
+        for d, n in zip((2, 1, 0), dims):  # plans are (z, y, x)
+            assert int(np.prod(plans[d])) == n, (dims, plans)
+        vals = _values(rng, idx.shape[0])
+        oracle = pipeline.HostPipeline(ttype, *dims, idx)
+        v = torch.from_numpy(vals).to(CT[dtype]).cuda()
+        out = torch.empty(dims[::-1], dtype=CT[dtype] if ttype == 0 else RT[dtype], device="cuda")
+        tr.backward(v, out)
+        want = oracle.backward(vals)
+        assert rel_l2(out.cpu().numpy(), want) <= TOL[dtype], (dims, plans)
+        f = torch.empty_like(v)
+        tr.forward(out, f)
+        assert rel_l2(f.cpu().numpy(), oracle.forward(out.cpu().numpy().astype(
+            np.complex128 if ttype == 0 else np.float64))) <= TOL[dtype], (dims, plans)
+
+
+@pytest.mark.parametrize("dtype", ["float64", "float32"])
 def test_reference_pipeline_golden(lib, dtype):
     """The library against golden vectors of the reference's OWN host transform path (run on the
     inputs of its local test suite, FP64; tests/golden/make_golden.py): C2C backward then forward,
