@@ -129,11 +129,11 @@ __host__ __device__ __forceinline__ void Dft<R, SIGN>::run(C* v) {
 // k1): DFT_B over b; the result X[k1 + A*k2] is left in registers (v[k2]) for the caller, which
 // either emits it or stores it back in place at buf[(k1*B + k2) * stride] -- the "transposed"
 // order, where X[k] lives at position (k mod A)*B + k div A. tw is the w_N table (forward sign).
-template <int N>
-struct Shape;  // N = A * B
+template <int N, int V = 0>
+struct Shape;  // N = A * B; V = 1 selects the split of the z and split-y kernels
 #define SPFFT_GB300_SHAPE(N_, A_, B_)        \
   template <>                              \
-  struct Shape<N_> {                       \
+  struct Shape<N_, 0> {                    \
     static constexpr int A = A_, B = B_;   \
   };
 SPFFT_GB300_SHAPE(3, 3, 1)
@@ -169,17 +169,26 @@ SPFFT_GB300_SHAPE(192, 16, 12)
 SPFFT_GB300_SHAPE(240, 16, 15)
 SPFFT_GB300_SHAPE(256, 16, 16)
 #undef SPFFT_GB300_SHAPE
+// Variant 1 is variant 0 except where another split measured faster in the z and split y kernels
+// (192 = 12 x 16 there: FP64 y backward 39.6 -> 35.5 us, FP32 batched z passes 4-6 % faster; the
+// fused plane kernels keep 16 x 12, which they run faster).
+template <int N>
+struct Shape<N, 1> : Shape<N, 0> {};
+template <>
+struct Shape<192, 1> {
+  static constexpr int A = 12, B = 16;
+};
 
 // Position of X[k] after pass 2 stored back in place.
-template <int N>
+template <int N, int V = 0>
 __host__ __device__ __forceinline__ int transposed_pos(int k) {
-  constexpr int A = Shape<N>::A, B = Shape<N>::B;
+  constexpr int A = Shape<N, V>::A, B = Shape<N, V>::B;
   return (k % A) * B + k / A;
 }
 
-template <int N, int SIGN, typename C>
+template <int N, int SIGN, int V = 0, typename C>
 __host__ __device__ __forceinline__ void fft_pass1(C* buf, int stride, int b, const C* __restrict__ tw) {
-  constexpr int A = Shape<N>::A, B = Shape<N>::B;
+  constexpr int A = Shape<N, V>::A, B = Shape<N, V>::B;
   C v[A];
 #pragma unroll
   for (int a = 0; a < A; ++a) v[a] = buf[(a * B + b) * stride];
@@ -193,9 +202,9 @@ __host__ __device__ __forceinline__ void fft_pass1(C* buf, int stride, int b, co
 }
 
 // Pass 1 with the inputs already in registers (loaded by the caller from elsewhere).
-template <int N, int SIGN, typename C>
-__host__ __device__ __forceinline__ void fft_pass1_regs(C (&v)[Shape<N>::A], int b, const C* __restrict__ tw) {
-  constexpr int A = Shape<N>::A, B = Shape<N>::B;
+template <int N, int SIGN, int V = 0, typename C>
+__host__ __device__ __forceinline__ void fft_pass1_regs(C (&v)[Shape<N, V>::A], int b, const C* __restrict__ tw) {
+  constexpr int A = Shape<N, V>::A, B = Shape<N, V>::B;
   Dft<A, SIGN>::run(v);
   if (B > 1) {
 #pragma unroll
@@ -203,9 +212,9 @@ __host__ __device__ __forceinline__ void fft_pass1_regs(C (&v)[Shape<N>::A], int
   }
 }
 
-template <int N, int SIGN, typename C>
-__host__ __device__ __forceinline__ void fft_pass2(const C* buf, int stride, int k1, C (&v)[Shape<N>::B]) {
-  constexpr int B = Shape<N>::B;
+template <int N, int SIGN, int V = 0, typename C>
+__host__ __device__ __forceinline__ void fft_pass2(const C* buf, int stride, int k1, C (&v)[Shape<N, V>::B]) {
+  constexpr int B = Shape<N, V>::B;
 #pragma unroll
   for (int b = 0; b < B; ++b) v[b] = buf[(k1 * B + b) * stride];
   Dft<B, SIGN>::run(v);

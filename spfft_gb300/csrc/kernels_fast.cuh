@@ -256,7 +256,7 @@ __device__ __forceinline__ void z_backward_body(const PlanView<S>& p, const S* _
   using TT = Types<S, A>;
   using CS = typename TT::CS;
   using CA = typename TT::CA;
-  constexpr int Az = Shape<NZ>::A, Bz = Shape<NZ>::B, PZ = ZLayout<NZ>::pitch;
+  constexpr int Az = Shape<NZ, 1>::A, Bz = Shape<NZ, 1>::B, PZ = ZLayout<NZ>::pitch;
   int& sExp = *sExpPtr;
   CA* tw = reinterpret_cast<CA*>(g_fast_smem);
   CA* buf = tw + NZ;
@@ -300,7 +300,7 @@ __device__ __forceinline__ void z_backward_body(const PlanView<S>& p, const S* _
 
   for (int i = threadIdx.x; i < nsb * Bz; i += blockDim.x) {
     const int sl = i / Bz, b = i - sl * Bz;
-    fft_pass1<NZ, +1>(buf + sl * PZ, 1, b, tw);
+    fft_pass1<NZ, +1, 1>(buf + sl * PZ, 1, b, tw);
   }
   __syncthreads();
   CS* sticks = reinterpret_cast<CS*>(p.sticks) + s0;
@@ -308,7 +308,7 @@ __device__ __forceinline__ void z_backward_body(const PlanView<S>& p, const S* _
   for (int i = threadIdx.x; i < nsb * Az; i += blockDim.x) {
     const int k1 = dns.div(i), sl = i - k1 * nsb;
     CA v[Bz];
-    fft_pass2<NZ, +1>(buf + sl * PZ, 1, k1, v);
+    fft_pass2<NZ, +1, 1>(buf + sl * PZ, 1, k1, v);
     if (raw) {
       CA* rs = reinterpret_cast<CA*>(sticks);
 #pragma unroll
@@ -336,7 +336,7 @@ __device__ __forceinline__ void z_forward_body(const PlanView<S>& p, S* __restri
   using TT = Types<S, A>;
   using CS = typename TT::CS;
   using CA = typename TT::CA;
-  constexpr int Az = Shape<NZ>::A, Bz = Shape<NZ>::B, PZ = ZLayout<NZ>::pitch;
+  constexpr int Az = Shape<NZ, 1>::A, Bz = Shape<NZ, 1>::B, PZ = ZLayout<NZ>::pitch;
   int& sExp = *sExpPtr;
   CA* tw = reinterpret_cast<CA*>(g_fast_smem);
   CA* buf = tw + NZ;
@@ -386,13 +386,13 @@ __device__ __forceinline__ void z_forward_body(const PlanView<S>& p, S* __restri
   }
   for (int i = threadIdx.x; i < nsb * Bz; i += blockDim.x) {
     const int sl = i / Bz, b = i - sl * Bz;
-    fft_pass1<NZ, -1>(buf + sl * PZ, 1, b, tw);
+    fft_pass1<NZ, -1, 1>(buf + sl * PZ, 1, b, tw);
   }
   __syncthreads();
   for (int i = threadIdx.x; i < nsb * Az; i += blockDim.x) {
     const int k1 = dns.div(i), sl = i - k1 * nsb;
     CA v[Bz];
-    fft_pass2<NZ, -1>(buf + sl * PZ, 1, k1, v);
+    fft_pass2<NZ, -1, 1>(buf + sl * PZ, 1, k1, v);
 #pragma unroll
     for (int k2 = 0; k2 < Bz; ++k2) buf[sl * PZ + k1 * Bz + k2] = v[k2];
   }
@@ -403,7 +403,7 @@ __device__ __forceinline__ void z_forward_body(const PlanView<S>& p, S* __restri
   for (int e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
     const int pos = p.entryPos[e] - base;
     const int sl = pos / NZ;
-    CS v = to_storage(buf[sl * PZ + transposed_pos<NZ>(pos - sl * NZ)], k);
+    CS v = to_storage(buf[sl * PZ + transposed_pos<NZ, 1>(pos - sl * NZ)], k);
     // scaling multiplies by S(1 / (Nx Ny Nz)) in S, like compress_kernel_scaled
     // (compression_kernels.cu:106-128)
     if (scale != S(0)) v = cscale(v, scale);
@@ -882,7 +882,7 @@ __device__ __forceinline__ void y_backward_body(const PlanView<S>& p, int cpb, i
   using TT = Types<S, A>;
   using CS = typename TT::CS;
   using CA = typename TT::CA;
-  constexpr int Ay = Shape<NY>::A, By = Shape<NY>::B;
+  constexpr int Ay = Shape<NY, 1>::A, By = Shape<NY, 1>::B;
   int& sExp = *sExpPtr;
   CA* tw = reinterpret_cast<CA*>(g_fast_smem);
   CA* buf = tw + NY;
@@ -953,7 +953,7 @@ __device__ __forceinline__ void y_backward_body(const PlanView<S>& p, int cpb, i
   if (p.r2c && c0 == 0 && p.columnX[0] == 0) line_fill(buf, NY, ncb);
   for (int i = threadIdx.x; i < ncb * By; i += blockDim.x) {
     const int b = dncb.div(i), c = i - b * ncb;
-    fft_pass1<NY, +1>(buf + c, ncb, b, tw);
+    fft_pass1<NY, +1, 1>(buf + c, ncb, b, tw);
   }
   __syncthreads();
   CS* planes = reinterpret_cast<CS*>(p.planes) + static_cast<size_t>(z) * NY * nc + c0;
@@ -961,7 +961,7 @@ __device__ __forceinline__ void y_backward_body(const PlanView<S>& p, int cpb, i
   for (int i = threadIdx.x; i < ncb * Ay; i += blockDim.x) {
     const int k1 = dncb.div(i), c = i - k1 * ncb;
     CA v[By];
-    fft_pass2<NY, +1>(buf + c, ncb, k1, v);
+    fft_pass2<NY, +1, 1>(buf + c, ncb, k1, v);
     if (raw) {
       CA* rp = reinterpret_cast<CA*>(planes);
 #pragma unroll
@@ -987,7 +987,7 @@ __device__ __forceinline__ void y_forward_body(const PlanView<S>& p, int cpb, in
   using TT = Types<S, A>;
   using CS = typename TT::CS;
   using CA = typename TT::CA;
-  constexpr int Ay = Shape<NY>::A, By = Shape<NY>::B;
+  constexpr int Ay = Shape<NY, 1>::A, By = Shape<NY, 1>::B;
   int& sExp = *sExpPtr;
   CA* tw = reinterpret_cast<CA*>(g_fast_smem);
   CA* buf = tw + NY;
@@ -1032,13 +1032,13 @@ __device__ __forceinline__ void y_forward_body(const PlanView<S>& p, int cpb, in
   }
   for (int i = threadIdx.x; i < ncb * By; i += blockDim.x) {
     const int b = dncb.div(i), c = i - b * ncb;
-    fft_pass1<NY, -1>(buf + c, ncb, b, tw);
+    fft_pass1<NY, -1, 1>(buf + c, ncb, b, tw);
   }
   __syncthreads();
   for (int i = threadIdx.x; i < ncb * Ay; i += blockDim.x) {
     const int k1 = dncb.div(i), c = i - k1 * ncb;
     CA v[By];
-    fft_pass2<NY, -1>(buf + c, ncb, k1, v);
+    fft_pass2<NY, -1, 1>(buf + c, ncb, k1, v);
 #pragma unroll
     for (int k2 = 0; k2 < By; ++k2) buf[(k1 * By + k2) * ncb + c] = v[k2];
   }
@@ -1057,7 +1057,7 @@ __device__ __forceinline__ void y_forward_body(const PlanView<S>& p, int cpb, in
     for (int u = 0; u < 4; ++u) {
       if (pos[u] >= 0) {
         const int y = dnc.div(pos[u]), c = pos[u] - y * nc;
-        const CA v = buf[transposed_pos<NY>(y) * ncb + (c - c0)];
+        const CA v = buf[transposed_pos<NY, 1>(y) * ncb + (c - c0)];
         if (raw) reinterpret_cast<CA*>(sticks)[st0 + u * blockDim.x] = v;
         else sticks[st0 + u * blockDim.x] = to_storage(v, k);
       }
