@@ -169,9 +169,10 @@ SPFFT_GB300_SHAPE(192, 16, 12)
 SPFFT_GB300_SHAPE(240, 16, 15)
 SPFFT_GB300_SHAPE(256, 16, 16)
 #undef SPFFT_GB300_SHAPE
-// Variant 1 is variant 0 except where another split measured faster in the z and split y kernels
-// (192 = 12 x 16 there: FP64 y backward 39.6 -> 35.5 us, FP32 batched z passes 4-6 % faster; the
-// fused plane kernels keep 16 x 12, which they run faster).
+// Variant 1 is variant 0 except where another split measured faster: 192 = 12 x 16 in the z
+// kernels, the split y kernels and the y pass of the fused backward plane kernel (FP64 y backward
+// 39.6 -> 35.5 us, FP32 batched z passes 4-6 % and fused backward 1 % faster); the fused forward
+// plane kernel keeps 16 x 12, which it runs 4 % faster.
 template <int N>
 struct Shape<N, 1> : Shape<N, 0> {};
 template <>

@@ -539,7 +539,7 @@ __device__ __forceinline__ void plane_backward_body(const PlanView<S>& p, S* __r
   using CS = typename TT::CS;
   using CA = typename TT::CA;
   using L = PlaneLayout<NX, NY, R2C>;
-  constexpr int Ay = Shape<NY>::A, By = Shape<NY>::B;
+  constexpr int Ay = Shape<NY, 1>::A, By = Shape<NY, 1>::B;
   constexpr int Ax = L::Ax, Bx = L::Bx;
   int& sExp = *sExpPtr;
   const int nc = p.numColumns;
@@ -576,13 +576,13 @@ __device__ __forceinline__ void plane_backward_body(const PlanView<S>& p, S* __r
   // y-FFT on every compact column, result rows left in transposed order
   for (int i = threadIdx.x; i < nc * By; i += blockDim.x) {
     const int b = dnc.div(i), c = i - b * nc;
-    fft_pass1<NY, +1>(s.P + c, nc, b, s.twy);
+    fft_pass1<NY, +1, 1>(s.P + c, nc, b, s.twy);
   }
   __syncthreads();
   for (int i = threadIdx.x; i < nc * Ay; i += blockDim.x) {
     const int k1 = dnc.div(i), c = i - k1 * nc;
     CA v[By];
-    fft_pass2<NY, +1>(s.P + c, nc, k1, v);
+    fft_pass2<NY, +1, 1>(s.P + c, nc, k1, v);
 #pragma unroll
     for (int k2 = 0; k2 < By; ++k2) s.P[(k1 * By + k2) * nc + c] = v[k2];
   }
@@ -597,13 +597,13 @@ __device__ __forceinline__ void plane_backward_body(const PlanView<S>& p, S* __r
   for (int r0 = rg.begin(NY); r0 < rEnd; r0 += gRows) {
     const int nr = min(gRows, rEnd - r0);
     if (R2C) {
-      c2r_pack_rows<L>([&](int rl) { return s.P + transposed_pos<NY>(r0 + rl) * nc; }, nr, W, s.colOf, s.twx,
+      c2r_pack_rows<L>([&](int rl) { return s.P + transposed_pos<NY, 1>(r0 + rl) * nc; }, nr, W, s.colOf, s.twx,
                        rg.t, rg.threads);
       rg.sync();
     }
     for (int i = rg.t; i < nr * Bx; i += rg.threads) {
       const int rl = i / Bx, b = i - rl * Bx;
-      const CA* prow = s.P + transposed_pos<NY>(r0 + rl) * nc;
+      const CA* prow = s.P + transposed_pos<NY, 1>(r0 + rl) * nc;
       CA* wrow = W + rl * L::WP;
       CA v[Ax];
 #pragma unroll
