@@ -126,8 +126,8 @@ SpfftError spfft_gb300_batch_info(SpfftGb300Batch batch, int* numGroups, int* nu
 }
 
 SpfftError spfft_gb300_batch_autotune(SpfftGb300Batch batch, int repetitions, void* stream, float* msPerPair) {
-  if (repetitions < 1) return SPFFT_INVALID_PARAMETER_ERROR;
   return with_batch(batch, [&](BatchHandle& h) {
+    if (repetitions < 1) throw spfft::InvalidParameterError();
     const float ms = h.d ? h.d->autotune(static_cast<cudaStream_t>(stream), repetitions)
                          : h.f->autotune(static_cast<cudaStream_t>(stream), repetitions);
     if (msPerPair) *msPerPair = ms;

@@ -243,8 +243,8 @@ SPFFT_GB300_GRID_C_API(spfft_float_grid_, GridFloat)
     });                                                                                           \
   }                                                                                               \
   SpfftError GPREFIX##autotune(void* transform, int repetitions, float* msPerPair) {              \
-    if (repetitions < 1) return SPFFT_INVALID_PARAMETER_ERROR;                                    \
     return with_handle<spfft::TRANSFORM>(transform, [&](spfft::TRANSFORM& t) {                    \
+      if (repetitions < 1) throw spfft::InvalidParameterError();                                  \
       const float ms = spfft::TransformAccess::get(t).autotune(repetitions);                      \
       if (msPerPair) *msPerPair = ms;                                                             \
     });                                                                                           \

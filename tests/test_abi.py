@@ -55,3 +55,42 @@ def test_cpp_classes_are_exported(lib):
                 "spfft::TransformFloat::forward(float const*, float*, SpfftScalingType)",
                 "spfft::multi_transform_backward(int, spfft::Transform*, double const* const*, double* const*)"]:
         assert sym in out, sym
+
+
+HANDLE_TYPES = ("SpfftGrid", "SpfftFloatGrid", "SpfftTransform", "SpfftFloatTransform", "SpfftGb300Batch")
+
+
+def handle_functions() -> list:
+    """(name, [parameter declarations]) of every declared C function whose first parameter is a
+    grid, transform or batch handle passed by value."""
+    out = []
+    for h in INCLUDE.glob("*.h"):
+        text = re.sub(r"/\*.*?\*/", "", h.read_text(), flags=re.S)
+        for name, params in re.findall(r"SPFFT_EXPORT\s+SpfftError\s+(\w+)\s*\(([^)]*)\)", text):
+            ps = [p.strip() for p in params.split(",") if p.strip()]
+            if ps and ps[0].split()[0] in HANDLE_TYPES and "*" not in ps[0]:
+                out.append((name, ps))
+    return out
+
+
+def test_null_handle_is_rejected_by_every_handle_function(lib):
+    """Every C function taking a handle returns SPFFT_INVALID_HANDLE_ERROR for a null handle
+    (transform.cpp:245-258 of the reference), before touching its other arguments, which here
+    point at a zeroed buffer."""
+    import ctypes
+
+    scratch = (ctypes.c_char * 4096)()
+    fns = handle_functions()
+    assert len(fns) >= 60, len(fns)
+    wrong = {}
+    for name, params in fns:
+        fn = getattr(lib, name)
+        args = [None]
+        for p in params[1:]:
+            args.append(ctypes.cast(scratch, ctypes.c_void_p) if "*" in p else 0)
+        fn.argtypes = [ctypes.c_void_p] + [ctypes.c_void_p if "*" in p else ctypes.c_int for p in params[1:]]
+        fn.restype = ctypes.c_int
+        code = fn(*args)
+        if code != sp.ErrorCode.SPFFT_INVALID_HANDLE_ERROR:
+            wrong[name] = code
+    assert not wrong, wrong
