@@ -135,15 +135,15 @@ SpfftError spfft_gb300_batch_autotune(SpfftGb300Batch batch, int repetitions, vo
 }
 
 SpfftError spfft_gb300_batch_transform_path(SpfftGb300Batch batch, int index, int* path) {
-  if (!path) return SPFFT_INVALID_PARAMETER_ERROR;
   return with_batch(batch, [&](BatchHandle& h) {
+    if (!path) throw spfft::InvalidParameterError();
     *path = h.d ? h.d->transform_path(index) : h.f->transform_path(index);
   });
 }
 
 SpfftError spfft_gb300_batch_row_groups(SpfftGb300Batch batch, int index, int* groups) {
-  if (!groups) return SPFFT_INVALID_PARAMETER_ERROR;
   return with_batch(batch, [&](BatchHandle& h) {
+    if (!groups) throw spfft::InvalidParameterError();
     *groups = h.d ? h.d->row_groups(index) : h.f->row_groups(index);
   });
 }
@@ -156,8 +156,8 @@ SpfftError spfft_gb300_multi_batched_calls(long long* count) {
 
 SpfftError spfft_gb300_batch_stage_times(SpfftGb300Batch batch, int direction, SpfftScalingType scaling,
                                          void* stream, float* stageMs) {
-  if (!stageMs || (direction != 0 && direction != 1)) return SPFFT_INVALID_PARAMETER_ERROR;
   return with_batch(batch, [&](BatchHandle& h) {
+    if (!stageMs || (direction != 0 && direction != 1)) throw spfft::InvalidParameterError();
     const bool s = scaling == SPFFT_FULL_SCALING;
     if (h.d) h.d->stage_times(direction, s, static_cast<cudaStream_t>(stream), stageMs);
     else h.f->stage_times(direction, s, static_cast<cudaStream_t>(stream), stageMs);

@@ -215,8 +215,8 @@ SPFFT_GB300_GRID_C_API(spfft_float_grid_, GridFloat)
   }                                                                                               \
   SpfftError GPREFIX##stage_times(void* transform, int direction, const T* input, T* output,     \
                                   SpfftScalingType scaling, void* stream, float* stageMs) {       \
-    if (!stageMs || (direction != 0 && direction != 1)) return SPFFT_INVALID_PARAMETER_ERROR;     \
     return with_handle<spfft::TRANSFORM>(transform, [&](spfft::TRANSFORM& t) {                    \
+      if (!stageMs || (direction != 0 && direction != 1)) throw spfft::InvalidParameterError();   \
       spfft::TransformAccess::get(t).stage_times(direction, input, output,                        \
                                                  scaling == SPFFT_FULL_SCALING,                   \
                                                  static_cast<cudaStream_t>(stream), stageMs);     \
@@ -250,8 +250,8 @@ SPFFT_GB300_GRID_C_API(spfft_float_grid_, GridFloat)
     });                                                                                           \
   }                                                                                               \
   SpfftError GPREFIX##tuning(void* transform, int* tuning) {                                      \
-    if (!tuning) return SPFFT_INVALID_PARAMETER_ERROR;                                            \
     return with_handle<spfft::TRANSFORM>(transform, [&](spfft::TRANSFORM& t) {                    \
+      if (!tuning) throw spfft::InvalidParameterError();                                          \
       const auto tu = spfft::TransformAccess::get(t).gpu_plan().tuning();                         \
       tuning[0] = tu.spb;                                                                         \
       tuning[1] = tu.path;                                                                        \
@@ -262,8 +262,8 @@ SPFFT_GB300_GRID_C_API(spfft_float_grid_, GridFloat)
     });                                                                                           \
   }                                                                                               \
   SpfftError GPREFIX##radix_plans(void* transform, int* numStages, int* radices) {                \
-    if (!numStages || !radices) return SPFFT_INVALID_PARAMETER_ERROR;                             \
     return with_handle<spfft::TRANSFORM>(transform, [&](spfft::TRANSFORM& t) {                    \
+      if (!numStages || !radices) throw spfft::InvalidParameterError();                           \
       const auto& plan = spfft::TransformAccess::get(t).gpu_plan();                               \
       for (int d = 0; d < 3; ++d) {                                                               \
         const spfft::gb300::RadixPlan r = plan.radix_plan(d);                                     \

@@ -85,12 +85,11 @@ def test_null_handle_is_rejected_by_every_handle_function(lib):
     wrong = {}
     for name, params in fns:
         fn = getattr(lib, name)
-        args = [None]
-        for p in params[1:]:
-            args.append(ctypes.cast(scratch, ctypes.c_void_p) if "*" in p else 0)
         fn.argtypes = [ctypes.c_void_p] + [ctypes.c_void_p if "*" in p else ctypes.c_int for p in params[1:]]
         fn.restype = ctypes.c_int
-        code = fn(*args)
-        if code != sp.ErrorCode.SPFFT_INVALID_HANDLE_ERROR:
-            wrong[name] = code
+        # other pointers valid or null, other integers 0 or 1: the handle is checked first
+        for ptr, num in ((ctypes.cast(scratch, ctypes.c_void_p), 0), (None, 1)):
+            code = fn(None, *[ptr if "*" in p else num for p in params[1:]])
+            if code != sp.ErrorCode.SPFFT_INVALID_HANDLE_ERROR:
+                wrong[name] = code
     assert not wrong, wrong
