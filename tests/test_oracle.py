@@ -68,6 +68,7 @@ def test_oracle_pipeline_matches_dense_on_reference_cases(t):
 
 
 @pytest.mark.skipif(not ref.available(), reason="reference sources not present (built by oracle/Makefile)")
+@pytest.mark.skipif(not ref.available(), reason="reference index code not built here")
 def test_oracle_indices_match_reference_binary_random():
     rng = np.random.default_rng(3)
     for trial in range(40):

@@ -6,6 +6,7 @@ import numpy as np
 import pytest
 
 import spfft_gb300 as sp
+from oracle import ref
 from util import load_npz_group, random_indices
 
 
@@ -114,3 +115,35 @@ def test_allocation_failure_hook_countdown(lib):
     assert sp.inject_allocation_failure(-1) == 2
     with pytest.raises(sp.SpfftError):
         sp.inject_allocation_failure(-2)
+
+
+@pytest.mark.skipif(not ref.available(), reason="reference index code not built here")
+def test_library_planner_matches_reference_planner_on_random_sets(lib):
+    """The library's planner against the reference's own (spfft::Parameters, compiled from its
+    sources into oracle/_ref) on random index sets: plain and centered, C2C and R2C, shuffled, with
+    duplicated triplets and with out-of-range indices -- bit-exact, or the same error code."""
+    rng = np.random.default_rng(29)
+    checked = errors = 0
+    for trial in range(160):
+        t = trial % 2
+        dx, dy, dz = (int(v) for v in rng.integers(1, 24, 3))
+        idx = random_indices(rng, dx, dy, dz, t == 1, 0.5, 0.5, centered=bool((trial // 2) % 2))
+        if len(idx) and trial % 5 == 0:
+            idx = np.concatenate([idx, idx[rng.integers(0, len(idx), 3)]])
+        if len(idx) and trial % 7 == 0:
+            idx = idx.copy()
+            idx[int(rng.integers(0, len(idx))), int(rng.integers(0, 3))] = int(rng.choice([dx, -dx, dy + 5]))
+        idx = np.ascontiguousarray(idx[rng.permutation(len(idx))].astype(np.int32))
+        r = ref.plan(t, dx, dy, dz, idx)
+        if "error" in r:
+            with pytest.raises(sp.SpfftError) as e:
+                sp.plan_indices(t, dx, dy, dz, idx)
+            assert e.value.error_code() == r["error"], (trial, dx, dy, dz)
+            errors += 1
+            continue
+        vi, sk, zz = sp.plan_indices(t, dx, dy, dz, idx)
+        np.testing.assert_array_equal(vi, r["value_indices"], err_msg=str(trial))
+        np.testing.assert_array_equal(sk, r["stick_keys"], err_msg=str(trial))
+        assert zz == r["zero_zero_stick"], trial
+        checked += 1
+    assert checked > 100 and errors > 5, (checked, errors)
