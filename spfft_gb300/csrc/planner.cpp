@@ -129,7 +129,11 @@ IndexPlan make_index_plan(SpfftTransformType type, int dimX, int dimY, int dimZ,
   // over the value positions, or a stable sort when the position range is very large).
   std::vector<int> order(numValues);
   const long long posRange = static_cast<long long>(numSticks) * dimZ;
-  if (posRange <= kTableLimit) {
+  bool increasing = true;  // values already in position order (z-stick order without duplicates)
+  for (int i = 1; i < numValues && increasing; ++i) increasing = p.valueIndices[i] > p.valueIndices[i - 1];
+  if (increasing) {
+    std::iota(order.begin(), order.end(), 0);
+  } else if (posRange <= kTableLimit) {
     std::vector<int> start(static_cast<size_t>(posRange) + 1, 0);
     for (int i = 0; i < numValues; ++i) ++start[p.valueIndices[i] + 1];
     for (long long q = 0; q < posRange; ++q) start[q + 1] += start[q];
