@@ -131,8 +131,9 @@ SPFFT_EXPORT SpfftError spfft_gb300_float_transform_path_info(SpfftFloatTransfor
 /* Autotuner (no counterpart in the reference). Times `repetitions` backward + scaled forward pairs
  * of every valid tile shape and plane strategy of the transform (first the sticks per z block with
  * the current plane strategy, then the fused plane pass with each chunk size and thread count and
- * the split passes with each column / row group size) on the transform's own device buffers, and
- * keeps the fastest; writes its time per pair in milliseconds to msPerPair (may be NULL).
+ * the split passes with each column / row group size, then the radix plans of the lengths that run
+ * on the generic kernels, spfft_gb300_transform_radix_plans) on the transform's own device buffers,
+ * and keeps the fastest; writes its time per pair in milliseconds to msPerPair (may be NULL).
  * Synchronous; overwrites the grid's internal device space-domain buffer; no other call on the
  * transform may run meanwhile. The choice lasts for the transform (clones start from the default
  * choice). */
@@ -187,7 +188,8 @@ SPFFT_EXPORT SpfftError spfft_gb300_batch_info(SpfftGb300Batch batch, int* numGr
                                                int* numUnbatched, int* launchesPerPair);
 /* Autotuner of a bound batch: for each group of equally shaped transforms, times `repetitions`
  * backward + scaled forward pairs of the group alone on `stream` for each plane strategy that fits
- * (fused, split) and each sticks-per-z-block size, and keeps the fastest. Overwrites the contents of
+ * (fused, split) and each sticks-per-z-block size, then for each row-group count of a fused group
+ * (spfft_gb300_batch_row_groups), and keeps the fastest. Overwrites the contents of
  * the bound buffers; drops captured graphs (the next graph call captures anew). Writes the sum of
  * the groups' best times per pair in milliseconds to msPerPair (may be NULL). Synchronous. */
 SPFFT_EXPORT SpfftError spfft_gb300_batch_autotune(SpfftGb300Batch batch, int repetitions, void* stream,
