@@ -23,56 +23,56 @@ __device__ __forceinline__ int find_transform(const int* __restrict__ starts, in
 
 template <typename S, typename A, int NZ>
 __global__ void __launch_bounds__(kThreads) z_backward_batch(const BatchView<S> bv, int spb) {
-  __shared__ int sExp;
+  __shared__ int sExp[2];
   const int t = find_transform(bv.starts, bv.count, blockIdx.x);
-  z_backward_body<S, A, NZ>(bv.views[t], bv.in[t], spb, blockIdx.x - bv.starts[t], &sExp);
+  z_backward_body<S, A, NZ>(bv.views[t], bv.in[t], spb, blockIdx.x - bv.starts[t], sExp);
 }
 
 template <typename S, typename A, int NZ>
 __global__ void __launch_bounds__(kThreads) z_forward_batch(const BatchView<S> bv, int spb) {
-  __shared__ int sExp;
+  __shared__ int sExp[2];
   const int t = find_transform(bv.starts, bv.count, blockIdx.x);
-  z_forward_body<S, A, NZ>(bv.views[t], bv.out[t], bv.scale, spb, blockIdx.x - bv.starts[t], &sExp);
+  z_forward_body<S, A, NZ>(bv.views[t], bv.out[t], bv.scale, spb, blockIdx.x - bv.starts[t], sExp);
 }
 
 template <typename S, typename A, int NY>
 __global__ void __launch_bounds__(kThreads, YMinBlocks<A>::value) y_backward_batch(const BatchView<S> bv, int cpb) {
-  __shared__ int sExp;
+  __shared__ int sExp[2];
   const int t = find_transform(bv.starts, bv.count, blockIdx.x);
   const PlanView<S>& p = bv.views[t];
   const int lb = blockIdx.x - bv.starts[t];
   const int gx = (p.numColumns + cpb - 1) / cpb;
-  y_backward_body<S, A, NY>(p, cpb, lb % gx, lb / gx, &sExp);
+  y_backward_body<S, A, NY>(p, cpb, lb % gx, lb / gx, sExp);
 }
 
 template <typename S, typename A, int NY>
 __global__ void __launch_bounds__(kThreads, YMinBlocks<A>::value) y_forward_batch(const BatchView<S> bv, int cpb) {
-  __shared__ int sExp;
+  __shared__ int sExp[2];
   const int t = find_transform(bv.starts, bv.count, blockIdx.x);
   const PlanView<S>& p = bv.views[t];
   const int lb = blockIdx.x - bv.starts[t];
   const int gx = (p.numColumns + cpb - 1) / cpb;
-  y_forward_body<S, A, NY>(p, cpb, lb % gx, lb / gx, &sExp);
+  y_forward_body<S, A, NY>(p, cpb, lb % gx, lb / gx, sExp);
 }
 
 template <typename S, typename A, int NX, bool R2C>
 __global__ void __launch_bounds__(kThreads) x_backward_batch(const BatchView<S> bv, int rpb) {
-  __shared__ int sExp;
+  __shared__ int sExp[2];
   const int t = find_transform(bv.starts, bv.count, blockIdx.x);
   const PlanView<S>& p = bv.views[t];
   const int lb = blockIdx.x - bv.starts[t];
   const int gx = (p.dimY + rpb - 1) / rpb;
-  x_backward_body<S, A, NX, R2C>(p, bv.out[t], rpb, lb % gx, lb / gx, &sExp);
+  x_backward_body<S, A, NX, R2C>(p, bv.out[t], rpb, lb % gx, lb / gx, sExp);
 }
 
 template <typename S, typename A, int NX, bool R2C>
 __global__ void __launch_bounds__(kThreads) x_forward_batch(const BatchView<S> bv, int rpb) {
-  __shared__ int sExp;
+  __shared__ int sExp[2];
   const int t = find_transform(bv.starts, bv.count, blockIdx.x);
   const PlanView<S>& p = bv.views[t];
   const int lb = blockIdx.x - bv.starts[t];
   const int gx = (p.dimY + rpb - 1) / rpb;
-  x_forward_body<S, A, NX, R2C>(p, bv.in[t], rpb, lb % gx, lb / gx, &sExp);
+  x_forward_body<S, A, NX, R2C>(p, bv.in[t], rpb, lb % gx, lb / gx, sExp);
 }
 
 // Fused y + x passes, one block per plane (cubic planes): starts count planes. `groups` row groups
@@ -80,17 +80,17 @@ __global__ void __launch_bounds__(kThreads) x_forward_batch(const BatchView<S> b
 template <typename S, typename A, int N, bool R2C>
 __global__ void __launch_bounds__(BatchPlaneThreads<A>::value, 2)
     plane_backward_batch(const BatchView<S> bv, int rows, int groups) {
-  __shared__ int sExp;
+  __shared__ int sExp[2];
   const int t = find_transform(bv.starts, bv.count, blockIdx.x);
-  plane_backward_body<S, A, N, N, R2C>(bv.views[t], bv.out[t], rows, blockIdx.x - bv.starts[t], &sExp, groups);
+  plane_backward_body<S, A, N, N, R2C>(bv.views[t], bv.out[t], rows, blockIdx.x - bv.starts[t], sExp, groups);
 }
 
 template <typename S, typename A, int N, bool R2C>
 __global__ void __launch_bounds__(BatchPlaneThreads<A>::value, 2)
     plane_forward_batch(const BatchView<S> bv, int rows, int wRows, int groups) {
-  __shared__ int sExp;
+  __shared__ int sExp[2];
   const int t = find_transform(bv.starts, bv.count, blockIdx.x);
-  plane_forward_body<S, A, N, N, R2C>(bv.views[t], bv.in[t], rows, wRows, blockIdx.x - bv.starts[t], &sExp,
+  plane_forward_body<S, A, N, N, R2C>(bv.views[t], bv.in[t], rows, wRows, blockIdx.x - bv.starts[t], sExp,
                                       groups);
 }
 

@@ -102,13 +102,39 @@ __device__ __forceinline__ ddc tw_arith(double2 v) {
   return make_c(dd_from_double(v.x, 0), dd_from_double(v.y, 0));
 }
 
+// Largest biased binary64 exponent field of a complex value (the first step of a block's
+// magnitude key, dd.cuh), and its largest subnormal key (the second step, for blocks of zeros and
+// subnormals only).
 __device__ __forceinline__ int max_exponent(float2) { return 0; }
 __device__ __forceinline__ int max_exponent(double2 v) {
   return max(dd_exponent_field(v.x), dd_exponent_field(v.y));
 }
-// Scale exponent k for a block whose largest biased binary64 exponent is e: 2^k * max in [1, 2).
-// Zero, subnormal-only and non-finite blocks use k = 0.
-__device__ __forceinline__ int block_scale(int e) { return (e == 0 || e == 2047) ? 0 : 1023 - e; }
+__device__ __forceinline__ int max_subnormal_key(float2) { return kDdNoSubnormal; }
+__device__ __forceinline__ int max_subnormal_key(double2 v) {
+  return max(dd_subnormal_key(v.x), dd_subnormal_key(v.y));
+}
+// Scale exponent k for a block with magnitude key e: 2^k * max in [1, 2), subnormal maxima
+// included. Zero and non-finite blocks use k = 0.
+__device__ __forceinline__ int block_scale(int e) { return dd_block_scale(e); }
+
+// Completes a block's magnitude key once the largest exponent field has been reduced into sExp[0]
+// (with sExp[1] = kDdNoSubnormal set before that reduction's barrier, and a barrier after it). A
+// block holding a normal or non-finite value keeps that field as its key. A block of zeros and
+// subnormals only (sExp[0] == 0, the same for every thread) reduces `scan()`, each thread's largest
+// max_subnormal_key, into sExp[1] and stores the exact key (0 for an all-zero block) in sExp[0].
+// Returns the key. Only that rare case adds a barrier; every thread has read sExp[0] before it, so
+// thread 0's store races with no reader.
+template <typename Scan>
+__device__ __forceinline__ int finish_block_key(int* sExp, Scan scan) {
+  const int e0 = sExp[0];
+  if (e0 != 0) return e0;
+  atomicMax(sExp + 1, scan());
+  __syncthreads();
+  const int sub = sExp[1];
+  const int key = sub == kDdNoSubnormal ? 0 : sub;
+  if (threadIdx.x == 0) sExp[0] = key;
+  return key;
+}
 
 // Double-float compact planes (PlanView::planesRaw): each producing block stores its scaled values
 // as they are and records its scale exponent k per column (y pass) or per row (x forward); a
@@ -116,7 +142,7 @@ __device__ __forceinline__ int block_scale(int e) { return (e == 0 || e == 2047)
 // exponent of its inputs (the largest magnitude) as its own scale and multiplies every other input
 // by 2^(k - k_input) <= 1, exactly (or to zero far below the block maximum).
 constexpr int kZeroExp = 1 << 20;
-__device__ __forceinline__ int produced_exp(int maxExponentField, int k) { return maxExponentField == 0 ? kZeroExp : k; }
+__device__ __forceinline__ int produced_exp(int maxKey, int k) { return maxKey == 0 ? kZeroExp : k; }
 __device__ __forceinline__ float2 scale_pow2(float2 v, int) { return v; }
 __device__ __forceinline__ ddc scale_pow2(ddc v, int d) {
   const float f = d < -126 ? 0.0f : __uint_as_float(static_cast<unsigned>(d + 127) << 23);
@@ -203,13 +229,20 @@ __device__ __forceinline__ int convert_block(typename Types<S, A>::CA* slots, in
   using TT = Types<S, A>;
   if (!TT::kScaled) return 0;
   using CS = typename TT::CS;
-  if (threadIdx.x == 0) *sExp = 0;
+  if (threadIdx.x == 0) {
+    sExp[0] = 0;
+    sExp[1] = kDdNoSubnormal;
+  }
   __syncthreads();
   int e = 0;
   for (int i = threadIdx.x; i < n; i += blockDim.x) e = max(e, max_exponent(reinterpret_cast<const CS*>(slots)[i]));
   atomicMax(sExp, e);
   __syncthreads();
-  const int k = block_scale(*sExp);
+  const int k = block_scale(finish_block_key(sExp, [&] {
+    int m = kDdNoSubnormal;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) m = max(m, max_subnormal_key(reinterpret_cast<const CS*>(slots)[i]));
+    return m;
+  }));
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
     const CS raw = reinterpret_cast<const CS*>(slots)[i];
     slots[i] = to_arith(raw, k);
@@ -326,8 +359,8 @@ __device__ __forceinline__ void z_backward_body(const PlanView<S>& p, const S* _
 template <typename S, typename A, int NZ>
 __global__ void __launch_bounds__(kThreads) z_backward(const PlanView<S> p,
                                                        const S* __restrict__ values, int spb) {
-  __shared__ int sExp;
-  z_backward_body<S, A, NZ>(p, values, spb, blockIdx.x, &sExp);
+  __shared__ int sExp[2];
+  z_backward_body<S, A, NZ>(p, values, spb, blockIdx.x, sExp);
 }
 
 template <typename S, typename A, int NZ>
@@ -414,8 +447,8 @@ __device__ __forceinline__ void z_forward_body(const PlanView<S>& p, S* __restri
 template <typename S, typename A, int NZ>
 __global__ void __launch_bounds__(kThreads) z_forward(const PlanView<S> p, S* __restrict__ values,
                                                       S scale, int spb) {
-  __shared__ int sExp;
-  z_forward_body<S, A, NZ>(p, values, scale, spb, blockIdx.x, &sExp);
+  __shared__ int sExp[2];
+  z_forward_body<S, A, NZ>(p, values, scale, spb, blockIdx.x, sExp);
 }
 
 // ================================================================================================
@@ -637,8 +670,8 @@ __device__ __forceinline__ void plane_backward_body(const PlanView<S>& p, S* __r
 template <typename S, typename A, int NX, int NY, bool R2C>
 __global__ void __launch_bounds__(kPlaneThreads) plane_backward(const PlanView<S> p,
                                                                 S* __restrict__ space, int rows) {
-  __shared__ int sExp;
-  plane_backward_body<S, A, NX, NY, R2C>(p, space, rows, blockIdx.x, &sExp);
+  __shared__ int sExp[2];
+  plane_backward_body<S, A, NX, NY, R2C>(p, space, rows, blockIdx.x, sExp);
 }
 
 template <typename S, typename A, int NX, int NY, bool R2C>
@@ -691,14 +724,23 @@ __device__ __forceinline__ void plane_forward_body(const PlanView<S>& p, const S
   // while the first chunk is in flight (the plane then stays in L2 for the chunk loads).
   int k = 0;
   if (TT::kScaled) {
-    if (threadIdx.x == 0) sExp = 0;
+    if (threadIdx.x == 0) {
+      sExp = 0;
+      (&sExp)[1] = kDdNoSubnormal;
+    }
     __syncthreads();
     int e = 0;
     for (int i = threadIdx.x; i < NY * L::LX; i += blockDim.x) e = max(e, max_exponent(plane[i]));
     atomicMax(&sExp, e);
   }
   __syncthreads();
-  if (TT::kScaled) k = block_scale(sExp);
+  if (TT::kScaled) {
+    k = block_scale(finish_block_key(&sExp, [&] {
+      int m = kDdNoSubnormal;
+      for (int i = threadIdx.x; i < NY * L::LX; i += blockDim.x) m = max(m, max_subnormal_key(plane[i]));
+      return m;
+    }));
+  }
 
   const CA* twl = R2C ? s.twm : s.twx;
   for (int chunk = 0; chunk < nchunks; ++chunk) {
@@ -796,8 +838,8 @@ __device__ __forceinline__ void plane_forward_body(const PlanView<S>& p, const S
 template <typename S, typename A, int NX, int NY, bool R2C>
 __global__ void __launch_bounds__(kPlaneThreads) plane_forward(const PlanView<S> p,
                                                                const S* __restrict__ space, int rows) {
-  __shared__ int sExp;
-  plane_forward_body<S, A, NX, NY, R2C>(p, space, rows, rows, blockIdx.x, &sExp);
+  __shared__ int sExp[2];
+  plane_forward_body<S, A, NX, NY, R2C>(p, space, rows, rows, blockIdx.x, sExp);
 }
 
 // ================================================================================================
@@ -977,8 +1019,8 @@ __device__ __forceinline__ void y_backward_body(const PlanView<S>& p, int cpb, i
 template <typename S, typename A, int NY>
 __global__ void __launch_bounds__(kThreads, YMinBlocks<A>::value) y_backward_split(const PlanView<S> p, int cpb,
                                                                                      int z0) {
-  __shared__ int sExp;
-  y_backward_body<S, A, NY>(p, cpb, blockIdx.x, z0 + blockIdx.y, &sExp);
+  __shared__ int sExp[2];
+  y_backward_body<S, A, NY>(p, cpb, blockIdx.x, z0 + blockIdx.y, sExp);
 }
 
 // y forward: block (column group, z)
@@ -1070,8 +1112,8 @@ __device__ __forceinline__ void y_forward_body(const PlanView<S>& p, int cpb, in
 template <typename S, typename A, int NY>
 __global__ void __launch_bounds__(kThreads, YMinBlocks<A>::value) y_forward_split(const PlanView<S> p, int cpb,
                                                                                     int z0) {
-  __shared__ int sExp;
-  y_forward_body<S, A, NY>(p, cpb, blockIdx.x, z0 + blockIdx.y, &sExp);
+  __shared__ int sExp[2];
+  y_forward_body<S, A, NY>(p, cpb, blockIdx.x, z0 + blockIdx.y, sExp);
 }
 
 // Shared memory of the x kernels: twx[NX] | (R2C) twm[M] | colOf[NXF] | P[rows][numColumns] |
@@ -1206,8 +1248,8 @@ __device__ __forceinline__ void x_backward_body(const PlanView<S>& p, S* __restr
 template <typename S, typename A, int NX, bool R2C>
 __global__ void __launch_bounds__(kThreads) x_backward_split(const PlanView<S> p, S* __restrict__ space,
                                                              int rpb, int z0) {
-  __shared__ int sExp;
-  x_backward_body<S, A, NX, R2C>(p, space, rpb, blockIdx.x, z0 + blockIdx.y, &sExp);
+  __shared__ int sExp[2];
+  x_backward_body<S, A, NX, R2C>(p, space, rpb, blockIdx.x, z0 + blockIdx.y, sExp);
 }
 
 // x forward: block (row group, z); space rows -> x-FFT -> compact rows to HBM
@@ -1224,7 +1266,10 @@ __device__ __forceinline__ void x_forward_body(const PlanView<S>& p, const S* __
   const FastDiv dnc(nc);
   const int y0 = bx * rpb, nr = min(rpb, ny - y0);
   RowSmem<CA, NX, R2C> s(nc, rpb, !R2C);
-  if (TT::kScaled && threadIdx.x == 0) sExp = 0;
+  if (TT::kScaled && threadIdx.x == 0) {
+    sExp = 0;
+    (&sExp)[1] = kDdNoSubnormal;
+  }
   row_load_tables<S, A, NX, R2C>(p, s);
   pdl_wait();
   pdl_trigger();
@@ -1244,7 +1289,15 @@ __device__ __forceinline__ void x_forward_body(const PlanView<S>& p, const S* __
     atomicMax(&sExp, e);
   }
   __syncthreads();
-  if (TT::kScaled) k = block_scale(sExp);
+  if (TT::kScaled) {
+    k = block_scale(finish_block_key(&sExp, [&] {
+      int m = kDdNoSubnormal;
+      for (RowWalk w(threadIdx.x, blockDim.x, L::LX); w.r < nr; w.next()) {
+        m = max(m, max_subnormal_key(reinterpret_cast<const CS*>(s.W)[w.r * L::WP + L::wpos(w.c)]));
+      }
+      return m;
+    }));
+  }
   const CA* twl = R2C ? s.twm : s.twx;
   for (int i = threadIdx.x; i < nr * Bx; i += blockDim.x) {
     const int rl = i / Bx, b = i - rl * Bx;
@@ -1304,8 +1357,8 @@ __device__ __forceinline__ void x_forward_body(const PlanView<S>& p, const S* __
 template <typename S, typename A, int NX, bool R2C>
 __global__ void __launch_bounds__(kThreads, YMinBlocks<A>::value) x_forward_split(const PlanView<S> p, const S* __restrict__ space,
                                                             int rpb, int z0) {
-  __shared__ int sExp;
-  x_forward_body<S, A, NX, R2C>(p, space, rpb, blockIdx.x, z0 + blockIdx.y, &sExp);
+  __shared__ int sExp[2];
+  x_forward_body<S, A, NX, R2C>(p, space, rpb, blockIdx.x, z0 + blockIdx.y, sExp);
 }
 
 template <typename S, typename A, int NY>

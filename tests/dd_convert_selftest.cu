@@ -2,9 +2,11 @@
 // split accuracy (hi + lo within 2^-46 of v * 2^k), round trips, faithful rounding of dd_to_double
 // (within one binary64 ulp of the exact sum) on normalised pairs, on pairs whose lo is not below
 // hi, on powers of two with a negative lo and on all-ones mantissas with a positive lo, signs,
-// zeros, infinities and NaN. Prints "ok <checks>" or the first failure.
+// zeros, infinities and NaN; subnormal binary64 inputs (magnitude key, block scale, split, round
+// trip) and results in the subnormal range. Prints "ok <checks>" or the first failure.
 #include <cmath>
 #include <cstdio>
+#include <cstring>
 #include <random>
 
 #include "dd.cuh"
@@ -74,6 +76,73 @@ int main() {
     }
     checks += 6;
   }
+  // subnormal binary64 inputs: the subnormal key orders them (below every normal, whose key is
+  // its exponent field >= 1), the block scale brings each into [1, 2), the split is exact for up
+  // to 47 significant bits (within 2^-46 otherwise) and the round trip returns to the subnormal
+  // within that error
+  std::uniform_int_distribution<int> subShift(0, 51);
+  for (int i = 0; i < 200000; ++i) {
+    const unsigned long long frac = (rng() & 0xFFFFFFFFFFFFFull) >> subShift(rng);
+    if (frac == 0) continue;
+    double v;
+    std::memcpy(&v, &frac, 8);
+    if (i & 1) v = -v;
+    const int key = dd_subnormal_key(v);
+    if (key < -52 || key > -1 || dd_exponent_field(v) != 0) {
+      std::printf("subnormal key %d for %.17g\n", key, v);
+      return 10;
+    }
+    const int k = dd_block_scale(key);
+    const long double scaled = std::fabs(std::ldexp((long double)v, k));
+    if (scaled < 1.0L || scaled >= 2.0L) {
+      std::printf("subnormal block scale %d for %.17g\n", k, v);
+      return 11;
+    }
+    const int kk = k - (i % 40);  // the value is not always the block maximum
+    const dd d = dd_from_double(v, kk);
+    const long double want = std::ldexp((long double)v, kk);
+    const long double got = (long double)d.hi + (long double)d.lo;
+    if (std::fabs((double)((got - want) / want)) > std::ldexp(1.0, -46)) {
+      std::printf("subnormal split error v=%.17g k=%d\n", v, kk);
+      return 12;
+    }
+    const double back = dd_to_double(d, -kk);
+    if (std::fabs(back - v) > std::ldexp(std::fabs(v), -46) + std::ldexp(1.0, -1074)) {
+      std::printf("subnormal round trip v=%.17g back=%.17g\n", v, back);
+      return 13;
+    }
+    // a subnormal scaled by a normal block maximum's k (2^-1022 .. 2^-1000 maxima)
+    const int kn = dd_block_scale(1 + (i % 23));
+    const dd dn = dd_from_double(v, kn);
+    const long double wn = std::ldexp((long double)v, kn);
+    if (std::fabs(wn) >= std::ldexp(1.0L, -100) &&
+        std::fabs((double)(((long double)dn.hi + (long double)dn.lo - wn) / wn)) > std::ldexp(1.0, -46)) {
+      std::printf("subnormal under a normal block scale v=%.17g k=%d\n", v, kn);
+      return 9;
+    }
+    checks += 4;
+  }
+  // results in the binary64 subnormal range: within one subnormal unit of the exact scaled sum
+  for (int i = 0; i < 200000; ++i) {
+    const float a = (float)mant(rng) * ((i & 1) ? -1.0f : 1.0f);
+    const float b = (float)mant(rng) * std::ldexp(1.0f, -24 - (i % 8)) * ((i & 2) ? -1.0f : 1.0f);
+    const dd n = dd_two_sum(a, b);
+    const int k = -1022 - (i % 70);  // 2^k * [1, 2) from the smallest normal down past 2^-1074
+    const double got = dd_to_double(n, k);
+    const long double want = std::ldexp((long double)n.hi + (long double)n.lo, k);
+    if (std::fabs((long double)got - want) > std::ldexp(1.0L, -1074)) {
+      std::printf("subnormal result error hi=%.9g lo=%.9g k=%d got %.17g want %.17Lg\n", n.hi, n.lo, k, got, want);
+      return 14;
+    }
+    if (got != 0.0 && std::signbit(got) != std::signbit(a)) return 15;
+    checks += 1;
+  }
+  // key edges
+  if (dd_subnormal_key(0.0) != kDdNoSubnormal || dd_subnormal_key(-0.0) != kDdNoSubnormal) return 16;
+  if (dd_subnormal_key(4.9406564584124654e-324) != -52) return 17;
+  if (dd_subnormal_key(std::nextafter(2.2250738585072014e-308, 0.0)) != -1) return 18;
+  if (dd_block_scale(dd_exponent_field(1.0)) != 0 || dd_block_scale(2047) != 0 || dd_block_scale(0) != 0) return 19;
+  if (dd_block_scale(-52) != 1074 || dd_block_scale(1) != 1022) return 20;
   // specials
   if (dd_to_double(dd_from_double(0.0, 5), -5) != 0.0) return 2;
   if (!std::signbit(dd_to_double(dd_from_double(-0.0, 0), 0))) return 3;
@@ -82,6 +151,6 @@ int main() {
   if (dd_exponent_field(1.0) != 1023 || dd_exponent_field(0.0) != 0) return 6;
   if (!std::isinf(dd_to_double(dd(1.5f, 0.0f), 2000))) return 7;
   if (dd_to_double(dd(1.5f, 0.0f), -2000) != 0.0) return 8;
-  std::printf("ok %ld\n", checks + 7);
+  std::printf("ok %ld\n", checks + 12);
   return 0;
 }
