@@ -227,15 +227,19 @@ SPFFT_EXPORT SpfftError spfft_gb300_multi_batched_calls(long long* count);
  * cudaStream_t; NULL is the default stream), keeping the z-stick and plane intermediates in a
  * static 64 MiB device array that is part of the library, instead of memory the library allocates.
  * For callers that cannot let the library call cudaMalloc: applications whose device memory is
- * owned by their own pool allocator, or code running inside CUDA stream capture, where cudaMalloc
- * is not permitted. The call allocates nothing and does not synchronise.
+ * owned and budgeted by their own pool or arena allocator, latency-critical loops that cannot
+ * afford an allocation's device synchronisation, plug-ins whose host application forbids them to
+ * allocate. The call allocates nothing and does not synchronise.
  * Limits and rules:
+ *  - values and space must be device memory of the transform's GPU (there is no staging through
+ *    host memory); anything else is rejected with SPFFT_INVALID_PARAMETER_ERROR before any launch;
+ *  - a CUDA error pending from earlier work is reported as SPFFT_GPU_PRECEDING_ERROR;
  *  - transforms whose intermediates exceed 64 MiB are rejected with SPFFT_INVALID_PARAMETER_ERROR;
  *  - every GPU that loads the library holds the 64 MiB array until the process exits;
  *  - all calls share the one array per GPU: calls that overlap on the GPU (different streams, or
  *    different transforms in flight at once) race and corrupt each other's results;
- *  - the first call on each device looks up the array's device address; make that first call
- *    before any stream capture. */
+ *  - the first call on each device (and the first after the device's context was reset) looks up
+ *    the array's device address; make that first call before any stream capture. */
 SPFFT_EXPORT SpfftError spfft_gb300_transform_backward_noalloc(SpfftTransform transform,
                                                                const double* values,
                                                                double* space, void* stream);

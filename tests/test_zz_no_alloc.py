@@ -1,10 +1,13 @@
 """GPU test of the allocation-free backward entry point (spfft_gb300_transform_backward_noalloc).
 
-That entry point serves callers that cannot let the library call cudaMalloc -- applications whose
-device memory belongs to their own pool allocator, or code running under CUDA stream capture. It
-keeps the transform's intermediates in a static 64 MiB device array. This test calls it through
-the C ABI twice in a row, with different inputs, and compares each result with the regular
-backward entry point (spfft_transform_backward_ptr) at the FP64 tolerance of the parity suite.
+That entry point serves callers that cannot let the library call cudaMalloc: applications whose
+device memory belongs to their own pool or arena allocator, latency-critical loops that cannot
+afford an allocation's device synchronisation, plug-ins whose host application forbids them to
+allocate. It keeps the transform's intermediates in a static 64 MiB device array. This test calls
+it through the C ABI twice in a row, with different inputs, and compares each result with the
+regular backward entry point (spfft_transform_backward_ptr) at the FP64 tolerance of the parity
+suite; it also checks that sizes above the limit, a null handle and buffers that are not device
+memory of the transform's GPU are rejected before any kernel runs.
 It lives in its own file, collected last, and passes both alone and after the other tests.
 """
 import ctypes
@@ -66,3 +69,32 @@ def test_noalloc_rejects_intermediates_above_the_limit(lib):
     fn = _noalloc(lib)
     assert fn(tr.handle, v.data_ptr(), out.data_ptr(), None) == sp.ErrorCode.SPFFT_INVALID_PARAMETER_ERROR
     assert fn(None, v.data_ptr(), out.data_ptr(), None) == sp.ErrorCode.SPFFT_INVALID_HANDLE_ERROR
+
+
+def test_noalloc_rejects_buffers_that_are_not_device_memory(lib):
+    # The kernels must never be handed a host address: a pageable numpy buffer, a pinned host
+    # buffer and a null space pointer are refused with SPFFT_INVALID_PARAMETER_ERROR, and a
+    # regular call afterwards still works (nothing was launched and no error is left pending).
+    idx = sphere_indices(32, 8)
+    tr = sp.Transform(1, sp.SPFFT_PU_GPU, sp.SPFFT_TRANS_C2C, 32, 32, 32, len(idx),
+                      sp.SPFFT_INDEX_TRIPLETS, idx)
+    rng = np.random.default_rng(7)
+    vals = rng.uniform(-1, 1, len(idx)) + 1j * rng.uniform(-1, 1, len(idx))
+    v = torch.from_numpy(vals).cuda()
+    out = torch.empty((32, 32, 32), dtype=torch.complex128, device="cuda")
+    host_vals = np.ascontiguousarray(vals)
+    host_space = np.zeros((32, 32, 32), dtype=np.complex128)
+    pinned_space = torch.zeros((32, 32, 32), dtype=torch.complex128).pin_memory()
+    fn = _noalloc(lib)
+    bad = sp.ErrorCode.SPFFT_INVALID_PARAMETER_ERROR
+    torch.cuda.synchronize()
+    assert fn(tr.handle, host_vals.ctypes.data, out.data_ptr(), None) == bad
+    assert fn(tr.handle, v.data_ptr(), host_space.ctypes.data, None) == bad
+    assert fn(tr.handle, v.data_ptr(), pinned_space.data_ptr(), None) == bad
+    assert fn(tr.handle, v.data_ptr(), None, None) == bad
+    assert not host_space.any() and not pinned_space.any()
+    assert fn(tr.handle, v.data_ptr(), out.data_ptr(), None) == 0
+    want = torch.empty_like(out)
+    tr.backward(v, want)
+    torch.cuda.synchronize()
+    assert rel_l2(out.cpu().numpy(), want.cpu().numpy()) <= 1e-12
