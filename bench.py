@@ -208,10 +208,26 @@ class ClockSampler:
 # ---------------------------------------------------------------------------------------------
 # multi-rank host logic (one process per GPU; covered by gloo tests on the CPU)
 # ---------------------------------------------------------------------------------------------
-def shard(count: int, rank: int, world: int) -> list:
-    """Transforms of a batch owned by `rank`: round robin, so every transform has exactly one
-    owner and the ranks' shares differ by at most one (no collective on the data path)."""
-    return list(range(rank, count, world))
+def transform_cost(n: int, radius: float, r2c: bool, tsize: int = 4) -> int:
+    """Algorithmic HBM bytes of one backward+forward pair of a batch transform (the sharding
+    weight): sparse values + int32 value map + dense space grid, each once per direction."""
+    npts = len(sphere_indices(n, radius, r2c))
+    return algorithmic_bytes(n, npts, 0, 0, r2c, tsize)["pair"]
+
+
+def shard(costs: list, rank: int, world: int) -> list:
+    """Transforms of a batch owned by `rank`, balanced by cost (algorithmic bytes): greedy
+    longest-processing-time assignment -- transforms in decreasing cost, each to the rank with the
+    least cost so far (ties to the lower rank). Every transform has exactly one owner and no
+    collective is needed on the data path."""
+    order = sorted(range(len(costs)), key=lambda j: (-costs[j], j))
+    load = [0] * world
+    owner = [0] * len(costs)
+    for j in order:
+        r = min(range(world), key=lambda q: (load[q], q))
+        owner[j] = r
+        load[r] += costs[j]
+    return [j for j in range(len(costs)) if owner[j] == rank]
 
 
 def max_over_ranks(value: float, world: int) -> float:
@@ -276,6 +292,35 @@ def load_traffic_table() -> dict:
             if len(parts) >= 4 and not line.startswith("#"):
                 out[(parts[0], parts[1], parts[2])] = float(parts[3])
     return out
+
+
+def oracle_errors(cases: list) -> dict:
+    """Per-transform error of GPU results against the FP64 oracle (the restated reference host
+    pipeline), computed after the timed regions. `cases` holds (label, n, r2c, idx, host_values,
+    gpu_space, gpu_scaled_forward_of_gpu_space): the backward is compared with the oracle's FP64
+    backward of the same values, the scaled forward with the oracle's scaled forward of the GPU's
+    own space domain. Relative L2 and relative max-abs (over the largest reference magnitude)."""
+    from oracle import pipeline
+
+    rows = []
+    for label, n, r2c, idx, host, space, fwd in cases:
+        o = pipeline.HostPipeline(1 if r2c else 0, n, n, n, idx)
+        want = o.backward(host)
+        d = space.astype(want.dtype) - want
+        b_l2 = float(np.linalg.norm(d.ravel()) / np.linalg.norm(want.ravel()))
+        b_max = float(np.abs(d).max() / np.abs(want).max())
+        want_f = o.forward(space.astype(np.float64 if r2c else np.complex128), scaled=True)
+        d = fwd.astype(np.complex128) - want_f
+        f_l2 = float(np.linalg.norm(d) / np.linalg.norm(want_f))
+        f_max = float(np.abs(d).max() / np.abs(want_f).max())
+        rows.append({"transform": label, "backward_rel_l2": float(f"{b_l2:.3g}"),
+                     "backward_rel_maxabs": float(f"{b_max:.3g}"), "forward_rel_l2": float(f"{f_l2:.3g}"),
+                     "forward_rel_maxabs": float(f"{f_max:.3g}")})
+    keys = ("backward_rel_l2", "backward_rel_maxabs", "forward_rel_l2", "forward_rel_maxabs")
+    return {"oracle": "FP64 numpy/scipy restatement of the reference host pipeline",
+            "transforms_checked": len(rows),
+            **{k + "_max": max(r[k] for r in rows) for k in keys},
+            "per_transform": rows}
 
 
 def measure_gpu(args, rank: int, world: int) -> dict:
@@ -440,6 +485,16 @@ def measure_gpu(args, rank: int, world: int) -> dict:
     sel = idx[:, 0] != 0 if r2c else slice(None)
     err = float(np.linalg.norm(got[sel] - want[sel]) / np.linalg.norm(want[sel]))
 
+    # the reference's own GPU path on the same workload (and its backward next to ours)
+    ours_space = None
+    if dtype == "float64":
+        tr.set_stream(None)
+        tr.backward(torch.from_numpy(vals_h).to(ct).cuda(), space)
+        torch.cuda.synchronize()
+        ours_space = space.cpu().numpy()
+    ref_gpu = (measure_reference_gpu(args, n, r2c, idx, vals_h, ours_space, args.batch)
+               if ours_space is not None and not args.no_reference_gpu else None)
+
     batched = None if args.no_batched else measure_batched(args, args.workload, args.batch, "float32")
     grad = None if args.no_batched else measure_grad(args)
 
@@ -447,11 +502,150 @@ def measure_gpu(args, rank: int, world: int) -> dict:
         "batched": batched, "grad": grad,
         "pairs_per_s": pairs_per_s, "ms_per_step": total_ms / args.steps, "wall_s": wall,
         "clocks": clocks.summary(), "roofline": roofline, "e2e": e2e,
-        "pair_gbs": pair_gbs, "roundtrip_rel_l2": err, "cufft_dense": cufft,
+        "pair_gbs": pair_gbs, "roundtrip_rel_l2": err, "cufft_dense": cufft, "reference_gpu": ref_gpu,
         "launches_per_step": 6 if tr.path_info()["split_plane"] else 4, "npts": npts, "nsticks": nsticks,
         "ncols": ncols, "tuning": tuned or tr.tuning(), "plan_ms": plan_ms,
         "plan_host_ms": plan_host_ms,
     }
+
+
+def measure_plain_compact(args, workload: str, dtype: str = "float64") -> dict:
+    """A single-transform configuration for the default line: pairs/s of the FP64 drop-in path on
+    device buffers (autotuned plan, L2 flushed between timed steps, CUDA events), the dominant
+    kernel's roofline, and one backward + scaled forward against the FP64 oracle."""
+    import torch
+
+    import spfft_gb300 as sp
+
+    n, radius, r2c = WORKLOADS[workload]
+    idx = sphere_indices(n, radius, r2c)
+    ttype = sp.SPFFT_TRANS_R2C if r2c else sp.SPFFT_TRANS_C2C
+    ct = torch.complex128 if dtype == "float64" else torch.complex64
+    rt = torch.float64 if dtype == "float64" else torch.float32
+    tr = sp.Transform(1, sp.SPFFT_PU_GPU, ttype, n, n, n, len(idx), sp.SPFFT_INDEX_TRIPLETS, idx, dtype=dtype)
+    vals_h = make_values(idx, r2c)
+    values = torch.from_numpy(vals_h).to(ct).cuda()
+    out_vals = torch.empty_like(values)
+    space = torch.empty((n, n, n), dtype=rt if r2c else ct, device="cuda")
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    stream = torch.cuda.Stream()
+    if not args.no_autotune:
+        tr.autotune(3)
+    tr.set_stream(stream)
+    tr.set_execution_mode(sp.SPFFT_EXEC_ASYNCHRONOUS)
+
+    def pair():
+        tr.backward(values, space)
+        tr.forward(space, out_vals, sp.SPFFT_NO_SCALING)
+
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            pair()
+    torch.cuda.synchronize()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    with torch.cuda.stream(stream):
+        for k in range(args.steps):
+            flush.zero_()
+            starts[k].record(stream)
+            pair()
+            ends[k].record(stream)
+    torch.cuda.synchronize()
+    ms = sum(a.elapsed_time(b) for a, b in zip(starts, ends))
+    nsticks = int(np.unique((idx[:, 0] % n) * n + idx[:, 1] % n).size)
+    ncols = int(np.unique(idx[:, 0] % n).size)
+    ab = algorithmic_bytes(n, len(idx), nsticks, ncols, r2c, 8 if dtype == "float64" else 4)
+    acc = {k: [] for k in ("z_backward", "y_backward", "x_backward", "x_forward", "y_forward", "z_forward")}
+    for _ in range(5):
+        flush.zero_()
+        torch.cuda.synchronize()
+        for nm, t in zip(("z_backward", "y_backward", "x_backward"), sp.stage_times(tr, 0, values, space, stream=stream)):
+            acc[nm].append(t)
+        flush.zero_()
+        torch.cuda.synchronize()
+        for nm, t in zip(("x_forward", "y_forward", "z_forward"), sp.stage_times(tr, 1, space, out_vals, stream=stream)):
+            acc[nm].append(t)
+    kern_ms = {k: statistics.median(v) for k, v in acc.items() if v}
+    dom = max(kern_ms, key=kern_ms.get)
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    achieved = ab["kernels"][dom] / (kern_ms[dom] * 1e-3) / 1e9 if kern_ms[dom] > 0 else 0.0
+    # accuracy: backward, then the scaled forward of the GPU's space domain, against the oracle
+    tr.backward(values, space)
+    tr.forward(space, out_vals, sp.SPFFT_FULL_SCALING)
+    torch.cuda.synchronize()
+    err = oracle_errors([(workload, n, r2c, idx, vals_h, space.cpu().numpy(), out_vals.cpu().numpy())])
+    return {"workload": workload, "dtype": dtype, "value": round(args.steps / (ms / 1e3), 2), "unit": UNIT,
+            "ms_per_step": round(ms / args.steps, 4), "frequency_values": len(idx),
+            "l2": "flushed between timed steps (256 MB write)",
+            "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak,
+                         "unit": "GB/s", "frac": round(achieved / peak, 4),
+                         "kernel_ms": {k: round(v, 4) for k, v in kern_ms.items()}},
+            "vs_oracle": {k: v for k, v in err.items() if k != "per_transform"}}
+
+
+def reference_source_dir() -> Path | None:
+    """The reference source tree for the comparison build: $SPFFT_REFERENCE_SRC, else the staged
+    copy baseline/_ref (git-ignored; see baseline/Makefile). None when neither exists."""
+    for cand in (os.environ.get("SPFFT_REFERENCE_SRC"), str(ROOT / "baseline" / "_ref")):
+        if cand and (Path(cand) / "src" / "execution" / "execution_gpu.cpp").exists():
+            return Path(cand).resolve()
+    return None
+
+
+def measure_reference_gpu(args, n: int, r2c: bool, idx: np.ndarray, vals_h: np.ndarray, ours_space: np.ndarray,
+                          batch: int) -> dict:
+    """The reference's own GPU path (its CUDA kernels plus cuFFT; baseline/Makefile builds it from
+    the reference's sources for sm_103a), timed by baseline/ref_gpu_bench on the same workload
+    with the same protocol: FP64 plain (device buffers, external space buffer, L2 flushed, CUDA
+    events) and FP32 over `batch` transforms through its multi-transform calls. The reference's
+    backward result is compared with ours (`ours_space`) to show that both compute the same
+    transform."""
+    import tempfile
+
+    src = reference_source_dir()
+    if src is None:
+        return {"unavailable": "the reference sources are not staged (baseline/_ref, or SPFFT_REFERENCE_SRC)"}
+    t0 = time.perf_counter()
+    build = subprocess.run(["make", "-s", "-j", str(os.cpu_count() or 4), "-C", str(ROOT / "baseline"),
+                            f"REF={src}"], capture_output=True, text=True)
+    build_s = time.perf_counter() - t0
+    exe = ROOT / "baseline" / "_ref" / "build" / "ref_gpu_bench"
+    if build.returncode != 0 or not exe.exists():
+        tail = (build.stderr or build.stdout).strip().splitlines()[-1:] or ["?"]
+        return {"unavailable": f"build of the reference GPU path failed: {tail[0][:200]}"}
+    out = {"source": "the reference's own GPU path (execution_gpu.cpp, its CUDA kernels, cuFFT), built from "
+                     "its sources for sm_103a by baseline/Makefile; driven through its public C++ API by "
+                     "baseline/ref_gpu_bench.cpp", "build_s": round(build_s, 1)}
+    with tempfile.TemporaryDirectory() as tmp:
+        inp = Path(tmp) / "input.bin"
+        with open(inp, "wb") as f:
+            np.array([1 if r2c else 0, n, len(idx)], dtype=np.int32).tofile(f)
+            np.ascontiguousarray(idx, dtype=np.int32).tofile(f)
+            np.ascontiguousarray(vals_h, dtype=np.complex128).view(np.float64).tofile(f)
+        space_out = Path(tmp) / "space.bin"
+        runs = (("fp64_plain", "64", 1, str(space_out)), ("fp32_multi_transform", "32", batch, None))
+        for key, prec, count, extra in runs:
+            cmd = [str(exe), str(inp), prec, str(count), str(max(3, args.steps)), str(args.warmup)]
+            if extra:
+                cmd.append(extra)
+            r = subprocess.run(cmd, capture_output=True, text=True, timeout=600)
+            if r.returncode != 0:
+                out[key] = {"unavailable": f"exit {r.returncode}: {(r.stderr or '').strip()[-200:]}"}
+                continue
+            res = json.loads(r.stdout.strip().splitlines()[-1])
+            out[key] = {"value": round(res["pairs_per_s"], 2), "unit": UNIT, "ms_per_step": res["ms_per_step"],
+                        "transforms_per_step": count}
+        if space_out.exists():
+            ref_space = np.fromfile(space_out, dtype=np.float64)
+            ref_space = ref_space if r2c else ref_space.view(np.complex128)
+            ours = ours_space.reshape(-1)
+            out["fp64_backward_rel_l2_ours_vs_reference"] = float(
+                np.linalg.norm(ours - ref_space) / np.linalg.norm(ref_space))
+    out["protocol"] = ("device buffers, external out-of-place space domain (FP64) / multi-transform pointer "
+                       "forms (FP32), asynchronous execution mode, CUDA events on the default stream, 256 MB "
+                       "L2 flush between timed steps")
+    return out
 
 
 def measure_cufft_dense(args, idx: np.ndarray, vals_h: np.ndarray, n: int, r2c: bool, ct, stream) -> dict:
@@ -622,28 +816,22 @@ def measure_batched(args, workload: str, batch: int, dtype: str, radii=None) -> 
         got = vals[b].cpu().numpy().astype(np.complex128)
         sel = idxs[b][:, 0] != 0 if r2c else slice(None)
         errs.append(float(np.linalg.norm(got[sel] - hosts[b][sel]) / np.linalg.norm(hosts[b][sel])))
-    # FP32 against FP64: backward of the first and the last transform against the FP64 transform
+    # FP32 against the FP64 oracle: backward and scaled forward of 8 transforms of the batch
     fp64_err = {}
     if dtype == "float32":
         for b in range(batch):
             vals[b].copy_(torch.from_numpy(hosts[b]).to(ct))
         bt.backward(stream)
         stream.synchronize()
-        rl2, mab = [], []
-        for b in sorted({0, batch - 1}):
-            t64 = sp.Transform(1, sp.SPFFT_PU_GPU, ttype, n, n, n, len(idxs[b]), sp.SPFFT_INDEX_TRIPLETS, idxs[b],
-                               dtype="float64")
-            s64 = torch.empty((n, n, n), dtype=torch.float64 if r2c else torch.complex128, device="cuda")
-            t64.backward(torch.from_numpy(hosts[b]).cuda(), s64)
-            d = (spaces[b].to(s64.dtype) - s64).flatten()
-            rl2.append(float(torch.linalg.vector_norm(d) / torch.linalg.vector_norm(s64.flatten())))
-            mab.append(float(d.abs().max() / s64.abs().max()))
-            del t64, s64
-        fp64_err = {"backward_space_rel_l2_max": max(rl2), "backward_space_rel_maxabs_max": max(mab),
-                    "transforms_checked": len(rl2)}
+        sample = sorted(set(np.linspace(0, batch - 1, min(8, batch)).astype(int).tolist()))
+        spaces_h = {b: spaces[b].cpu().numpy() for b in sample}
+        bt.forward(sp.SPFFT_FULL_SCALING, stream)
+        stream.synchronize()
+        fp64_err = oracle_errors([(f"{workload}[{b}]", n, r2c, idxs[b], hosts[b], spaces_h[b],
+                                   vals[b].cpu().numpy()) for b in sample])
     info = bt.info()
     return {"value": round(batch * args.steps / (ms / 1e3), 2), "unit": UNIT, "dtype": dtype,
-            "fp32_vs_fp64": fp64_err,
+            "fp32_vs_fp64_oracle": fp64_err,
             "transforms_per_step": batch, "ms_per_step": round(ms / args.steps, 4),
             "graph_launches_per_step": 1, "kernel_launches_per_step": info["launches_per_pair"],
             "shape_groups": info["groups"], "roundtrip_rel_l2_max": max(errs),
@@ -667,19 +855,38 @@ def batch_values(idx: np.ndarray, r2c: bool, seed: int) -> np.ndarray:
     return v
 
 
-def measure_batch_workload(args, rank: int, world: int) -> dict:
-    """A batch of independent transforms (sharded over the ranks, no collective): FP32 pairs/s as
-    one captured graph per step, the FP64 plain drop-in path over the same transforms one by one,
-    the FP32 error against that FP64 path, per-pass roofline, and an end-to-end leg with the
-    frequency values in pinned host memory."""
+def oracle_sample(specs: list, mine: list, workload: str) -> list:
+    """Positions (within `mine`) of the transforms whose FP32 results are checked against the FP64
+    oracle: for c2c_128_uneven256 the smallest and the largest radius plus the first others (8 in
+    all); otherwise the first transform of every (grid size, transform type) (16 for mixed_512)."""
+    if workload == "c2c_128_uneven256":
+        radii = [specs[j][1] for j in mine]
+        pick = [int(np.argmin(radii)), int(np.argmax(radii))]
+        pick += [i for i in range(len(mine)) if i not in pick][:6]
+        return sorted(set(pick))
+    first = {}
+    for i, j in enumerate(mine):
+        n, _, r2c = specs[j]
+        first.setdefault((n, r2c), i)
+    return sorted(first.values())
+
+
+def measure_batch_workload(args, rank: int, world: int, workload: str | None = None,
+                           compact: bool = False) -> dict:
+    """A batch of independent transforms (sharded over the ranks by algorithmic bytes, no
+    collective): FP32 pairs/s as one captured graph per step, the FP64 plain drop-in path over the
+    same transforms one by one, the FP32 error against the FP64 oracle on a sample and against the
+    FP64 GPU path on every transform, per-pass roofline, and (unless `compact`) an end-to-end leg
+    with the frequency values in pinned host memory."""
     import torch
 
     import spfft_gb300 as sp
 
+    workload = workload or args.workload
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(dev)
-    specs_all = batch_specs(args.workload)
-    mine = shard(len(specs_all), rank, world)
+    specs_all = batch_specs(workload)
+    mine = shard([transform_cost(*sp_) for sp_ in specs_all], rank, world)
     idxs, hosts, geo = [], [], []
     for j in mine:
         n, radius, r2c = specs_all[j]
@@ -704,19 +911,21 @@ def measure_batch_workload(args, rank: int, world: int) -> dict:
 
     stream = torch.cuda.Stream()
     # ---- FP32 batched -------------------------------------------------------------------------
-    # creation of the whole set with the host planner (discarded), then with the default planner
-    os.environ["SPFFT_GB300_PLANNER"] = "host"
-    t0 = time.perf_counter()
-    discard = make("float32")
-    create_host_s = time.perf_counter() - t0
-    del os.environ["SPFFT_GB300_PLANNER"], discard
+    creation = {}
+    if not compact:
+        # creation of the whole set with the host planner (discarded), then the default planner
+        os.environ["SPFFT_GB300_PLANNER"] = "host"
+        t0 = time.perf_counter()
+        discard = make("float32")
+        creation["ms_total_host_planner"] = round((time.perf_counter() - t0) * 1e3, 1)
+        del os.environ["SPFFT_GB300_PLANNER"], discard
     plans_before = sp.plan_cache_size()
     t0 = time.perf_counter()
     trs32, vals32, spaces32, ct32 = make("float32")
     create_s = time.perf_counter() - t0
-    creation = {"ms_total": round(create_s * 1e3, 1), "ms_total_host_planner": round(create_host_s * 1e3, 1),
-                "transforms": len(trs32), "index_plans": sp.plan_cache_size() - plans_before,
-                "includes": "index planning, device tables, grid buffers, value and space buffers"}
+    creation.update({"ms_total": round(create_s * 1e3, 1), "transforms": len(trs32),
+                     "index_plans": sp.plan_cache_size() - plans_before,
+                     "includes": "index planning, device tables, grid buffers, value and space buffers"})
     bt = sp.Batch(trs32)
     bt.bind(vals32, spaces32)
     if not args.no_autotune:
@@ -764,49 +973,58 @@ def measure_batch_workload(args, rank: int, world: int) -> dict:
     roofline = {"bound": "hbm", "kernel": dominant + "_batch", "achieved": round(achieved, 1), "peak": peak,
                 "unit": "GB/s", "frac": round(achieved / peak, 4),
                 "peak_source": "measured" if "hbm_gbs" in peaks else "fallback",
-                "traffic": load_traffic_table().get((dominant + "_batch", args.workload, "float32")),
+                "traffic": load_traffic_table().get((dominant + "_batch", workload, "float32")),
                 "algorithmic_bytes": pass_bytes[dominant],
                 "pass_ms": {k: round(v, 4) for k, v in pass_ms.items()},
                 "pass_gbs": {k: round(pass_bytes[k] / (pass_ms[k] * 1e-3) / 1e9, 1) for k in pass_ms
                              if pass_bytes[k]}}
 
     # ---- end to end: values from / to pinned host memory around the captured pair ---------------
-    hv = [torch.from_numpy(v).to(ct32).pin_memory() for v in hosts]
-    ho = [torch.empty_like(h).pin_memory() for h in hv]
-    e2e_steps = max(3, args.steps)
+    e2e = None
+    if not compact:
+        hv = [torch.from_numpy(v).to(ct32).pin_memory() for v in hosts]
+        ho = [torch.empty_like(h).pin_memory() for h in hv]
+        e2e_steps = max(3, args.steps)
 
-    def e2e_step():
-        with torch.cuda.stream(stream):
-            for d, h in zip(vals32, hv):
-                d.copy_(h, non_blocking=True)
-            bt.pair_graph(sp.SPFFT_FULL_SCALING, stream)
-            for h, d in zip(ho, vals32):
-                h.copy_(d, non_blocking=True)
-        stream.synchronize()
+        def e2e_step():
+            with torch.cuda.stream(stream):
+                for d, h in zip(vals32, hv):
+                    d.copy_(h, non_blocking=True)
+                bt.pair_graph(sp.SPFFT_FULL_SCALING, stream)
+                for h, d in zip(ho, vals32):
+                    h.copy_(d, non_blocking=True)
+            stream.synchronize()
 
-    for _ in range(2):
-        e2e_step()
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        e2e_step()
-    e2e_s = time.perf_counter() - t0
-    vbytes = int(sum(h.numel() * h.element_size() for h in hv))
-    e2e = {"value": round(len(specs_all) * e2e_steps / e2e_s, 2), "unit": UNIT,
-           "h2d_bytes_per_step": vbytes * world, "d2h_bytes_per_step": vbytes * world,
-           "buffers": "frequency values in pinned host memory, space domains on the device"}
+        for _ in range(2):
+            e2e_step()
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            e2e_step()
+        e2e_s = time.perf_counter() - t0
+        vbytes = int(sum(h.numel() * h.element_size() for h in hv))
+        e2e = {"value": round(len(specs_all) * e2e_steps / e2e_s, 2), "unit": UNIT,
+               "h2d_bytes_per_step": vbytes * world, "d2h_bytes_per_step": vbytes * world,
+               "buffers": "frequency values in pinned host memory, space domains on the device"}
 
-    # ---- FP32 error against the FP64 drop-in path on a sample ----------------------------------
-    trs64, vals64, spaces64, ct64 = make("float64")
+    # ---- FP32 against the FP64 oracle on a sample (backward, then scaled forward) ---------------
     for d, h in zip(vals32, hosts):
         d.copy_(torch.from_numpy(h).to(ct32))
     bt.backward(stream)
     stream.synchronize()
-    # every transform of this rank: relative L2 and relative max-abs error of the FP32 backward
-    # (space) and of the FP32 forward of that space (values), each against the FP64 path
-    sample = list(range(len(mine)))
+    picked = oracle_sample(specs_all, mine, workload)
+    space_h = {i: spaces32[i].cpu().numpy() for i in picked}
+    bt.forward(sp.SPFFT_FULL_SCALING, stream)  # batched scaled forward of the FP32 space domains
+    stream.synchronize()
+    fwd32 = [v.clone() for v in vals32]
+    vs_oracle = oracle_errors([(f"{workload}[{mine[i]}] {specs_all[mine[i]][0]}^3 "
+                                f"{'R2C' if specs_all[mine[i]][2] else 'C2C'}",
+                                specs_all[mine[i]][0], specs_all[mine[i]][2], idxs[i], hosts[i],
+                                space_h[i], fwd32[i].cpu().numpy()) for i in picked])
+
+    # ---- FP32 against the FP64 GPU path on every transform of this rank --------------------------
+    trs64, vals64, spaces64, ct64 = make("float64")
     errs_b, errs_f, maxabs_b, maxabs_f = [], [], [], []
-    out32 = [torch.empty_like(vals32[i]) for i in range(len(mine))]
-    for i in sample:
+    for i in range(len(mine)):
         trs64[i].backward(vals64[i], spaces64[i])
         d = (spaces32[i].to(spaces64[i].dtype) - spaces64[i]).flatten()
         ref = spaces64[i].flatten()
@@ -814,8 +1032,7 @@ def measure_batch_workload(args, rank: int, world: int) -> dict:
         maxabs_b.append(float(d.abs().max() / ref.abs().max()))
         f64 = torch.empty_like(vals64[i])
         trs64[i].forward(spaces64[i], f64, sp.SPFFT_FULL_SCALING)
-        trs32[i].forward(spaces32[i], out32[i], sp.SPFFT_FULL_SCALING)
-        d = (out32[i].to(ct64) - f64).flatten()
+        d = (fwd32[i].to(ct64) - f64).flatten()
         errs_f.append(float(torch.linalg.vector_norm(d) / torch.linalg.vector_norm(f64.flatten())))
         maxabs_f.append(float(d.abs().max() / f64.abs().max()))
 
@@ -840,7 +1057,8 @@ def measure_batch_workload(args, rank: int, world: int) -> dict:
             plain_step()
     a1.record(stream)
     torch.cuda.synchronize()
-    plain = len(mine) * psteps / (a0.elapsed_time(a1) / 1e3) * world
+    plain_ms = max_over_ranks(a0.elapsed_time(a1), world)
+    plain = len(specs_all) * psteps / (plain_ms / 1e3)
     info = bt.info()
     del trs64, vals64, spaces64
     return {"value": value, "ms_per_step": total_ms / args.steps, "clocks": clocks.summary(),
@@ -848,13 +1066,26 @@ def measure_batch_workload(args, rank: int, world: int) -> dict:
             "launches_per_step": info["launches_per_pair"], "groups": info["groups"],
             "creation": creation,
             "unbatched": info["unbatched"], "fp64_plain": plain,
-            "err_backward": max(errs_b), "err_forward": max(errs_f), "sampled": len(sample),
+            "vs_oracle": vs_oracle,
+            "err_backward": max(errs_b), "err_forward": max(errs_f), "sampled": len(mine),
             "err_stats": {"backward_space_rel_l2": {"max": max(errs_b), "median": statistics.median(errs_b)},
                           "backward_space_rel_maxabs": {"max": max(maxabs_b), "median": statistics.median(maxabs_b)},
                           "forward_values_rel_l2": {"max": max(errs_f), "median": statistics.median(errs_f)},
-                          "forward_values_rel_maxabs": {"max": max(maxabs_f), "median": statistics.median(maxabs_f)},
-                          "per_transform_backward_rel_l2": [float(f"{e:.3g}") for e in errs_b]},
+                          "forward_values_rel_maxabs": {"max": max(maxabs_f), "median": statistics.median(maxabs_f)}},
             "transforms": len(specs_all)}
+
+
+def batch_config_summary(res: dict) -> dict:
+    """Compact form of measure_batch_workload's result for the default benchmark line."""
+    return {"fp32_batched": {"value": round(res["value"], 2), "unit": UNIT,
+                             "ms_per_step": round(res["ms_per_step"], 4),
+                             "kernel_launches_per_pair": res["launches_per_step"],
+                             "shape_groups": res["groups"]},
+            "fp64_plain": {"value": round(res["fp64_plain"], 2), "unit": UNIT},
+            "ratio_fp32_batched_vs_fp64_plain": round(res["value"] / res["fp64_plain"], 2),
+            "roofline": {k: res["roofline"][k] for k in ("bound", "kernel", "achieved", "peak", "unit", "frac")},
+            "fp32_vs_fp64_oracle": {k: v for k, v in res["vs_oracle"].items()},
+            "clocks": res["clocks"]}
 
 
 def cpu_batch_pairs_per_s(workload: str, min_seconds: float, max_pairs: int, exact: bool = False,
@@ -892,6 +1123,19 @@ def cpu_batch_pairs_per_s(workload: str, min_seconds: float, max_pairs: int, exa
                       f"of the reference host pipeline, {cores} threads, plans built before timing), {dt:.2f} s"}
 
 
+def relaunch_ranks(n: int) -> int:
+    """`--gpus N` (N > 1) without a launcher: start N ranks on this node, one process per GPU,
+    through torch.distributed.run with the same arguments, and return its exit status."""
+    import socket
+
+    with socket.socket() as sock:
+        sock.bind(("127.0.0.1", 0))
+        port = sock.getsockname()[1]
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={n}",
+           "--master-addr=127.0.0.1", f"--master-port={port}", str(Path(__file__).resolve()), *sys.argv[1:]]
+    return subprocess.call(cmd)
+
+
 def main() -> int:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -907,11 +1151,27 @@ def main() -> int:
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the plan-time default tile shapes instead of running the autotuner")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="leave the other configurations' compact legs out of the default line")
+    ap.add_argument("--no-reference-gpu", action="store_true",
+                    help="leave out the timing of the reference's own GPU path")
+    ap.add_argument("--launch-check", action="store_true",
+                    help="print this rank's place in the job as JSON and exit, before any GPU work")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
-    world = int(os.environ.get("WORLD_SIZE", "1"))
+    env_world = os.environ.get("WORLD_SIZE")
+    if env_world is None and args.gpus > 1 and args.impl == "ours":
+        return relaunch_ranks(args.gpus)
+    world = int(env_world or "1")
     rank = int(os.environ.get("RANK", "0"))
+    if args.impl == "ours" and world != args.gpus:
+        print(f"bench.py: --gpus {args.gpus} does not match the launcher's WORLD_SIZE {world}", file=sys.stderr)
+        return 2
+    if args.launch_check:
+        print(json.dumps({"rank": rank, "world_size": world,
+                          "local_rank": int(os.environ.get("LOCAL_RANK", "0")), "gpus": args.gpus}), flush=True)
+        return 0
     if args.workload in BATCH_WORKLOADS:
         return batch_main(args, rank, world)
     n, radius, r2c = WORKLOADS[args.workload]
@@ -953,14 +1213,15 @@ def main() -> int:
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(res["ms_per_step"], 4),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64" if args.dtype == "float64" else "f32", "data": "synthetic",
-        "config": {**config, "frequency_values": res["npts"], "z_sticks": res["nsticks"],
-                   "x_columns": res["ncols"]},
+        "config": config,
+        "workload_stats": {"frequency_values": res["npts"], "z_sticks": res["nsticks"], "x_columns": res["ncols"]},
         "roofline": res["roofline"],
         "hbm_gbs_per_pair_accounting": round(res["pair_gbs"], 1),
         "e2e": res["e2e"], "clocks": res["clocks"],
         "gpu_launches": res["launches_per_step"] * args.steps,
         "roundtrip_rel_l2": res["roundtrip_rel_l2"], "tuning": res["tuning"],
         "cufft_dense_comparison": res["cufft_dense"],
+        "reference_gpu": res["reference_gpu"],
         "transform_creation_ms": {"device_planner": round(res["plan_ms"], 2),
                                   "host_planner": round(res["plan_host_ms"], 2)},
     }
@@ -969,6 +1230,15 @@ def main() -> int:
         line["fp32_batched"]["ratio_vs_value"] = round(res["batched"]["value"] / res["pairs_per_s"], 2)
     if res["grad"]:
         line["differentiation"] = res["grad"]
+    if world == 1 and not args.no_configs and args.workload == "r2c_192_sphere48":
+        # the other configurations, compact: 64^3 C2C FP64 plain, and the two batched sets (FP32
+        # batched against FP64 plain, FP32 error per transform against the FP64 oracle)
+        line["configs"] = {
+            "c2c_64_sphere16": measure_plain_compact(args, "c2c_64_sphere16"),
+            "c2c_128_uneven256": batch_config_summary(
+                measure_batch_workload(args, 0, 1, "c2c_128_uneven256", compact=True)),
+            "mixed_512": batch_config_summary(measure_batch_workload(args, 0, 1, "mixed_512", compact=True)),
+        }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_pairs_per_s(args.workload, args.cpu_seconds, 400)
         line["cpu_baseline"]["value"] = round(line["cpu_baseline"]["value"], 3)
@@ -1023,9 +1293,10 @@ def batch_main(args, rank: int, world: int) -> int:
         "transform_creation": res["creation"],
         "fp64_plain": {"value": round(res["fp64_plain"], 2), "unit": UNIT,
                        "ratio_fp32_batched_vs_fp64_plain": round(res["value"] / res["fp64_plain"], 2)},
-        "fp32_vs_fp64_errors": res["err_stats"],
-        "fp32_vs_fp64_rel_l2_max": {"backward_space": res["err_backward"], "forward_values": res["err_forward"],
-                                    "transforms_checked": res["sampled"]},
+        "fp32_vs_fp64_oracle": res["vs_oracle"],
+        "fp32_vs_fp64_gpu_errors": res["err_stats"],
+        "fp32_vs_fp64_gpu_rel_l2_max": {"backward_space": res["err_backward"], "forward_values": res["err_forward"],
+                                        "transforms_checked": res["sampled"]},
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_batch_pairs_per_s(args.workload, args.cpu_seconds, 2000)
