@@ -10,6 +10,13 @@ on the current CUDA stream and register the hand-written adjoints
   those multiplicities for R2C, scaled like the forward.
 
 Gradients use PyTorch's convention for complex tensors (dL/dRe + i dL/dIm).
+
+Concurrency: every call (the transform and its adjoint alike) runs on the transform's one set of
+intermediate buffers (its grid's stick and plane scratch). Calls that use the same transform must
+therefore not overlap on the GPU: two autograd graphs that run one transform on different CUDA
+streams at the same time race on that scratch and corrupt each other's results. Give each
+concurrently used stream its own Transform (``Transform.clone()`` creates one with its own grid),
+or order the streams.
 """
 from __future__ import annotations
 
