@@ -174,43 +174,39 @@ __host__ __device__ __forceinline__ dd dd_assemble(unsigned sign, int e, unsigne
   return dd(hi, lo);
 }
 
-// Subnormal v (nonzero, exponent field 0) times 2^k as dd: the fraction is shifted up to the
-// implicit bit and the exponent lowered to match (E = 1 - shift). Kept out of line: no binary64
-// value but a subnormal takes this path.
-static __host__ __device__ __noinline__ dd dd_from_subnormal(unsigned long long u, int k) {
-  const unsigned sign = static_cast<unsigned>(u >> 32) & 0x80000000u;
+// v * 2^k as dd: hi takes the top 24 significant bits of v (truncated), lo the next 23 (the last
+// 6 of binary64's 53 are dropped: relative error below 2^-46). lo is formed exactly on the FP32
+// pipe as (2^(e-23) * 1.f) - 2^(e-23) from two assembled bit patterns, so no count of leading
+// zeros or variable shift is needed. Values whose scaled exponent e is below -126 become signed
+// zero (their lo already below e = -103), and so do binary64 subnormals; above 127 they become
+// infinity. Callers choose k so that the block maximum lands in [1, 2); subnormals then lie more
+// than 2^60 below it unless k >= 962, where the callers use dd_from_double_exact.
+__host__ __device__ __forceinline__ dd dd_from_double(double v, int k) {
+  const unsigned long long u = dd_bits64(v);
+  const unsigned hw = static_cast<unsigned>(u >> 32), lw = static_cast<unsigned>(u);
+  const unsigned sign = hw & 0x80000000u;
+  const int E = static_cast<int>((hw >> 20) & 0x7ffu);
+  const int e = E - 1023 + k;
+  if (e > 127) {  // overflow, or inf / NaN (k = 0 for blocks that hold them)
+    const bool nan = E == 0x7ff && (((hw & 0xFFFFFu) | lw) != 0u);
+    return dd(dd_float_from_bits(sign | 0x7f800000u | (nan ? 0x400000u : 0u)), 0.0f);
+  }
+  return dd_assemble(sign, E == 0 ? -1000 : e, ((hw & 0xFFFFFu) << 3) | (lw >> 29), (lw >> 6) & 0x7FFFFFu);
+}
+
+// dd_from_double for every binary64 class: a subnormal v is normalised first (its fraction
+// shifted up to the implicit bit, its exponent lowered to match: E = 1 - shift).
+__host__ __device__ __forceinline__ dd dd_from_double_exact(double v, int k) {
+  const unsigned long long u = dd_bits64(v);
   const unsigned long long f = u & 0xFFFFFFFFFFFFFull;
+  if (((u >> 52) & 0x7ffu) != 0u || f == 0ull) return dd_from_double(v, k);
+  const unsigned sign = static_cast<unsigned>(u >> 32) & 0x80000000u;
   const int lz = dd_clz64(f) - 11;  // 1 .. 52
   const unsigned long long m = (f << lz) & 0xFFFFFFFFFFFFFull;
   const unsigned hw = static_cast<unsigned>(m >> 32), lw = static_cast<unsigned>(m);
   const int e = (1 - lz) - 1023 + k;
   if (e > 127) return dd(dd_float_from_bits(sign | 0x7f800000u), 0.0f);
   return dd_assemble(sign, e, (hw << 3) | (lw >> 29), (lw >> 6) & 0x7FFFFFu);
-}
-
-// v * 2^k as dd: hi takes the top 24 significant bits of v (truncated), lo the next 23 (the last
-// 6 of binary64's 53 are dropped: relative error below 2^-46). lo is formed exactly on the FP32
-// pipe as (2^(e-23) * 1.f) - 2^(e-23) from two assembled bit patterns, so no count of leading
-// zeros or variable shift is needed for normal values; a subnormal v is normalised first
-// (dd_from_subnormal). Values whose scaled exponent e is below -126 become signed zero (their lo
-// already below e = -103); above 127 they become infinity. Callers choose k so that the block
-// maximum lands in [1, 2).
-__host__ __device__ __forceinline__ dd dd_from_double(double v, int k) {
-  const unsigned long long u = dd_bits64(v);
-  const unsigned hw = static_cast<unsigned>(u >> 32), lw = static_cast<unsigned>(u);
-  const unsigned sign = hw & 0x80000000u;
-  const int E = static_cast<int>((hw >> 20) & 0x7ffu);
-  if (E == 0) {
-    if (((hw & 0xFFFFFu) | lw) != 0u) return dd_from_subnormal(u, k);
-    const float z = dd_float_from_bits(sign);
-    return dd(z, z);
-  }
-  const int e = E - 1023 + k;
-  if (e > 127) {  // overflow, or inf / NaN (k = 0 for blocks that hold them)
-    const bool nan = E == 0x7ff && (((hw & 0xFFFFFu) | lw) != 0u);
-    return dd(dd_float_from_bits(sign | 0x7f800000u | (nan ? 0x400000u : 0u)), 0.0f);
-  }
-  return dd_assemble(sign, e, ((hw & 0xFFFFFu) << 3) | (lw >> 29), (lw >> 6) & 0x7FFFFFu);
 }
 
 // Rounded m * 2^s for s <= 28 (round half up), as an integer count.
@@ -220,35 +216,14 @@ __host__ __device__ __forceinline__ unsigned long long dd_shift_round(unsigned m
   return (static_cast<unsigned long long>(m) + (1ull << (-s - 1))) >> (-s);
 }
 
-// A normalised pair (hb, lb: the bit patterns of hi and lo after two_sum, hi normal) whose scaled
-// value lies below the binary64 normal range (E, the biased binary64 exponent of hi * 2^k, at most
-// 0), as a subnormal double: hi * 2^k = Mh * 2^(E + 28) and lo * 2^k = Ml * 2^(E + 28 + el' - eh)
-// in units of 2^-1074 (el' = 1 for a subnormal lo), each rounded to an integer count and added
-// (an error of at most one subnormal unit). A count of 2^52 is the smallest normal, which the bit
-// pattern encodes by itself. Kept out of line: only results below 2^-1022 take this path.
-static __host__ __device__ __noinline__ double dd_to_subnormal_double(unsigned hb, unsigned lb, int E) {
-  const unsigned sign = hb & 0x80000000u;
-  if (E < -60) return dd_double_from_bits(static_cast<unsigned long long>(sign) << 32);
-  const int eh = static_cast<int>((hb >> 23) & 0xffu);
-  const int el = static_cast<int>((lb >> 23) & 0xffu);
-  const unsigned ml = el ? ((lb & 0x7FFFFFu) | 0x800000u) : (lb & 0x7FFFFFu);
-  const int sh = E + 28;
-  const unsigned long long H = dd_shift_round((hb & 0x7FFFFFu) | 0x800000u, sh);
-  const unsigned long long L = dd_shift_round(ml, sh + (el ? el : 1) - eh);
-  const bool opposite = ((hb ^ lb) >> 31) != 0u;
-  const unsigned long long T = opposite ? (H > L ? H - L : 0ull) : H + L;
-  return dd_double_from_bits((static_cast<unsigned long long>(sign) << 32) | T);
-}
-
 // (hi + lo) * 2^k as a double, faithfully rounded (error below one unit in the last place), for
 // any pair of binary32 values whose sum is finite: two_sum first makes |lo| <= ulp(hi) / 2, then
 // lo is added to hi's binary64 bit pattern as an integer count of binary64 ulps of hi (at most
 // 2^28 in magnitude, so the sum never carries into the next binade; when hi is a power of two and
 // lo pulls below it the count is doubled, since the ulps there are half as large, except at the
 // bottom of the normal range where the subnormal ulps below are not). Scaled results below the
-// binary64 normal range are assembled as subnormals (dd_to_subnormal_double); results below half
-// the smallest subnormal become signed zero, above the normal range infinity; inf / NaN in hi pass
-// through. Integer and FP32 instructions only.
+// binary64 normal range become signed zero (dd_to_double_exact assembles them as subnormals),
+// above it infinity; inf / NaN in hi pass through. Integer and FP32 instructions only.
 __host__ __device__ __forceinline__ double dd_to_double(dd v, int k) {
   const dd n = dd_two_sum(v.hi, v.lo);
   const unsigned hb = dd_bits32(n.hi), lb = dd_bits32(n.lo);
@@ -259,8 +234,7 @@ __host__ __device__ __forceinline__ double dd_to_double(dd v, int k) {
                                ((hb & 0x7fffffu) ? 0x8000000000000ull : 0ull));
   }
   const int E = eh - 127 + k + 1023;  // biased binary64 exponent of hi * 2^k
-  if (eh == 0) return dd_double_from_bits(static_cast<unsigned long long>(sign) << 32);
-  if (E <= 0) return dd_to_subnormal_double(hb, lb, E);
+  if (eh == 0 || E <= 0) return dd_double_from_bits(static_cast<unsigned long long>(sign) << 32);
   if (E >= 2047) return dd_double_from_bits((static_cast<unsigned long long>(sign) << 32) | 0x7ff0000000000000ull);
   const unsigned long long H =
       (static_cast<unsigned long long>(sign | (static_cast<unsigned>(E) << 20) | ((hb >> 3) & 0xFFFFFu)) << 32) |
@@ -279,6 +253,30 @@ __host__ __device__ __forceinline__ double dd_to_double(dd v, int k) {
   }
   const unsigned long long Y = static_cast<unsigned long long>(y);
   return dd_double_from_bits(opposite ? H - Y : H + Y);
+}
+
+// dd_to_double with results below the binary64 normal range assembled as subnormals: for a
+// normalised pair (hb, lb after two_sum, hi normal) with E, the biased binary64 exponent of
+// hi * 2^k, at most 0, hi * 2^k = Mh * 2^(E + 28) and lo * 2^k = Ml * 2^(E + 28 + el' - eh) in units
+// of 2^-1074 (el' = 1 for a subnormal lo), each rounded to an integer count and added (an error
+// of at most one subnormal unit). A count of 2^52 is the smallest normal, which the bit pattern
+// encodes by itself. Results below half the smallest subnormal become signed zero.
+__host__ __device__ __forceinline__ double dd_to_double_exact(dd v, int k) {
+  const dd n = dd_two_sum(v.hi, v.lo);
+  const unsigned hb = dd_bits32(n.hi), lb = dd_bits32(n.lo);
+  const int eh = static_cast<int>((hb >> 23) & 0xffu);
+  const int E = eh - 127 + k + 1023;
+  if (eh == 0xff || eh == 0 || E > 0) return dd_to_double(v, k);
+  const unsigned sign = hb & 0x80000000u;
+  if (E < -60) return dd_double_from_bits(static_cast<unsigned long long>(sign) << 32);
+  const int el = static_cast<int>((lb >> 23) & 0xffu);
+  const unsigned ml = el ? ((lb & 0x7FFFFFu) | 0x800000u) : (lb & 0x7FFFFFu);
+  const int sh = E + 28;
+  const unsigned long long H = dd_shift_round((hb & 0x7FFFFFu) | 0x800000u, sh);
+  const unsigned long long L = dd_shift_round(ml, sh + (el ? el : 1) - eh);
+  const bool opposite = ((hb ^ lb) >> 31) != 0u;
+  const unsigned long long T = opposite ? (H > L ? H - L : 0ull) : H + L;
+  return dd_double_from_bits((static_cast<unsigned long long>(sign) << 32) | T);
 }
 
 }  // namespace gb300

@@ -54,6 +54,15 @@ template <>
 struct YMinBlocks<dd> {
   static constexpr int value = 3;
 };
+// The double-float z forward kernel keeps three 256-thread blocks per SM (at most 80 registers).
+template <typename A>
+struct ZForwardMinBlocks {
+  static constexpr int value = 1;
+};
+template <>
+struct ZForwardMinBlocks<dd> {
+  static constexpr int value = 3;
+};
 template <>
 struct BatchPlaneThreads<dd> {
   static constexpr int value = batch_plane_threads<double>();
@@ -96,6 +105,42 @@ __device__ __forceinline__ float2 to_storage(float2 v, int) { return v; }
 __device__ __forceinline__ double2 to_storage(ddc v, int k) {
   return make_double2(dd_to_double(v.x, -k), dd_to_double(v.y, -k));
 }
+// The same conversions for every binary64 class: subnormal inputs normalised, results below
+// 2^-1022 assembled as subnormals.
+__device__ __forceinline__ float2 to_arith_exact(float2 v, int) { return v; }
+__device__ __forceinline__ ddc to_arith_exact(double2 v, int k) {
+  return make_c(dd_from_double_exact(v.x, k), dd_from_double_exact(v.y, k));
+}
+__device__ __forceinline__ float2 to_storage_exact(float2 v, int) { return v; }
+__device__ __forceinline__ double2 to_storage_exact(ddc v, int k) {
+  return make_double2(dd_to_double_exact(v.x, -k), dd_to_double_exact(v.y, -k));
+}
+// Which conversions a block needs. A block scaled by k brings its largest magnitude into [1, 2),
+// and its largest FFT output is at least that large (Parseval), so binary64 subnormals -- inputs or
+// outputs -- lie below 2^(k - 1022) of the block's largest value. Below k = 962 that is under 2^-60
+// and the fast conversions flush them to zero; blocks of tiny values (largest magnitude below
+// 2^-961) use the exact ones. k is the same for every thread of a block, so every branch on it is
+// uniform and the exact code never runs in ordinary blocks.
+constexpr int kExactScale = 962;
+__device__ __forceinline__ bool exact_block(int k) { return k >= kExactScale; }
+struct FastStore {
+  template <typename CA>
+  __device__ __forceinline__ auto operator()(CA v, int k) const { return to_storage(v, k); }
+};
+struct ExactStore {
+  template <typename CA>
+  __device__ __forceinline__ auto operator()(CA v, int k) const { return to_storage_exact(v, k); }
+};
+// Runs `store(conv)` with the storage conversion the block's scale k needs (outputs held in
+// registers).
+template <typename F>
+__device__ __forceinline__ void with_store(int k, F&& store) {
+  if (exact_block(k)) {
+    store(ExactStore{});
+  } else {
+    store(FastStore{});
+  }
+}
 // twiddles: double tables -> dd, float tables as they are
 __device__ __forceinline__ float2 tw_arith(float2 v) { return v; }
 __device__ __forceinline__ ddc tw_arith(double2 v) {
@@ -124,16 +169,37 @@ __device__ __forceinline__ int block_scale(int e) { return dd_block_scale(e); }
 // max_subnormal_key, into sExp[1] and stores the exact key (0 for an all-zero block) in sExp[0].
 // Returns the key. Only that rare case adds a barrier; every thread has read sExp[0] before it, so
 // thread 0's store races with no reader.
+// The rare part is a separate function (not inlined) so that it costs the common path no
+// registers; `scan` captures by value.
 template <typename Scan>
-__device__ __forceinline__ int finish_block_key(int* sExp, Scan scan) {
-  const int e0 = sExp[0];
-  if (e0 != 0) return e0;
+__device__ __noinline__ int subnormal_block_key(int* sExp, Scan scan) {
   atomicMax(sExp + 1, scan());
   __syncthreads();
   const int sub = sExp[1];
   const int key = sub == kDdNoSubnormal ? 0 : sub;
   if (threadIdx.x == 0) sExp[0] = key;
   return key;
+}
+template <typename Scan>
+__device__ __forceinline__ int finish_block_key(int* sExp, Scan scan) {
+  const int e0 = sExp[0];
+  if (e0 != 0) return e0;
+  return subnormal_block_key(sExp, scan);
+}
+// Outputs that sit in shared memory: a block of tiny values converts them in place to storage
+// form first (exactly; n slots from `buf`, strided over `nthreads` threads from `tid`; the caller
+// synchronises), and the store loop reads them with stored_value instead of converting.
+template <typename S, typename A>
+__device__ __forceinline__ void convert_exact_in_place(typename Types<S, A>::CA* buf, int n, int k, int tid,
+                                                       int nthreads) {
+  using CS = typename Types<S, A>::CS;
+  for (int i = tid; i < n; i += nthreads) reinterpret_cast<CS*>(buf)[i] = to_storage_exact(buf[i], k);
+}
+template <typename S, typename A>
+__device__ __forceinline__ typename Types<S, A>::CS stored_value(const typename Types<S, A>::CA* slot, int k,
+                                                                 bool converted) {
+  using CS = typename Types<S, A>::CS;
+  return converted ? *reinterpret_cast<const CS*>(slot) : to_storage(*slot, k);
 }
 
 // Double-float compact planes (PlanView::planesRaw): each producing block stores its scaled values
@@ -238,14 +304,21 @@ __device__ __forceinline__ int convert_block(typename Types<S, A>::CA* slots, in
   for (int i = threadIdx.x; i < n; i += blockDim.x) e = max(e, max_exponent(reinterpret_cast<const CS*>(slots)[i]));
   atomicMax(sExp, e);
   __syncthreads();
-  const int k = block_scale(finish_block_key(sExp, [&] {
+  const int k = block_scale(finish_block_key(sExp, [=] {
     int m = kDdNoSubnormal;
     for (int i = threadIdx.x; i < n; i += blockDim.x) m = max(m, max_subnormal_key(reinterpret_cast<const CS*>(slots)[i]));
     return m;
   }));
-  for (int i = threadIdx.x; i < n; i += blockDim.x) {
-    const CS raw = reinterpret_cast<const CS*>(slots)[i];
-    slots[i] = to_arith(raw, k);
+  if (exact_block(k)) {
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+      const CS raw = reinterpret_cast<const CS*>(slots)[i];
+      slots[i] = to_arith_exact(raw, k);
+    }
+  } else {
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+      const CS raw = reinterpret_cast<const CS*>(slots)[i];
+      slots[i] = to_arith(raw, k);
+    }
   }
   __syncthreads();
   return k;
@@ -347,10 +420,12 @@ __device__ __forceinline__ void z_backward_body(const PlanView<S>& p, const S* _
 #pragma unroll
       for (int k2 = 0; k2 < Bz; ++k2) rs[static_cast<size_t>(k1 + Az * k2) * p.numSticks + sl] = v[k2];
     } else {
+      with_store(k, [&](auto conv) {
 #pragma unroll
-      for (int k2 = 0; k2 < Bz; ++k2) {
-        sticks[static_cast<size_t>(k1 + Az * k2) * p.numSticks + sl] = to_storage(v[k2], k);
-      }
+        for (int k2 = 0; k2 < Bz; ++k2) {
+          sticks[static_cast<size_t>(k1 + Az * k2) * p.numSticks + sl] = conv(v[k2], k);
+        }
+      });
     }
   }
   if (raw && threadIdx.x < nsb) p.stickExp[s0 + threadIdx.x] = produced_exp(sExp, k);
@@ -433,10 +508,15 @@ __device__ __forceinline__ void z_forward_body(const PlanView<S>& p, S* __restri
   CS* out = reinterpret_cast<CS*>(values);
   const int e0 = p.stickEntryStart[s0], e1 = p.stickEntryStart[s0 + nsb];
   const int base = s0 * NZ;
+  const bool converted = TT::kScaled && exact_block(k);
+  if (converted) {
+    convert_exact_in_place<S, A>(buf, nsb * PZ, k, threadIdx.x, blockDim.x);
+    __syncthreads();
+  }
   for (int e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
     const int pos = p.entryPos[e] - base;
     const int sl = pos / NZ;
-    CS v = to_storage(buf[sl * PZ + transposed_pos<NZ, 1>(pos - sl * NZ)], k);
+    CS v = stored_value<S, A>(buf + sl * PZ + transposed_pos<NZ, 1>(pos - sl * NZ), k, converted);
     // scaling multiplies by S(1 / (Nx Ny Nz)) in S, like compress_kernel_scaled
     // (compression_kernels.cu:106-128)
     if (scale != S(0)) v = cscale(v, scale);
@@ -445,7 +525,7 @@ __device__ __forceinline__ void z_forward_body(const PlanView<S>& p, S* __restri
 }
 
 template <typename S, typename A, int NZ>
-__global__ void __launch_bounds__(kThreads) z_forward(const PlanView<S> p, S* __restrict__ values,
+__global__ void __launch_bounds__(kThreads, ZForwardMinBlocks<A>::value) z_forward(const PlanView<S> p, S* __restrict__ values,
                                                       S scale, int spb) {
   __shared__ int sExp[2];
   z_forward_body<S, A, NZ>(p, values, scale, spb, blockIdx.x, sExp);
@@ -660,8 +740,10 @@ __device__ __forceinline__ void plane_backward_body(const PlanView<S>& p, S* __r
       fft_pass2<L::LX, +1>(W + rl * L::WP + k1 * L::PAD, 1, k1, v);
       // C2C: complex x row; C2R: pairs (x[2m], x[2m+1]) of the real row
       CS* out = reinterpret_cast<CS*>(space + (static_cast<size_t>(z) * NY + r0 + rl) * NX * (R2C ? 1 : 2));
+      with_store(k, [&](auto conv) {
 #pragma unroll
-      for (int k2 = 0; k2 < Bx; ++k2) out[k1 + Ax * k2] = to_storage(v[k2], k);
+        for (int k2 = 0; k2 < Bx; ++k2) out[k1 + Ax * k2] = conv(v[k2], k);
+      });
     }
     rg.sync();
   }
@@ -735,7 +817,7 @@ __device__ __forceinline__ void plane_forward_body(const PlanView<S>& p, const S
   }
   __syncthreads();
   if (TT::kScaled) {
-    k = block_scale(finish_block_key(&sExp, [&] {
+    k = block_scale(finish_block_key(&sExp, [=] {
       int m = kDdNoSubnormal;
       for (int i = threadIdx.x; i < NY * L::LX; i += blockDim.x) m = max(m, max_subnormal_key(plane[i]));
       return m;
@@ -754,6 +836,16 @@ __device__ __forceinline__ void plane_forward_body(const PlanView<S>& p, const S
       cp_async_wait<0>();
     }
     rg.sync();
+    // a plane of tiny values converts its chunk exactly first (uniform branch)
+    const bool pre = TT::kScaled && exact_block(k);
+    if (pre) {
+      for (int i = rg.t; i < nr * L::LX; i += rg.threads) {
+        const int rl = i / L::LX, e = i - rl * L::LX;
+        CA* slot = wbase + rl * L::WP + L::wpos(e);
+        *slot = to_arith_exact(*reinterpret_cast<const CS*>(slot), k);
+      }
+      rg.sync();
+    }
     for (int i = rg.t; i < nr * Bx; i += rg.threads) {
       const int rl = i / Bx, b = i - rl * Bx;
       // padded row: element a*Bx + b sits at a*(Bx + PAD) + b (raw storage values until here)
@@ -761,7 +853,8 @@ __device__ __forceinline__ void plane_forward_body(const PlanView<S>& p, const S
       CA v[Ax];
 #pragma unroll
       for (int a = 0; a < Ax; ++a) {
-        v[a] = to_arith(reinterpret_cast<const CS*>(wrow)[a * (Bx + L::PAD) + b], k);
+        const int slot = a * (Bx + L::PAD) + b;
+        v[a] = pre ? wrow[slot] : to_arith(reinterpret_cast<const CS*>(wrow)[slot], k);
       }
       fft_pass1_regs<L::LX, -1>(v, b, twl);
 #pragma unroll
@@ -818,6 +911,11 @@ __device__ __forceinline__ void plane_forward_body(const PlanView<S>& p, const S
   __syncthreads();
   CS* sticks = reinterpret_cast<CS*>(p.sticks) + static_cast<size_t>(z) * p.numSticks;
   const int ns = p.numSticks;
+  const bool converted = TT::kScaled && exact_block(k);
+  if (converted) {
+    convert_exact_in_place<S, A>(s.P, NY * nc, k, threadIdx.x, blockDim.x);
+    __syncthreads();
+  }
   for (int st0 = threadIdx.x; st0 < ns; st0 += 4 * blockDim.x) {
     int pos[4];
 #pragma unroll
@@ -829,7 +927,7 @@ __device__ __forceinline__ void plane_forward_body(const PlanView<S>& p, const S
     for (int u = 0; u < 4; ++u) {
       if (pos[u] >= 0) {
         const int y = dnc.div(pos[u]), c = pos[u] - y * nc;
-        sticks[st0 + u * blockDim.x] = to_storage(s.P[transposed_pos<NY>(y) * nc + c], k);
+        sticks[st0 + u * blockDim.x] = stored_value<S, A>(s.P + transposed_pos<NY>(y) * nc + c, k, converted);
       }
     }
   }
@@ -1009,8 +1107,10 @@ __device__ __forceinline__ void y_backward_body(const PlanView<S>& p, int cpb, i
 #pragma unroll
       for (int k2 = 0; k2 < By; ++k2) rp[static_cast<size_t>(k1 + Ay * k2) * nc + c] = v[k2];
     } else {
+      with_store(k, [&](auto conv) {
 #pragma unroll
-      for (int k2 = 0; k2 < By; ++k2) planes[static_cast<size_t>(k1 + Ay * k2) * nc + c] = to_storage(v[k2], k);
+        for (int k2 = 0; k2 < By; ++k2) planes[static_cast<size_t>(k1 + Ay * k2) * nc + c] = conv(v[k2], k);
+      });
     }
   }
   if (raw && threadIdx.x < ncb) p.planeExp[z * nc + c0 + threadIdx.x] = produced_exp(sExp, k);
@@ -1088,6 +1188,11 @@ __device__ __forceinline__ void y_forward_body(const PlanView<S>& p, int cpb, in
   CS* sticks = reinterpret_cast<CS*>(p.sticks) + static_cast<size_t>(z) * p.numSticks;
   const int sBegin = p.columnStickStart[c0], sEnd = p.columnStickStart[c0 + ncb];
   const bool raw = TT::kScaled && p.sticksRaw;
+  const bool converted = TT::kScaled && !raw && exact_block(k);
+  if (converted) {
+    convert_exact_in_place<S, A>(buf, NY * ncb, k, threadIdx.x, blockDim.x);
+    __syncthreads();
+  }
   for (int st0 = sBegin + threadIdx.x; st0 < sEnd; st0 += 4 * blockDim.x) {
     int pos[4];
 #pragma unroll
@@ -1099,9 +1204,9 @@ __device__ __forceinline__ void y_forward_body(const PlanView<S>& p, int cpb, in
     for (int u = 0; u < 4; ++u) {
       if (pos[u] >= 0) {
         const int y = dnc.div(pos[u]), c = pos[u] - y * nc;
-        const CA v = buf[transposed_pos<NY, 1>(y) * ncb + (c - c0)];
-        if (raw) reinterpret_cast<CA*>(sticks)[st0 + u * blockDim.x] = v;
-        else sticks[st0 + u * blockDim.x] = to_storage(v, k);
+        const CA* slot = buf + transposed_pos<NY, 1>(y) * ncb + (c - c0);
+        if (raw) reinterpret_cast<CA*>(sticks)[st0 + u * blockDim.x] = *slot;
+        else sticks[st0 + u * blockDim.x] = stored_value<S, A>(slot, k, converted);
       }
     }
   }
@@ -1239,8 +1344,10 @@ __device__ __forceinline__ void x_backward_body(const PlanView<S>& p, S* __restr
     CA v[Bx];
     fft_pass2<L::LX, +1>(s.W + rl * L::WP + k1 * L::PAD, 1, k1, v);
     CS* out = reinterpret_cast<CS*>(space + (static_cast<size_t>(z) * ny + y0 + rl) * NX * (R2C ? 1 : 2));
+    with_store(k, [&](auto conv) {
 #pragma unroll
-    for (int k2 = 0; k2 < Bx; ++k2) out[k1 + Ax * k2] = to_storage(v[k2], k);
+      for (int k2 = 0; k2 < Bx; ++k2) out[k1 + Ax * k2] = conv(v[k2], k);
+    });
   }
 }
 
@@ -1290,7 +1397,7 @@ __device__ __forceinline__ void x_forward_body(const PlanView<S>& p, const S* __
   }
   __syncthreads();
   if (TT::kScaled) {
-    k = block_scale(finish_block_key(&sExp, [&] {
+    k = block_scale(finish_block_key(&sExp, [=] {
       int m = kDdNoSubnormal;
       for (RowWalk w(threadIdx.x, blockDim.x, L::LX); w.r < nr; w.next()) {
         m = max(m, max_subnormal_key(reinterpret_cast<const CS*>(s.W)[w.r * L::WP + L::wpos(w.c)]));
@@ -1298,13 +1405,26 @@ __device__ __forceinline__ void x_forward_body(const PlanView<S>& p, const S* __
       return m;
     }));
   }
+  // blocks of tiny values convert every slot exactly first (uniform branch); the FFT below then
+  // reads the converted slots
+  const bool pre = TT::kScaled && exact_block(k);
+  if (pre) {
+    for (RowWalk w(threadIdx.x, blockDim.x, L::LX); w.r < nr; w.next()) {
+      CA* slot = s.W + w.r * L::WP + L::wpos(w.c);
+      *slot = to_arith_exact(*reinterpret_cast<const CS*>(slot), k);
+    }
+    __syncthreads();
+  }
   const CA* twl = R2C ? s.twm : s.twx;
   for (int i = threadIdx.x; i < nr * Bx; i += blockDim.x) {
     const int rl = i / Bx, b = i - rl * Bx;
     CA* wrow = s.W + rl * L::WP;
     CA v[Ax];
 #pragma unroll
-    for (int a = 0; a < Ax; ++a) v[a] = to_arith(reinterpret_cast<const CS*>(wrow)[a * (Bx + L::PAD) + b], k);
+    for (int a = 0; a < Ax; ++a) {
+      const int slot = a * (Bx + L::PAD) + b;
+      v[a] = pre ? wrow[slot] : to_arith(reinterpret_cast<const CS*>(wrow)[slot], k);
+    }
     fft_pass1_regs<L::LX, -1>(v, b, twl);
 #pragma unroll
     for (int k1 = 0; k1 < Ax; ++k1) wrow[k1 * (Bx + L::PAD) + b] = v[k1];
@@ -1333,22 +1453,29 @@ __device__ __forceinline__ void x_forward_body(const PlanView<S>& p, const S* __
   CA* rawPlanes = reinterpret_cast<CA*>(planes);
   if (R2C) {
     // output columns straight to the compact plane rows (consecutive threads, consecutive columns)
-    for (int i = threadIdx.x; i < nr * nc; i += blockDim.x) {
-      const int rl = dnc.div(i), c = i - rl * nc;
-      const int4 ci = s.colInfo[c];
-      const CA* wrow = s.W + rl * L::WP;
-      const CA zk = wrow[ci.x];
-      const CA zm = wrow[ci.y];
-      const CA dif = make_c(zk.x - zm.x, zk.y + zm.y);
-      const CA u = cmul(dif, s.twx[ci.z]);
-      const CA xv = make_c(half_of(zk.x + zm.x + u.y), half_of(zk.y - zm.y - u.x));
-      if (raw) rawPlanes[i] = xv;
-      else planes[i] = to_storage(xv, k);
-    }
+    with_store(k, [&](auto conv) {
+      for (int i = threadIdx.x; i < nr * nc; i += blockDim.x) {
+        const int rl = dnc.div(i), c = i - rl * nc;
+        const int4 ci = s.colInfo[c];
+        const CA* wrow = s.W + rl * L::WP;
+        const CA zk = wrow[ci.x];
+        const CA zm = wrow[ci.y];
+        const CA dif = make_c(zk.x - zm.x, zk.y + zm.y);
+        const CA u = cmul(dif, s.twx[ci.z]);
+        const CA xv = make_c(half_of(zk.x + zm.x + u.y), half_of(zk.y - zm.y - u.x));
+        if (raw) rawPlanes[i] = xv;
+        else planes[i] = conv(xv, k);
+      }
+    });
   } else {
+    const bool converted = TT::kScaled && !raw && exact_block(k);
+    if (converted) {
+      convert_exact_in_place<S, A>(s.P, nr * nc, k, threadIdx.x, blockDim.x);
+      __syncthreads();
+    }
     for (int i = threadIdx.x; i < nr * nc; i += blockDim.x) {
       if (raw) rawPlanes[i] = s.P[i];
-      else planes[i] = to_storage(s.P[i], k);
+      else planes[i] = stored_value<S, A>(s.P + i, k, converted);
     }
   }
   if (raw && threadIdx.x < nr) p.planeExp[z * ny + y0 + threadIdx.x] = produced_exp(sExp, k);

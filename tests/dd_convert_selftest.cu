@@ -2,8 +2,9 @@
 // split accuracy (hi + lo within 2^-46 of v * 2^k), round trips, faithful rounding of dd_to_double
 // (within one binary64 ulp of the exact sum) on normalised pairs, on pairs whose lo is not below
 // hi, on powers of two with a negative lo and on all-ones mantissas with a positive lo, signs,
-// zeros, infinities and NaN; subnormal binary64 inputs (magnitude key, block scale, split, round
-// trip) and results in the subnormal range. Prints "ok <checks>" or the first failure.
+// zeros, infinities and NaN; subnormal binary64 inputs (subnormal key, block scale, split, round
+// trip; the exact conversions, which the fast ones match on normal values) and results in the
+// subnormal range. Prints "ok <checks>" or the first failure.
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -36,8 +37,18 @@ int main() {
       std::printf("split error v=%.17g k=%d\n", v, k);
       return 1;
     }
+    // the exact conversions agree bit for bit with the fast ones on normal values
+    const dd de = dd_from_double_exact(v, k);
+    if (de.hi != d.hi || de.lo != d.lo) {
+      std::printf("exact split differs v=%.17g\n", v);
+      return 1;
+    }
     // round trip
     const double back = dd_to_double(d, -k);
+    if (dd_to_double_exact(d, -k) != back) {
+      std::printf("exact combine differs v=%.17g\n", v);
+      return 1;
+    }
     if (std::fabs((back - v) / v) > std::ldexp(1.0, -46)) {
       std::printf("round trip error v=%.17g back=%.17g\n", v, back);
       return 1;
@@ -99,21 +110,26 @@ int main() {
       return 11;
     }
     const int kk = k - (i % 40);  // the value is not always the block maximum
-    const dd d = dd_from_double(v, kk);
+    const dd d = dd_from_double_exact(v, kk);
+    const dd flushed = dd_from_double(v, kk);  // the fast conversion flushes subnormals
+    if (flushed.hi != 0.0f || flushed.lo != 0.0f) {
+      std::printf("fast conversion kept a subnormal v=%.17g\n", v);
+      return 8;
+    }
     const long double want = std::ldexp((long double)v, kk);
     const long double got = (long double)d.hi + (long double)d.lo;
     if (std::fabs((double)((got - want) / want)) > std::ldexp(1.0, -46)) {
       std::printf("subnormal split error v=%.17g k=%d\n", v, kk);
       return 12;
     }
-    const double back = dd_to_double(d, -kk);
+    const double back = dd_to_double_exact(d, -kk);
     if (std::fabs(back - v) > std::ldexp(std::fabs(v), -46) + std::ldexp(1.0, -1074)) {
       std::printf("subnormal round trip v=%.17g back=%.17g\n", v, back);
       return 13;
     }
     // a subnormal scaled by a normal block maximum's k (2^-1022 .. 2^-1000 maxima)
     const int kn = dd_block_scale(1 + (i % 23));
-    const dd dn = dd_from_double(v, kn);
+    const dd dn = dd_from_double_exact(v, kn);
     const long double wn = std::ldexp((long double)v, kn);
     if (std::fabs(wn) >= std::ldexp(1.0L, -100) &&
         std::fabs((double)(((long double)dn.hi + (long double)dn.lo - wn) / wn)) > std::ldexp(1.0, -46)) {
@@ -128,7 +144,7 @@ int main() {
     const float b = (float)mant(rng) * std::ldexp(1.0f, -24 - (i % 8)) * ((i & 2) ? -1.0f : 1.0f);
     const dd n = dd_two_sum(a, b);
     const int k = -1022 - (i % 70);  // 2^k * [1, 2) from the smallest normal down past 2^-1074
-    const double got = dd_to_double(n, k);
+    const double got = dd_to_double_exact(n, k);
     const long double want = std::ldexp((long double)n.hi + (long double)n.lo, k);
     if (std::fabs((long double)got - want) > std::ldexp(1.0L, -1074)) {
       std::printf("subnormal result error hi=%.9g lo=%.9g k=%d got %.17g want %.17Lg\n", n.hi, n.lo, k, got, want);
