@@ -146,6 +146,12 @@ SPFFT_EXPORT SpfftError spfft_gb300_float_transform_autotune(SpfftFloatTransform
  * threads per block, [4] split: columns per y block, [5] split: rows per x block. */
 SPFFT_EXPORT SpfftError spfft_gb300_transform_tuning(SpfftTransform transform, int* tuning);
 SPFFT_EXPORT SpfftError spfft_gb300_float_transform_tuning(SpfftFloatTransform transform, int* tuning);
+/* Split plane passes: rows per block of the x backward kernel, which the autotuner chooses apart
+ * from the x forward kernel's (tuning[5]; it holds the compact rows besides the FFT rows, so fewer
+ * rows can let more blocks share an SM); 0 when the plane passes are not split. Starts equal to
+ * tuning[5] (SPFFT_GB300_XB_ROWS=n at transform creation sets n, where n is a candidate). */
+SPFFT_EXPORT SpfftError spfft_gb300_transform_x_backward_rows(SpfftTransform transform, int* rows);
+SPFFT_EXPORT SpfftError spfft_gb300_float_transform_x_backward_rows(SpfftFloatTransform transform, int* rows);
 
 /* The radix plans of the generic (runtime-radix) kernels for the z, y and x lengths: numStages[d]
  * stages with radices radices[d * 24 + 0 .. numStages[d] - 1] (d = 0 z, 1 y, 2 x; 24 slots per

@@ -133,6 +133,7 @@ def _declare(lib: ctypes.CDLL) -> None:
         getattr(lib, prefix + "transform_path_info").argtypes = [_vp, _ip]
         getattr(lib, prefix + "transform_autotune").argtypes = [_vp, _i, ctypes.POINTER(ctypes.c_float)]
         getattr(lib, prefix + "transform_tuning").argtypes = [_vp, _ip]
+        getattr(lib, prefix + "transform_x_backward_rows").argtypes = [_vp, _ip]
         getattr(lib, prefix + "transform_radix_plans").argtypes = [_vp, _ip, _ip]
         getattr(lib, prefix + "transform_adjoint_backward").argtypes = [_vp, _vp, _vp, _vp]
         getattr(lib, prefix + "transform_adjoint_forward").argtypes = [_vp, _vp, _vp, _i, _vp]
@@ -429,9 +430,11 @@ class Transform:
         """The tile shapes the transform runs with."""
         v = (ctypes.c_int * 6)()
         _call("spfft_gb300_" + self._p[len("spfft_"):] + "transform_tuning", self._h, v)
+        xb = ctypes.c_int(0)
+        _call("spfft_gb300_" + self._p[len("spfft_"):] + "transform_x_backward_rows", self._h, ctypes.byref(xb))
         return {"sticks_per_z_block": v[0], "plane": ("generic", "fused", "split")[v[1]],
                 "fused_half_rows": v[2], "fused_threads": v[3], "columns_per_y_block": v[4],
-                "rows_per_x_block": v[5]}
+                "rows_per_x_block": v[5], "rows_per_x_backward_block": xb.value}
 
     def radix_plans(self) -> list:
         """Radix stages of the generic kernels for the z, y and x lengths ([[...], [...], [...]])."""

@@ -261,6 +261,12 @@ SPFFT_GB300_GRID_C_API(spfft_float_grid_, GridFloat)
       tuning[5] = tu.rpb;                                                                         \
     });                                                                                           \
   }                                                                                               \
+  SpfftError GPREFIX##x_backward_rows(void* transform, int* rows) {                               \
+    return with_handle<spfft::TRANSFORM>(transform, [&](spfft::TRANSFORM& t) {                    \
+      if (!rows) throw spfft::InvalidParameterError();                                            \
+      *rows = spfft::TransformAccess::get(t).gpu_plan().tuning().rpbB;                            \
+    });                                                                                           \
+  }                                                                                               \
   SpfftError GPREFIX##radix_plans(void* transform, int* numStages, int* radices) {                \
     return with_handle<spfft::TRANSFORM>(transform, [&](spfft::TRANSFORM& t) {                    \
       if (!numStages || !radices) throw spfft::InvalidParameterError();                           \

@@ -4,6 +4,7 @@
 #include "planner_gpu.hpp"
 
 #include <algorithm>
+#include <array>
 #include <cstdlib>
 #include <cstring>
 #include <string>
@@ -294,6 +295,14 @@ GpuPlan<T>::GpuPlan(const IndexPlan& p, int device) {
       cpb = std::min(cpb, std::max(1, ncol));
       rpb = std::min(rpb, p.dimY);
       if (splitOk) {
+        // the x backward kernel holds the compact rows besides the FFT rows, so it may want fewer
+        // rows per block (more blocks per SM) than the x forward kernel: its own candidates
+        std::vector<int> rowsB;
+        for (int r : {8, 12, 16, 24, 32}) {
+          a.param = r;
+          fast_dispatch<T>(FastOp::XSmem, p.dimX, r2c, a);
+          if (sm <= optin && r <= p.dimY) rowsB.push_back(r);
+        }
         for (int c : {4, 8, 16, 32}) {
           a.param = c;
           fast_dispatch<T>(FastOp::YSmem, p.dimY, r2c, a);
@@ -301,11 +310,13 @@ GpuPlan<T>::GpuPlan(const IndexPlan& p, int device) {
           for (int r : {8, 16, 32}) {
             a.param = r;
             fast_dispatch<T>(FastOp::XSmem, p.dimX, r2c, a);
-            if (sm <= optin && r <= p.dimY) splitCands_.emplace_back(c, r);
+            if (sm > optin || r > p.dimY) continue;
+            for (int rb : rowsB) splitCands_.push_back({c, r, rb});
           }
         }
-        if (std::find(splitCands_.begin(), splitCands_.end(), std::make_pair(cpb, rpb)) == splitCands_.end()) {
-          splitCands_.emplace_back(cpb, rpb);
+        const std::array<int, 3> dflt{cpb, rpb, rpb};
+        if (std::find(splitCands_.begin(), splitCands_.end(), dflt) == splitCands_.end()) {
+          splitCands_.push_back(dflt);
         }
       }
     }
@@ -331,6 +342,14 @@ GpuPlan<T>::GpuPlan(const IndexPlan& p, int device) {
     fastRows_ = fusedRows;
     splitCpb_ = cpb;
     splitRpb_ = rpb;
+    splitRpbB_ = rpb;
+    // SPFFT_GB300_XB_ROWS=n: rows per x backward block, where n is one of the candidates
+    if (const char* xb = std::getenv("SPFFT_GB300_XB_ROWS")) {
+      const int want = std::atoi(xb);
+      for (const auto& c : splitCands_) {
+        if (c[0] == cpb && c[1] == rpb && c[2] == want) splitRpbB_ = want;
+      }
+    }
   }
 
   radixCands_[0] = radix_plan_candidates(p.dimZ);
@@ -443,7 +462,7 @@ void GpuPlan<T>::backward(const T* values, T* space, void* scratch, cudaStream_t
     fast_dispatch<T>(FastOp::YBackward, base_.dimY, base_.r2c != 0, a);
     check_launch(cudaGetLastError());
     mark(events, 2, stream);
-    a.param = splitRpb_;
+    a.param = splitRpbB_;
     a.out = space;
     fast_dispatch<T>(FastOp::XBackward, base_.dimX, base_.r2c != 0, a);
     check_launch(cudaGetLastError());
@@ -608,7 +627,7 @@ bool GpuPlan<T>::backward_staged(const T* values, T* devSpace, T* hostSpace, voi
     a.param = splitCpb_;
     fast_dispatch<T>(FastOp::YBackward, base_.dimY, base_.r2c != 0, a);
     check_launch(cudaGetLastError());
-    a.param = splitRpb_;
+    a.param = splitRpbB_;
     fast_dispatch<T>(FastOp::XBackward, base_.dimX, base_.r2c != 0, a);
     check_launch(cudaGetLastError());
     check_cuda(cudaEventRecord(events[c], stream));
@@ -634,6 +653,7 @@ typename GpuPlan<T>::Tuning GpuPlan<T>::tuning() const {
   if (t.path == 2) {
     t.cpb = splitCpb_;
     t.rpb = splitRpb_;
+    t.rpbB = splitRpbB_;
   }
   for (int d = 0; d < 3; ++d) t.radix[d] = radixChoice_[d];
   return t;
@@ -651,19 +671,20 @@ std::vector<typename GpuPlan<T>::Tuning> GpuPlan<T>::candidates() const {
       t.path = 1;
       t.fusedRows = f.first;
       t.fusedThreads = f.second;
-      t.cpb = t.rpb = 0;
+      t.cpb = t.rpb = t.rpbB = 0;
       out.push_back(t);
     }
     for (const auto& sp : splitCands_) {
       t.path = 2;
       t.fusedRows = t.fusedThreads = 0;
-      t.cpb = sp.first;
-      t.rpb = sp.second;
+      t.cpb = sp[0];
+      t.rpb = sp[1];
+      t.rpbB = sp[2];
       out.push_back(t);
     }
     if (fusedCands_.empty() && splitCands_.empty()) {
       t.path = 0;
-      t.fusedRows = t.fusedThreads = t.cpb = t.rpb = 0;
+      t.fusedRows = t.fusedThreads = t.cpb = t.rpb = t.rpbB = 0;
       out.push_back(t);
     }
   }
@@ -675,7 +696,7 @@ void GpuPlan<T>::set_tuning(const Tuning& t) {
   bool ok = false;
   for (const Tuning& c : candidates()) {
     ok |= c.spb == t.spb && c.path == t.path && c.fusedRows == t.fusedRows && c.fusedThreads == t.fusedThreads &&
-          c.cpb == t.cpb && c.rpb == t.rpb;
+          c.cpb == t.cpb && c.rpb == t.rpb && c.rpbB == t.rpbB;
   }
   for (int d = 0; d < 3; ++d) ok &= t.radix[d] >= 0 && t.radix[d] < static_cast<int>(radixCands_[d].size());
   if (!ok) throw InvalidParameterError();
@@ -692,6 +713,7 @@ void GpuPlan<T>::set_tuning(const Tuning& t) {
   if (t.path == 2) {
     splitCpb_ = t.cpb;
     splitRpb_ = t.rpb;
+    splitRpbB_ = t.rpbB;
   }
 }
 
@@ -726,7 +748,8 @@ float GpuPlan<T>::autotune(T* values, T* space, void* scratch, cudaStream_t stre
       const Tuning base = best;
       for (Tuning c : candidates()) {
         const bool zOnly = c.path == base.path && c.fusedRows == base.fusedRows &&
-                           c.fusedThreads == base.fusedThreads && c.cpb == base.cpb && c.rpb == base.rpb;
+                           c.fusedThreads == base.fusedThreads && c.cpb == base.cpb && c.rpb == base.rpb &&
+                           c.rpbB == base.rpbB;
         const bool planeOnly = c.spb == base.spb;
         if ((pass == 0 && !zOnly) || (pass == 1 && !planeOnly)) continue;
         for (int d = 0; d < 3; ++d) c.radix[d] = base.radix[d];

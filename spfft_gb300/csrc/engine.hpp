@@ -6,6 +6,7 @@
 
 #include <cuda_runtime.h>
 
+#include <array>
 #include <memory>
 #include <utility>
 #include <vector>
@@ -72,7 +73,8 @@ public:
     int path = 0;          // 0 generic, 1 fused plane, 2 split y and x
     int fusedRows = 0;     // fused: half of the x chunk buffer rows
     int fusedThreads = 0;  // fused: threads per block (256: two blocks per SM, 512: one)
-    int cpb = 0, rpb = 0;  // split: columns per y block, rows per x block
+    int cpb = 0, rpb = 0;  // split: columns per y block, rows per x forward block
+    int rpbB = 0;          // split: rows per x backward block
     int radix[3] = {0, 0, 0};  // generic kernels: radix plan of z, y, x (index into radix_plans())
   };
   // Radix plans available to the generic kernels for the z, y and x lengths (dim 0, 1, 2), and
@@ -113,8 +115,8 @@ private:
   // valid shapes, for the autotuner
   std::vector<int> zCands_;
   std::vector<std::pair<int, int>> fusedCands_;  // (rows, threads)
-  std::vector<std::pair<int, int>> splitCands_;  // (cpb, rpb)
-  int fastSpb_ = 0, fastRows_ = 0, splitCpb_ = 0, splitRpb_ = 0, fusedThreads_ = 512;
+  std::vector<std::array<int, 3>> splitCands_;  // (cpb, rpb, rpbB)
+  int fastSpb_ = 0, fastRows_ = 0, splitCpb_ = 0, splitRpb_ = 0, splitRpbB_ = 0, fusedThreads_ = 512;
   int stagedChunks_ = 8;
   std::vector<RadixPlan> radixCands_[3];
   int radixChoice_[3] = {0, 0, 0};

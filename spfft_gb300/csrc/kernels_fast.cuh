@@ -411,6 +411,7 @@ __device__ __forceinline__ void z_backward_body(const PlanView<S>& p, const S* _
   __syncthreads();
   CS* sticks = reinterpret_cast<CS*>(p.sticks) + s0;
   const bool raw = TT::kScaled && p.sticksRaw;
+  const bool park = TT::kScaled && !raw && exact_block(k);
   for (int i = threadIdx.x; i < nsb * Az; i += blockDim.x) {
     const int k1 = dns.div(i), sl = i - k1 * nsb;
     CA v[Bz];
@@ -419,13 +420,22 @@ __device__ __forceinline__ void z_backward_body(const PlanView<S>& p, const S* _
       CA* rs = reinterpret_cast<CA*>(sticks);
 #pragma unroll
       for (int k2 = 0; k2 < Bz; ++k2) rs[static_cast<size_t>(k1 + Az * k2) * p.numSticks + sl] = v[k2];
-    } else {
-      with_store(k, [&](auto conv) {
+    } else if (park) {
+      // blocks of tiny values: results back into this item's own pass-2 slots, stored exactly below
 #pragma unroll
-        for (int k2 = 0; k2 < Bz; ++k2) {
-          sticks[static_cast<size_t>(k1 + Az * k2) * p.numSticks + sl] = conv(v[k2], k);
-        }
-      });
+      for (int k2 = 0; k2 < Bz; ++k2) buf[sl * PZ + k1 * Bz + k2] = v[k2];
+    } else {
+#pragma unroll
+      for (int k2 = 0; k2 < Bz; ++k2) {
+        sticks[static_cast<size_t>(k1 + Az * k2) * p.numSticks + sl] = to_storage(v[k2], k);
+      }
+    }
+  }
+  if (park) {
+    __syncthreads();
+    for (int i = threadIdx.x; i < nsb * NZ; i += blockDim.x) {
+      const int sl = i / NZ, e = i - sl * NZ, k1 = e / Bz, k2 = e - k1 * Bz;
+      sticks[static_cast<size_t>(k1 + Az * k2) * p.numSticks + sl] = to_storage_exact(buf[sl * PZ + e], k);
     }
   }
   if (raw && threadIdx.x < nsb) p.stickExp[s0 + threadIdx.x] = produced_exp(sExp, k);
@@ -734,16 +744,30 @@ __device__ __forceinline__ void plane_backward_body(const PlanView<S>& p, S* __r
       for (int k1 = 0; k1 < Ax; ++k1) wrow[k1 * (Bx + L::PAD) + b] = v[k1];  // L::wpos(k1 * Bx + b)
     }
     rg.sync();
+    const bool park = TT::kScaled && exact_block(k);
     for (int i = rg.t; i < nr * Ax; i += rg.threads) {
       const int rl = i / Ax, k1 = i - rl * Ax;
       CA v[Bx];
-      fft_pass2<L::LX, +1>(W + rl * L::WP + k1 * L::PAD, 1, k1, v);
+      CA* w2 = W + rl * L::WP + k1 * L::PAD;
+      fft_pass2<L::LX, +1>(w2, 1, k1, v);
       // C2C: complex x row; C2R: pairs (x[2m], x[2m+1]) of the real row
       CS* out = reinterpret_cast<CS*>(space + (static_cast<size_t>(z) * NY + r0 + rl) * NX * (R2C ? 1 : 2));
-      with_store(k, [&](auto conv) {
+      if (park) {
+        // blocks of tiny values: results back into this item's own pass-2 slots, stored exactly below
 #pragma unroll
-        for (int k2 = 0; k2 < Bx; ++k2) out[k1 + Ax * k2] = conv(v[k2], k);
-      });
+        for (int k2 = 0; k2 < Bx; ++k2) w2[k1 * Bx + k2] = v[k2];
+      } else {
+#pragma unroll
+        for (int k2 = 0; k2 < Bx; ++k2) out[k1 + Ax * k2] = to_storage(v[k2], k);
+      }
+    }
+    if (park) {
+      rg.sync();
+      for (int i = rg.t; i < nr * L::LX; i += rg.threads) {
+        const int rl = i / L::LX, e = i - rl * L::LX, k1 = e / Bx, k2 = e - k1 * Bx;
+        CS* out = reinterpret_cast<CS*>(space + (static_cast<size_t>(z) * NY + r0 + rl) * NX * (R2C ? 1 : 2));
+        out[k1 + Ax * k2] = to_storage_exact(W[rl * L::WP + L::wpos(e)], k);
+      }
     }
     rg.sync();
   }
@@ -1098,6 +1122,7 @@ __device__ __forceinline__ void y_backward_body(const PlanView<S>& p, int cpb, i
   __syncthreads();
   CS* planes = reinterpret_cast<CS*>(p.planes) + static_cast<size_t>(z) * NY * nc + c0;
   const bool raw = TT::kScaled && p.planesRaw;
+  const bool park = TT::kScaled && !raw && exact_block(k);
   for (int i = threadIdx.x; i < ncb * Ay; i += blockDim.x) {
     const int k1 = dncb.div(i), c = i - k1 * ncb;
     CA v[By];
@@ -1106,11 +1131,20 @@ __device__ __forceinline__ void y_backward_body(const PlanView<S>& p, int cpb, i
       CA* rp = reinterpret_cast<CA*>(planes);
 #pragma unroll
       for (int k2 = 0; k2 < By; ++k2) rp[static_cast<size_t>(k1 + Ay * k2) * nc + c] = v[k2];
-    } else {
-      with_store(k, [&](auto conv) {
+    } else if (park) {
+      // blocks of tiny values: results back into this item's own pass-2 slots, stored exactly below
 #pragma unroll
-        for (int k2 = 0; k2 < By; ++k2) planes[static_cast<size_t>(k1 + Ay * k2) * nc + c] = conv(v[k2], k);
-      });
+      for (int k2 = 0; k2 < By; ++k2) buf[(k1 * By + k2) * ncb + c] = v[k2];
+    } else {
+#pragma unroll
+      for (int k2 = 0; k2 < By; ++k2) planes[static_cast<size_t>(k1 + Ay * k2) * nc + c] = to_storage(v[k2], k);
+    }
+  }
+  if (park) {
+    __syncthreads();
+    for (int i = threadIdx.x; i < NY * ncb; i += blockDim.x) {
+      const int e = i / ncb, c = i - e * ncb, k1 = e / By, k2 = e - k1 * By;
+      planes[static_cast<size_t>(k1 + Ay * k2) * nc + c] = to_storage_exact(buf[e * ncb + c], k);
     }
   }
   if (raw && threadIdx.x < ncb) p.planeExp[z * nc + c0 + threadIdx.x] = produced_exp(sExp, k);
@@ -1339,15 +1373,29 @@ __device__ __forceinline__ void x_backward_body(const PlanView<S>& p, S* __restr
     for (int k1 = 0; k1 < Ax; ++k1) wrow[k1 * (Bx + L::PAD) + b] = v[k1];  // L::wpos(k1 * Bx + b)
   }
   __syncthreads();
+  const bool park = TT::kScaled && exact_block(k);
   for (int i = threadIdx.x; i < nr * Ax; i += blockDim.x) {
     const int rl = i / Ax, k1 = i - rl * Ax;
     CA v[Bx];
     fft_pass2<L::LX, +1>(s.W + rl * L::WP + k1 * L::PAD, 1, k1, v);
     CS* out = reinterpret_cast<CS*>(space + (static_cast<size_t>(z) * ny + y0 + rl) * NX * (R2C ? 1 : 2));
-    with_store(k, [&](auto conv) {
+    if (park) {
+      // blocks of tiny values: results back into this item's own pass-2 slots, stored exactly below
+      CA* w2 = s.W + rl * L::WP + k1 * L::PAD;
 #pragma unroll
-      for (int k2 = 0; k2 < Bx; ++k2) out[k1 + Ax * k2] = conv(v[k2], k);
-    });
+      for (int k2 = 0; k2 < Bx; ++k2) w2[k1 * Bx + k2] = v[k2];
+    } else {
+#pragma unroll
+      for (int k2 = 0; k2 < Bx; ++k2) out[k1 + Ax * k2] = to_storage(v[k2], k);
+    }
+  }
+  if (park) {
+    __syncthreads();
+    for (int i = threadIdx.x; i < nr * L::LX; i += blockDim.x) {
+      const int rl = i / L::LX, e = i - rl * L::LX, k1 = e / Bx, k2 = e - k1 * Bx;
+      CS* out = reinterpret_cast<CS*>(space + (static_cast<size_t>(z) * ny + y0 + rl) * NX * (R2C ? 1 : 2));
+      out[k1 + Ax * k2] = to_storage_exact(s.W[rl * L::WP + L::wpos(e)], k);
+    }
   }
 }
 
