@@ -71,12 +71,116 @@ __host__ __device__ __forceinline__ bool operator!=(dd a, int z) {
   return a.hi != static_cast<float>(z) || a.lo != 0.0f;
 }
 
+// Complex double-float, stored as the pair of high parts (real, imaginary) and the pair of low
+// parts: each pair is one float2, so an operation applied to the real and the imaginary part at
+// once runs as one packed FP32x2 instruction (FADD2 / FMUL2 / FFMA2, sm_100 and later) instead of
+// two. The 16 bytes hold re.hi, im.hi, re.lo, im.lo.
 struct ddc {
-  dd x, y;
+  float2 hi, lo;
 };
 static_assert(sizeof(ddc) == 16, "ddc must match double2");
 
-__host__ __device__ __forceinline__ ddc make_c(dd x, dd y) { return ddc{x, y}; }
+__host__ __device__ __forceinline__ ddc make_c(dd x, dd y) {
+  return ddc{make_float2(x.hi, y.hi), make_float2(x.lo, y.lo)};
+}
+__host__ __device__ __forceinline__ dd re(ddc c) { return dd(c.hi.x, c.lo.x); }
+__host__ __device__ __forceinline__ dd im(ddc c) { return dd(c.hi.y, c.lo.y); }
+
+// Packed FP32x2 arithmetic (one instruction for both lanes on sm_100 and later; each lane rounds
+// like the scalar instruction). a - b is b * -1 + a: the product is exact, one rounding.
+#if defined(__CUDA_ARCH__) && (__CUDA_ARCH__ >= 1000)
+#define SPFFT_GB300_DD_PACKED 1
+#endif
+__host__ __device__ __forceinline__ float2 f2_add(float2 a, float2 b) {
+#ifdef SPFFT_GB300_DD_PACKED
+  return __fadd2_rn(a, b);
+#else
+  return make_float2(a.x + b.x, a.y + b.y);
+#endif
+}
+__host__ __device__ __forceinline__ float2 f2_sub(float2 a, float2 b) {
+#ifdef SPFFT_GB300_DD_PACKED
+  return __ffma2_rn(b, make_float2(-1.0f, -1.0f), a);
+#else
+  return make_float2(a.x - b.x, a.y - b.y);
+#endif
+}
+__host__ __device__ __forceinline__ float2 f2_mul(float2 a, float2 b) {
+#ifdef SPFFT_GB300_DD_PACKED
+  return __fmul2_rn(a, b);
+#else
+  return make_float2(a.x * b.x, a.y * b.y);
+#endif
+}
+__host__ __device__ __forceinline__ float2 f2_fma(float2 a, float2 b, float2 c) {
+#ifdef SPFFT_GB300_DD_PACKED
+  return __ffma2_rn(a, b, c);
+#else
+  return make_float2(fmaf(a.x, b.x, c.x), fmaf(a.y, b.y, c.y));
+#endif
+}
+
+// Complex double-float operations on both parts at once: the same operation sequence per part as
+// the scalar dd operators above (so the same results), in packed instructions.
+// a + b: two_sum of the high pairs, low pairs added into the error.
+__host__ __device__ __forceinline__ ddc cadd(ddc a, ddc b) {
+  const float2 s = f2_add(a.hi, b.hi);
+  const float2 bb = f2_sub(s, a.hi);
+  const float2 e = f2_add(f2_sub(a.hi, f2_sub(s, bb)), f2_sub(b.hi, bb));
+  return ddc{s, f2_add(e, f2_add(a.lo, b.lo))};
+}
+// a - b = a + (-b): two_sum(a, -b) with (-b) - bb = -(b + bb).
+__host__ __device__ __forceinline__ ddc csub(ddc a, ddc b) {
+  const float2 s = f2_sub(a.hi, b.hi);
+  const float2 bb = f2_sub(s, a.hi);
+  const float2 e = f2_sub(f2_sub(a.hi, f2_sub(s, bb)), f2_add(b.hi, bb));
+  return ddc{s, f2_add(e, f2_sub(a.lo, b.lo))};
+}
+// a * s for a real double-float s: two_prod of the high parts, cross terms into the error.
+__host__ __device__ __forceinline__ ddc cscale(ddc a, dd s) {
+  const float2 sh = make_float2(s.hi, s.hi), sl = make_float2(s.lo, s.lo);
+  const float2 p = f2_mul(a.hi, sh);
+  float2 e = f2_fma(a.hi, sh, make_float2(-p.x, -p.y));
+  e = f2_fma(a.hi, sl, e);
+  e = f2_fma(a.lo, sh, e);
+  return ddc{p, e};
+}
+// a * s + b for a real s
+__host__ __device__ __forceinline__ ddc cfma_r(ddc a, dd s, ddc b) { return cadd(cscale(a, s), b); }
+// a / 2 (exact in both parts)
+__host__ __device__ __forceinline__ ddc chalf(ddc a) {
+  const float2 h = make_float2(0.5f, 0.5f);
+  return ddc{f2_mul(a.hi, h), f2_mul(a.lo, h)};
+}
+// a - b / 2 (halving is exact in both parts)
+__host__ __device__ __forceinline__ ddc csub_half(ddc a, ddc b) {
+  return csub(a, chalf(b));
+}
+__host__ __device__ __forceinline__ ddc cconj(ddc a) {
+  return ddc{make_float2(a.hi.x, -a.hi.y), make_float2(a.lo.x, -a.lo.y)};
+}
+// Multiply by sign * i.
+template <int SIGN>
+__host__ __device__ __forceinline__ ddc cmul_i(ddc a) {
+  return SIGN > 0 ? ddc{make_float2(-a.hi.y, a.hi.x), make_float2(-a.lo.y, a.lo.x)}
+                  : ddc{make_float2(a.hi.y, -a.hi.x), make_float2(a.lo.y, -a.lo.x)};
+}
+// General complex products (run-time twiddles): part by part in scalar dd arithmetic.
+__host__ __device__ __forceinline__ ddc cmul(ddc a, ddc b) {
+  return make_c(re(a) * re(b) - im(a) * im(b), re(a) * im(b) + im(a) * re(b));
+}
+// a * conj(b)
+__host__ __device__ __forceinline__ ddc cmulc(ddc a, ddc b) {
+  return make_c(re(a) * re(b) + im(a) * im(b), im(a) * re(b) - re(a) * im(b));
+}
+// a * (c + i s) for real constants c, s: a c + (i a) s.
+__host__ __device__ __forceinline__ ddc cmul_cs(ddc a, dd c, dd s) { return cfma_r(cmul_i<1>(a), s, cscale(a, c)); }
+__host__ __device__ __forceinline__ ddc cneg(ddc a) {
+  return ddc{make_float2(-a.hi.x, -a.hi.y), make_float2(-a.lo.x, -a.lo.y)};
+}
+__host__ __device__ __forceinline__ bool cnonzero(ddc a) {
+  return a.hi.x != 0.0f || a.lo.x != 0.0f || a.hi.y != 0.0f || a.lo.y != 0.0f;
+}
 
 // double <-> dd conversion by FP64 instructions (host side and constants).
 __host__ __device__ __forceinline__ dd to_dd(double v) {

@@ -27,15 +27,15 @@ struct TwConst<dd> {
 // Multiply by exp(SIGN * 2 pi i * m / R) with m, R compile-time constants after unrolling.
 template <int R, int SIGN, typename C>
 __host__ __device__ __forceinline__ C twiddle_const(C a, int m) {
-  using T = decltype(a.x);
+  using T = decltype(re(a));
   m %= R;
   if (m == 0) return a;
-  if (2 * m == R) return make_c(-a.x, -a.y);
+  if (2 * m == R) return cneg(a);
   if (4 * m == R) return cmul_i<SIGN>(a);
   if (4 * m == 3 * R) return cmul_i<-SIGN>(a);
   const T c = TwConst<T>::cos(R, m);
   const T s = SIGN > 0 ? TwConst<T>::sin(R, m) : -TwConst<T>::sin(R, m);
-  return make_c(a.x * c - a.y * s, a.x * s + a.y * c);
+  return cmul_cs(a, c, s);
 }
 
 template <int R>

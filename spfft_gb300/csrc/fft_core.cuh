@@ -31,6 +31,14 @@ struct Complex<float> {
 };
 
 __host__ __device__ __forceinline__ double2 make_c(double x, double y) { return make_double2(x, y); }
+// Real and imaginary parts (double-float complex values define their own).
+__host__ __device__ __forceinline__ float re(float2 c) { return c.x; }
+__host__ __device__ __forceinline__ float im(float2 c) { return c.y; }
+__host__ __device__ __forceinline__ double re(double2 c) { return c.x; }
+__host__ __device__ __forceinline__ double im(double2 c) { return c.y; }
+// Multiplication by 1/2 (double-float overloads it with an exact two-part scaling).
+__host__ __device__ __forceinline__ float half_of(float a) { return 0.5f * a; }
+__host__ __device__ __forceinline__ double half_of(double a) { return 0.5 * a; }
 __host__ __device__ __forceinline__ float2 make_c(float x, float y) { return make_float2(x, y); }
 
 template <typename C>
@@ -54,6 +62,80 @@ template <typename C, typename T>
 __host__ __device__ __forceinline__ C cscale(C a, T s) {
   return make_c(a.x * s, a.y * s);
 }
+// a * (c + i s) for real c, s
+template <typename C, typename T>
+__host__ __device__ __forceinline__ C cmul_cs(C a, T c, T s) {
+  return make_c(a.x * c - a.y * s, a.x * s + a.y * c);
+}
+template <typename C>
+__host__ __device__ __forceinline__ C cneg(C a) {
+  return make_c(-a.x, -a.y);
+}
+// a * s + b for a real s
+template <typename C, typename T>
+__host__ __device__ __forceinline__ C cfma_r(C a, T s, C b) {
+  return make_c(a.x * s + b.x, a.y * s + b.y);
+}
+// a / 2
+template <typename C>
+__host__ __device__ __forceinline__ C chalf(C a) {
+  return make_c(half_of(a.x), half_of(a.y));
+}
+// a - b / 2
+template <typename C>
+__host__ __device__ __forceinline__ C csub_half(C a, C b) {
+  return make_c(a.x - half_of(b.x), a.y - half_of(b.y));
+}
+
+// FP32 complex values on sm_100 and later: the real and imaginary parts go through one packed
+// FP32x2 instruction (FADD2 / FMUL2 / FFMA2) instead of two, which halves the issue slots of the
+// butterflies' additions and real scalings. Each lane rounds exactly like the scalar instruction
+// (a - b as b * -1 + a, a - b/2 as b * -0.5 + a: the products are exact, one rounding each).
+#if defined(__CUDA_ARCH__) && (__CUDA_ARCH__ >= 1000)
+#define SPFFT_GB300_PACKED_F32X2 1
+#endif
+__host__ __device__ __forceinline__ float2 cadd(float2 a, float2 b) {
+#ifdef SPFFT_GB300_PACKED_F32X2
+  return __fadd2_rn(a, b);
+#else
+  return make_float2(a.x + b.x, a.y + b.y);
+#endif
+}
+__host__ __device__ __forceinline__ float2 csub(float2 a, float2 b) {
+#ifdef SPFFT_GB300_PACKED_F32X2
+  return __ffma2_rn(b, make_float2(-1.0f, -1.0f), a);
+#else
+  return make_float2(a.x - b.x, a.y - b.y);
+#endif
+}
+__host__ __device__ __forceinline__ float2 cscale(float2 a, float s) {
+#ifdef SPFFT_GB300_PACKED_F32X2
+  return __fmul2_rn(a, make_float2(s, s));
+#else
+  return make_float2(a.x * s, a.y * s);
+#endif
+}
+__host__ __device__ __forceinline__ float2 cfma_r(float2 a, float s, float2 b) {
+#ifdef SPFFT_GB300_PACKED_F32X2
+  return __ffma2_rn(a, make_float2(s, s), b);
+#else
+  return make_float2(a.x * s + b.x, a.y * s + b.y);
+#endif
+}
+__host__ __device__ __forceinline__ float2 chalf(float2 a) {
+#ifdef SPFFT_GB300_PACKED_F32X2
+  return __fmul2_rn(a, make_float2(0.5f, 0.5f));
+#else
+  return make_float2(0.5f * a.x, 0.5f * a.y);
+#endif
+}
+__host__ __device__ __forceinline__ float2 csub_half(float2 a, float2 b) {
+#ifdef SPFFT_GB300_PACKED_F32X2
+  return __ffma2_rn(b, make_float2(-0.5f, -0.5f), a);
+#else
+  return make_float2(a.x - 0.5f * b.x, a.y - 0.5f * b.y);
+#endif
+}
 template <typename C>
 __host__ __device__ __forceinline__ C cconj(C a) {
   return make_c(a.x, -a.y);
@@ -68,9 +150,6 @@ template <int SIGN, typename C>
 __host__ __device__ __forceinline__ C ctw(C a, C tw) {
   return SIGN < 0 ? cmul(a, tw) : cmulc(a, tw);
 }
-// Multiplication by 1/2 (double-float overloads it with an exact two-part scaling).
-__host__ __device__ __forceinline__ float half_of(float a) { return 0.5f * a; }
-__host__ __device__ __forceinline__ double half_of(double a) { return 0.5 * a; }
 template <typename C>
 __host__ __device__ __forceinline__ bool cnonzero(C a) {
   return a.x != 0 || a.y != 0;
@@ -87,11 +166,11 @@ __host__ __device__ __forceinline__ void dft2(C* v) {
 
 template <int SIGN, typename C>
 __host__ __device__ __forceinline__ void dft3(C* v) {
-  using T = decltype(v[0].x);
+  using T = decltype(re(v[0]));
   constexpr T h = T(0.8660254037844386467637232);  // sin(2 pi / 3)
   C t1 = cadd(v[1], v[2]);
   C t2 = csub(v[1], v[2]);
-  C m = make_c(v[0].x - half_of(t1.x), v[0].y - half_of(t1.y));
+  C m = csub_half(v[0], t1);
   C n = cmul_i<SIGN>(cscale(t2, h));
   v[0] = cadd(v[0], t1);
   v[1] = cadd(m, n);
@@ -112,17 +191,17 @@ __host__ __device__ __forceinline__ void dft4(C* v) {
 
 template <int SIGN, typename C>
 __host__ __device__ __forceinline__ void dft5(C* v) {
-  using T = decltype(v[0].x);
+  using T = decltype(re(v[0]));
   constexpr T c1 = T(0.3090169943749474241022934), c2 = T(-0.8090169943749474241022934);
   constexpr T s1 = T(0.9510565162951535721164393), s2 = T(0.5877852522924731291687060);
   C a = cadd(v[1], v[4]), b = cadd(v[2], v[3]);
   C c = csub(v[1], v[4]), d = csub(v[2], v[3]);
   C x0 = v[0];
   v[0] = cadd(x0, cadd(a, b));
-  C m1 = make_c(x0.x + c1 * a.x + c2 * b.x, x0.y + c1 * a.y + c2 * b.y);
-  C m2 = make_c(x0.x + c2 * a.x + c1 * b.x, x0.y + c2 * a.y + c1 * b.y);
-  C n1 = cmul_i<SIGN>(make_c(s1 * c.x + s2 * d.x, s1 * c.y + s2 * d.y));
-  C n2 = cmul_i<SIGN>(make_c(s2 * c.x - s1 * d.x, s2 * c.y - s1 * d.y));
+  C m1 = cfma_r(b, c2, cfma_r(a, c1, x0));
+  C m2 = cfma_r(b, c1, cfma_r(a, c2, x0));
+  C n1 = cmul_i<SIGN>(cfma_r(d, s2, cscale(c, s1)));
+  C n2 = cmul_i<SIGN>(cfma_r(d, -s1, cscale(c, s2)));
   v[1] = cadd(m1, n1);
   v[4] = csub(m1, n1);
   v[2] = cadd(m2, n2);
@@ -131,7 +210,7 @@ __host__ __device__ __forceinline__ void dft5(C* v) {
 
 template <int SIGN, typename C>
 __host__ __device__ __forceinline__ void dft7(C* v) {
-  using T = decltype(v[0].x);
+  using T = decltype(re(v[0]));
   constexpr T C1 = T(0.6234898018587335305250049), C2 = T(-0.2225209339563144042889026),
               C3 = T(-0.9009688679024191262361023);
   constexpr T S1 = T(0.7818314824680298087084445), S2 = T(0.9749279121818236070181317),
@@ -141,25 +220,25 @@ __host__ __device__ __forceinline__ void dft7(C* v) {
   C x0 = v[0];
   v[0] = cadd(x0, cadd(a1, cadd(a2, a3)));
   // q = 1: cos (C1, C2, C3), sin (S1, S2, S3)
-  C m = make_c(x0.x + C1 * a1.x + C2 * a2.x + C3 * a3.x, x0.y + C1 * a1.y + C2 * a2.y + C3 * a3.y);
-  C n = cmul_i<SIGN>(make_c(S1 * d1.x + S2 * d2.x + S3 * d3.x, S1 * d1.y + S2 * d2.y + S3 * d3.y));
+  C m = cfma_r(a3, C3, cfma_r(a2, C2, cfma_r(a1, C1, x0)));
+  C n = cmul_i<SIGN>(cfma_r(d3, S3, cfma_r(d2, S2, cscale(d1, S1))));
   v[1] = cadd(m, n);
   v[6] = csub(m, n);
   // q = 2: cos (C2, C3, C1), sin (S2, -S3, -S1)
-  m = make_c(x0.x + C2 * a1.x + C3 * a2.x + C1 * a3.x, x0.y + C2 * a1.y + C3 * a2.y + C1 * a3.y);
-  n = cmul_i<SIGN>(make_c(S2 * d1.x - S3 * d2.x - S1 * d3.x, S2 * d1.y - S3 * d2.y - S1 * d3.y));
+  m = cfma_r(a3, C1, cfma_r(a2, C3, cfma_r(a1, C2, x0)));
+  n = cmul_i<SIGN>(cfma_r(d3, -S1, cfma_r(d2, -S3, cscale(d1, S2))));
   v[2] = cadd(m, n);
   v[5] = csub(m, n);
   // q = 3: cos (C3, C1, C2), sin (S3, -S1, S2)
-  m = make_c(x0.x + C3 * a1.x + C1 * a2.x + C2 * a3.x, x0.y + C3 * a1.y + C1 * a2.y + C2 * a3.y);
-  n = cmul_i<SIGN>(make_c(S3 * d1.x - S1 * d2.x + S2 * d3.x, S3 * d1.y - S1 * d2.y + S2 * d3.y));
+  m = cfma_r(a3, C2, cfma_r(a2, C1, cfma_r(a1, C3, x0)));
+  n = cmul_i<SIGN>(cfma_r(d3, S2, cfma_r(d2, -S1, cscale(d1, S3))));
   v[3] = cadd(m, n);
   v[4] = csub(m, n);
 }
 
 template <int SIGN, typename C>
 __host__ __device__ __forceinline__ void dft8(C* v) {
-  using T = decltype(v[0].x);
+  using T = decltype(re(v[0]));
   constexpr T r = T(0.7071067811865475244008444);
   C b[4], c[4];
 #pragma unroll
@@ -168,9 +247,9 @@ __host__ __device__ __forceinline__ void dft8(C* v) {
     c[i] = csub(v[i], v[i + 4]);
   }
   // c_r *= exp(sign * 2 pi i r / 8)
-  c[1] = make_c(r * (c[1].x - SIGN * c[1].y), r * (c[1].y + SIGN * c[1].x));
+  c[1] = cscale(cadd(c[1], cmul_i<SIGN>(c[1])), r);
   c[2] = cmul_i<SIGN>(c[2]);
-  c[3] = make_c(r * (-c[3].x - SIGN * c[3].y), r * (-c[3].y + SIGN * c[3].x));
+  c[3] = cscale(csub(cmul_i<SIGN>(c[3]), c[3]), r);
   dft4<SIGN>(b);
   dft4<SIGN>(c);
 #pragma unroll

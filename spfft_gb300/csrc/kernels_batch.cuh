@@ -22,7 +22,7 @@ __device__ __forceinline__ int find_transform(const int* __restrict__ starts, in
 }
 
 template <typename S, typename A, int NZ>
-__global__ void __launch_bounds__(kThreads) z_backward_batch(const BatchView<S> bv, int spb) {
+__global__ void __launch_bounds__(kThreads, ZBackwardMinBlocks<A>::value) z_backward_batch(const BatchView<S> bv, int spb) {
   __shared__ int sExp[2];
   const int t = find_transform(bv.starts, bv.count, blockIdx.x);
   z_backward_body<S, A, NZ>(bv.views[t], bv.in[t], spb, blockIdx.x - bv.starts[t], sExp);

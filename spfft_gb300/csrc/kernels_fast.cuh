@@ -54,10 +54,19 @@ template <>
 struct YMinBlocks<dd> {
   static constexpr int value = 3;
 };
-// The double-float z forward kernel keeps three 256-thread blocks per SM (at most 80 registers).
+// Minimum resident 256-thread blocks per SM asked of the compiler for the z kernels: double-float
+// z backward two (at most 128 registers), z forward three (at most 80).
+template <typename A>
+struct ZBackwardMinBlocks {
+  static constexpr int value = 4;  // FP32: at most 64 registers (the kernel needs about 50)
+};
+template <>
+struct ZBackwardMinBlocks<dd> {
+  static constexpr int value = 2;
+};
 template <typename A>
 struct ZForwardMinBlocks {
-  static constexpr int value = 1;
+  static constexpr int value = 3;  // FP32: at most 80 registers (the kernel needs about 60)
 };
 template <>
 struct ZForwardMinBlocks<dd> {
@@ -103,7 +112,7 @@ __device__ __forceinline__ ddc to_arith(double2 v, int k) {
 // arithmetic -> storage, undoing the block scale
 __device__ __forceinline__ float2 to_storage(float2 v, int) { return v; }
 __device__ __forceinline__ double2 to_storage(ddc v, int k) {
-  return make_double2(dd_to_double(v.x, -k), dd_to_double(v.y, -k));
+  return make_double2(dd_to_double(re(v), -k), dd_to_double(im(v), -k));
 }
 // The same conversions for every binary64 class: subnormal inputs normalised, results below
 // 2^-1022 assembled as subnormals.
@@ -113,7 +122,7 @@ __device__ __forceinline__ ddc to_arith_exact(double2 v, int k) {
 }
 __device__ __forceinline__ float2 to_storage_exact(float2 v, int) { return v; }
 __device__ __forceinline__ double2 to_storage_exact(ddc v, int k) {
-  return make_double2(dd_to_double_exact(v.x, -k), dd_to_double_exact(v.y, -k));
+  return make_double2(dd_to_double_exact(re(v), -k), dd_to_double_exact(im(v), -k));
 }
 // Which conversions a block needs. A block scaled by k brings its largest magnitude into [1, 2),
 // and its largest FFT output is at least that large (Parseval), so binary64 subnormals -- inputs or
@@ -212,7 +221,7 @@ __device__ __forceinline__ int produced_exp(int maxKey, int k) { return maxKey =
 __device__ __forceinline__ float2 scale_pow2(float2 v, int) { return v; }
 __device__ __forceinline__ ddc scale_pow2(ddc v, int d) {
   const float f = d < -126 ? 0.0f : __uint_as_float(static_cast<unsigned>(d + 127) << 23);
-  return make_c(dd(v.x.hi * f, v.x.lo * f), dd(v.y.hi * f, v.y.lo * f));
+  return ddc{f2_mul(v.hi, make_float2(f, f)), f2_mul(v.lo, make_float2(f, f))};
 }
 
 // Programmatic dependent launch (sm_90+): kernels of the same transform are launched so that the
@@ -442,7 +451,7 @@ __device__ __forceinline__ void z_backward_body(const PlanView<S>& p, const S* _
 }
 
 template <typename S, typename A, int NZ>
-__global__ void __launch_bounds__(kThreads) z_backward(const PlanView<S> p,
+__global__ void __launch_bounds__(kThreads, ZBackwardMinBlocks<A>::value) z_backward(const PlanView<S> p,
                                                        const S* __restrict__ values, int spb) {
   __shared__ int sExp[2];
   z_backward_body<S, A, NZ>(p, values, spb, blockIdx.x, sExp);
@@ -634,7 +643,7 @@ __device__ __forceinline__ void plane_load_tables(const PlanView<S>& p,
 template <typename L, typename CA, typename RowFn>
 __device__ __forceinline__ void c2r_pack_rows(RowFn row, int nr, CA* W, const int* colOf, const CA* twx,
                                               int tid, int nthreads) {
-  using A = decltype(CA{}.x);
+  using A = decltype(re(CA{}));
   constexpr int M = L::M, H = M / 2;
   for (int i = tid; i < nr * (H + 1); i += nthreads) {
     const int rl = i / (H + 1), j = i - rl * (H + 1);
@@ -644,13 +653,16 @@ __device__ __forceinline__ void c2r_pack_rows(RowFn row, int nr, CA* W, const in
     const CA xk = ck >= 0 ? prow[ck] : make_c(A(0), A(0));
     const CA xm = cm >= 0 ? prow[cm] : make_c(A(0), A(0));
     if (j == 0) {
-      wrow[L::wpos(0)] = make_c(xk.x + xm.x, xk.x - xm.x);
+      wrow[L::wpos(0)] = make_c(re(xk) + re(xm), re(xk) - re(xm));
     } else {
-      const CA sum = make_c(xk.x + xm.x, xk.y - xm.y);
-      const CA dif = make_c(xk.x - xm.x, xk.y + xm.y);
+      // sum = xk + conj xm, dif = xk - conj xm
+      const CA xmc = cconj(xm);
+      const CA sum = cadd(xk, xmc);
+      const CA dif = csub(xk, xmc);
       const CA u = cmulc(dif, twx[j]);
-      wrow[L::wpos(j)] = make_c(sum.x - u.y, sum.y + u.x);
-      if (2 * j != M) wrow[L::wpos(M - j)] = make_c(sum.x + u.y, u.x - sum.y);  // M - j = j only for even M
+      const CA iu = cmul_i<1>(u);
+      wrow[L::wpos(j)] = cadd(sum, iu);  // (sum.x - u.y, sum.y + u.x)
+      if (2 * j != M) wrow[L::wpos(M - j)] = cconj(csub(sum, iu));  // (sum.x + u.y, u.x - sum.y); M - j = j only for even M
     }
   }
 }
@@ -911,9 +923,10 @@ __device__ __forceinline__ void plane_forward_body(const PlanView<S>& p, const S
         const CA* wrow = wbase + rl * L::WP;
         const CA zk = wrow[ci.x];
         const CA zm = wrow[ci.y];
-        const CA dif = make_c(zk.x - zm.x, zk.y + zm.y);
+        const CA zmc = cconj(zm);
+        const CA dif = csub(zk, zmc);  // (zk.x - zm.x, zk.y + zm.y)
         const CA u = cmul(dif, s.twx[ci.z]);
-        s.P[(r0 + rl) * nc + c] = make_c(half_of(zk.x + zm.x + u.y), half_of(zk.y - zm.y - u.x));
+        s.P[(r0 + rl) * nc + c] = chalf(csub(cadd(zk, zmc), cmul_i<1>(u)));
       }
       rg.sync();
     }
@@ -1508,9 +1521,10 @@ __device__ __forceinline__ void x_forward_body(const PlanView<S>& p, const S* __
         const CA* wrow = s.W + rl * L::WP;
         const CA zk = wrow[ci.x];
         const CA zm = wrow[ci.y];
-        const CA dif = make_c(zk.x - zm.x, zk.y + zm.y);
+        const CA zmc = cconj(zm);
+        const CA dif = csub(zk, zmc);  // (zk.x - zm.x, zk.y + zm.y)
         const CA u = cmul(dif, s.twx[ci.z]);
-        const CA xv = make_c(half_of(zk.x + zm.x + u.y), half_of(zk.y - zm.y - u.x));
+        const CA xv = chalf(csub(cadd(zk, zmc), cmul_i<1>(u)));
         if (raw) rawPlanes[i] = xv;
         else planes[i] = conv(xv, k);
       }

@@ -115,8 +115,8 @@ static bool check_two_pass_dd() {
   auto y = direct(x, SIGN);
   long double num = 0, den = 0;
   for (int i = 0; i < N; ++i) {
-    const long double er = (long double)to_double(out[i].x) - y[i].real();
-    const long double ei = (long double)to_double(out[i].y) - y[i].imag();
+    const long double er = (long double)to_double(re(out[i])) - y[i].real();
+    const long double ei = (long double)to_double(im(out[i])) - y[i].imag();
     num += er * er + ei * ei;
     den += std::norm(y[i]);
   }
