@@ -759,9 +759,29 @@ def measure_grad(args) -> dict:
     end.record()
     torch.cuda.synchronize()
     ms = start.elapsed_time(end) / steps
+    # the library's share of a step: the backward transform and the adjoint gradient kernels alone
+    # (the loss's own gradient V * psi stands in as the adjoint's input)
+    psi = torch.empty((n, n, n), dtype=torch.complex128, device="cuda")
+    g_c = torch.empty(len(idx), dtype=torch.complex128, device="cuda")
+    cs = c.detach()
+    s = torch.cuda.current_stream().cuda_stream
+    tr.backward_device(cs, psi, s)
+    g_psi = (weight * 2.0).to(torch.complex128) * psi
+    for _ in range(3):
+        tr.backward_device(cs, psi, s)
+        tr.adjoint_backward(g_psi, g_c, s)
+    start.record()
+    for _ in range(steps):
+        tr.backward_device(cs, psi, s)
+        tr.adjoint_backward(g_psi, g_c, s)
+    end.record()
+    torch.cuda.synchronize()
+    ms_lib = start.elapsed_time(end) / steps
     return {"workload": "c2c_96_sphere24 (57,777 values), L = sum V |backward(c)|^2, FP64",
             "grad_steps_per_s": round(1e3 / ms, 1), "ms_per_step": round(ms, 4),
-            "step": "backward transform + loss + adjoint gradient (torch elementwise ops for the loss)"}
+            "transform_and_adjoint_ms": round(ms_lib, 4),
+            "step": "backward transform + loss + adjoint gradient (torch elementwise ops for the loss); "
+                    "transform_and_adjoint_ms: the library's two kernel sequences of a step alone"}
 
 
 def measure_batched(args, workload: str, batch: int, dtype: str, radii=None) -> dict:

@@ -326,6 +326,28 @@ def test_plane_strategies_agree(lib, plane, dtype, monkeypatch):
         assert rel_l2(f.cpu().numpy(), oracle.forward(out.cpu().numpy().astype(np.complex128 if ttype == 0 else np.float64))) <= TOL[dtype]
 
 
+@pytest.mark.parametrize("rows", ["8", "12", "24"])
+@pytest.mark.parametrize("dtype", ["float64", "float32"])
+def test_x_backward_rows_per_block(lib, rows, dtype, monkeypatch):
+    """Split plane passes with the x backward kernel on its own row count (SPFFT_GB300_XB_ROWS, the
+    autotuner's extra dimension): same results as the oracle, including a last block with fewer rows
+    (96 rows over 24- and 12-row blocks, 100 over 8 / 12 / 24)."""
+    monkeypatch.setenv("SPFFT_GB300_PLANE", "split")
+    monkeypatch.setenv("SPFFT_GB300_XB_ROWS", rows)
+    rng = np.random.default_rng(23)
+    for n, radius, ttype in [(96, 24, 1), (100, 25, 0)]:
+        idx = sphere_indices(n, radius, r2c=(ttype == 1))
+        tr = _transform(dtype, ttype, (n, n, n), idx)
+        assert tr.path_info()["split_plane"]
+        assert tr.tuning()["rows_per_x_backward_block"] == int(rows), tr.tuning()
+        vals = _values(rng, len(idx))
+        want = pipeline.HostPipeline(ttype, n, n, n, idx).backward(vals)
+        st = CT[dtype] if ttype == 0 else RT[dtype]
+        out = torch.empty((n, n, n), dtype=st, device="cuda")
+        tr.backward(torch.from_numpy(vals).to(CT[dtype]).cuda(), out)
+        assert rel_l2(out.cpu().numpy(), want) <= TOL[dtype], (n, ttype, rows)
+
+
 @pytest.mark.parametrize("access", ["direct", "copy"])
 @pytest.mark.parametrize("dtype", ["float64", "float32"])
 def test_pinned_host_buffers(lib, access, dtype, monkeypatch):
