@@ -134,6 +134,7 @@ def _declare(lib: ctypes.CDLL) -> None:
         getattr(lib, prefix + "transform_autotune").argtypes = [_vp, _i, ctypes.POINTER(ctypes.c_float)]
         getattr(lib, prefix + "transform_tuning").argtypes = [_vp, _ip]
         getattr(lib, prefix + "transform_x_backward_rows").argtypes = [_vp, _ip]
+        getattr(lib, prefix + "transform_splits").argtypes = [_vp, _ip]
         getattr(lib, prefix + "transform_radix_plans").argtypes = [_vp, _ip, _ip]
         getattr(lib, prefix + "transform_adjoint_backward").argtypes = [_vp, _vp, _vp, _vp]
         getattr(lib, prefix + "transform_adjoint_forward").argtypes = [_vp, _vp, _vp, _i, _vp]
@@ -436,8 +437,23 @@ class Transform:
                 "fused_half_rows": v[2], "fused_threads": v[3], "columns_per_y_block": v[4],
                 "rows_per_x_block": v[5], "rows_per_x_backward_block": xb.value}
 
+    def splits(self) -> dict:
+        """Two-pass split (A, B) of each size-specialised pass (None for a generic-kernel pass)."""
+        v = (ctypes.c_int * 6)()
+        _call("spfft_gb300_" + self._p[len("spfft_"):] + "transform_splits", self._h, v)
+        dims = {"z": self.dim_z(), "y": self.dim_y(), "x": self.dim_x()}
+        out = {}
+        for i, name in enumerate(["z_backward", "z_forward", "y_backward", "y_forward", "x_backward",
+                                  "x_forward"]):
+            n = dims[name[0]]
+            if name[0] == "x" and self._type == SPFFT_TRANS_R2C:
+                n //= 2
+            out[name] = (v[i], n // v[i]) if v[i] > 0 else None
+        return out
+
     def radix_plans(self) -> list:
-        """Radix stages of the generic kernels for the z, y and x lengths ([[...], [...], [...]])."""
+        """Radix stages of the z, y and x lengths ([[...], [...], [...]]): the generic kernels'
+        plan, or the two radices of a size-specialised backward pass's split."""
         stages = (ctypes.c_int * 3)()
         radices = (ctypes.c_int * (3 * 24))()
         _call("spfft_gb300_" + self._p[len("spfft_"):] + "transform_radix_plans", self._h, stages, radices)

@@ -179,6 +179,18 @@ template <>
 struct Shape<192, 1> {
   static constexpr int A = 12, B = 16;
 };
+// Variant 2 swaps the two factors of variant 1 (B x A instead of A x B): the z and split-y kernels
+// are built in both orders for every length where the swap differs, and the autotuner chooses one
+// per pass.
+template <int N>
+struct Shape<N, 2> {
+  static constexpr int A = Shape<N, 1>::B > 1 ? Shape<N, 1>::B : Shape<N, 1>::A;
+  static constexpr int B = Shape<N, 1>::B > 1 ? Shape<N, 1>::A : 1;
+};
+template <int N>
+constexpr bool has_swapped_split() {
+  return Shape<N, 2>::A != Shape<N, 1>::A;
+}
 
 // Position of X[k] after pass 2 stored back in place.
 template <int N, int V = 0>

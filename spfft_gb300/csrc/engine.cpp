@@ -5,6 +5,7 @@
 
 #include <algorithm>
 #include <array>
+#include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <string>
@@ -350,6 +351,28 @@ GpuPlan<T>::GpuPlan(const IndexPlan& p, int device) {
         if (c[0] == cpb && c[1] == rpb && c[2] == want) splitRpbB_ = want;
       }
     }
+    // Passes that can run the swapped two-pass split of their length (FastOp::SplitRadix): the
+    // specialised z pass and the split y passes. SPFFT_GB300_SPLITS=zb,zf,yb,yf (each 0 or 1)
+    // chooses it per pass at creation (z backward, z forward, y backward, y forward).
+    {
+      size_t rad = 0;
+      a.smemOut = &rad;
+      a.split = 1;
+      a.param = 0;
+      zSwap_ = fastZ_ && fast_dispatch<T>(FastOp::SplitRadix, nz, false, a) && rad > 0;
+      a.param = 1;
+      ySwap_ = splitOk && fast_dispatch<T>(FastOp::SplitRadix, p.dimY, r2c, a) && rad > 0;
+      a.split = 0;
+      if (const char* sw = std::getenv("SPFFT_GB300_SPLITS")) {
+        int v[4] = {0, 0, 0, 0};
+        if (std::sscanf(sw, "%d,%d,%d,%d", &v[0], &v[1], &v[2], &v[3]) == 4) {
+          for (int i = 0; i < 4; ++i) {
+            const bool ok = i < 2 ? zSwap_ : (ySwap_ && planePath_ == PlanePath::Split);
+            splitChoice_[i] = (v[i] == 1 && ok) ? 1 : 0;
+          }
+        }
+      }
+    }
   }
 
   radixCands_[0] = radix_plan_candidates(p.dimZ);
@@ -444,6 +467,7 @@ void GpuPlan<T>::backward(const T* values, T* space, void* scratch, cudaStream_t
   if (fastZ_) {
     a.param = fastSpb_;
     a.in = values;
+    a.split = splitChoice_[0];
     fast_dispatch<T>(FastOp::ZBackward, base_.dimZ, base_.r2c != 0, a);
   } else {
     check_launch(launch_generic<T>(GenericPass::ZBackward, v, config_, values, nullptr, T(0), stream));
@@ -459,6 +483,7 @@ void GpuPlan<T>::backward(const T* values, T* space, void* scratch, cudaStream_t
     mark(events, 2, stream);
   } else if (planePath_ == PlanePath::Split && aligned) {
     a.param = splitCpb_;
+    a.split = splitChoice_[2];
     fast_dispatch<T>(FastOp::YBackward, base_.dimY, base_.r2c != 0, a);
     check_launch(cudaGetLastError());
     mark(events, 2, stream);
@@ -528,6 +553,7 @@ void GpuPlan<T>::forward(const T* space, T* values, bool scaled, void* scratch,
     check_launch(cudaGetLastError());
     mark(events, 1, stream);
     a.param = splitCpb_;
+    a.split = splitChoice_[3];
     fast_dispatch<T>(FastOp::YForward, base_.dimY, base_.r2c != 0, a);
     check_launch(cudaGetLastError());
   } else {
@@ -541,6 +567,7 @@ void GpuPlan<T>::forward(const T* space, T* values, bool scaled, void* scratch,
     a.param = fastSpb_;
     a.out = values;
     a.scale = scale;
+    a.split = splitChoice_[1];
     fast_dispatch<T>(FastOp::ZForward, base_.dimZ, base_.r2c != 0, a);
     check_launch(cudaGetLastError());
   } else {
@@ -580,6 +607,7 @@ bool GpuPlan<T>::forward_staged(const T* hostSpace, T* devSpace, T* values, bool
     fast_dispatch<T>(FastOp::XForward, base_.dimX, base_.r2c != 0, a);
     check_launch(cudaGetLastError());
     a.param = splitCpb_;
+    a.split = splitChoice_[3];
     fast_dispatch<T>(FastOp::YForward, base_.dimY, base_.r2c != 0, a);
     check_launch(cudaGetLastError());
   }
@@ -590,6 +618,7 @@ bool GpuPlan<T>::forward_staged(const T* hostSpace, T* devSpace, T* values, bool
     a.param = fastSpb_;
     a.out = values;
     a.scale = scale;
+    a.split = splitChoice_[1];
     fast_dispatch<T>(FastOp::ZForward, base_.dimZ, base_.r2c != 0, a);
     check_launch(cudaGetLastError());
   } else {
@@ -611,6 +640,7 @@ bool GpuPlan<T>::backward_staged(const T* values, T* devSpace, T* hostSpace, voi
   if (fastZ_) {
     a.param = fastSpb_;
     a.in = values;
+    a.split = splitChoice_[0];
     fast_dispatch<T>(FastOp::ZBackward, base_.dimZ, base_.r2c != 0, a);
   } else {
     check_launch(launch_generic<T>(GenericPass::ZBackward, v, config_, values, nullptr, T(0), stream));
@@ -625,6 +655,7 @@ bool GpuPlan<T>::backward_staged(const T* values, T* devSpace, T* hostSpace, voi
     a.zBegin = z0;
     a.zCount = cnt;
     a.param = splitCpb_;
+    a.split = splitChoice_[2];
     fast_dispatch<T>(FastOp::YBackward, base_.dimY, base_.r2c != 0, a);
     check_launch(cudaGetLastError());
     a.param = splitRpbB_;
@@ -656,7 +687,37 @@ typename GpuPlan<T>::Tuning GpuPlan<T>::tuning() const {
     t.rpbB = splitRpbB_;
   }
   for (int d = 0; d < 3; ++d) t.radix[d] = radixChoice_[d];
+  for (int i = 0; i < 2; ++i) t.split[i] = fastZ_ ? splitChoice_[i] : 0;
+  for (int i = 2; i < 4; ++i) t.split[i] = t.path == 2 ? splitChoice_[i] : 0;
   return t;
+}
+
+template <typename T>
+void GpuPlan<T>::split_radices(int* radices) const {
+  for (int i = 0; i < 6; ++i) radices[i] = 0;
+  FastArgs<T> a;
+  size_t rad = 0;
+  a.smemOut = &rad;
+  const bool r2c = base_.r2c != 0;
+  auto query = [&](int which, int split, int n) {
+    a.param = which;
+    a.split = split;
+    rad = 0;
+    return fast_dispatch<T>(FastOp::SplitRadix, n, r2c, a) ? static_cast<int>(rad) : 0;
+  };
+  if (fastZ_) {
+    radices[0] = query(0, splitChoice_[0], base_.dimZ);
+    radices[1] = query(0, splitChoice_[1], base_.dimZ);
+  }
+  if (planePath_ == PlanePath::Split) {
+    radices[2] = query(1, splitChoice_[2], base_.dimY);
+    radices[3] = query(1, splitChoice_[3], base_.dimY);
+    radices[4] = radices[5] = query(4, 0, base_.dimX);
+  } else if (planePath_ == PlanePath::Fused) {
+    radices[2] = query(2, 0, base_.dimY);
+    radices[3] = query(3, 0, base_.dimY);
+    radices[4] = radices[5] = query(4, 0, base_.dimX);
+  }
 }
 
 template <typename T>
@@ -699,7 +760,12 @@ void GpuPlan<T>::set_tuning(const Tuning& t) {
           c.cpb == t.cpb && c.rpb == t.rpb && c.rpbB == t.rpbB;
   }
   for (int d = 0; d < 3; ++d) ok &= t.radix[d] >= 0 && t.radix[d] < static_cast<int>(radixCands_[d].size());
+  for (int i = 0; i < 4; ++i) {
+    const bool swappable = i < 2 ? (zSwap_ && t.spb > 0) : (ySwap_ && t.path == 2);
+    ok &= t.split[i] == 0 || (t.split[i] == 1 && swappable);
+  }
   if (!ok) throw InvalidParameterError();
+  for (int i = 0; i < 4; ++i) splitChoice_[i] = t.split[i];
   for (int d = 0; d < 3; ++d) radixChoice_[d] = t.radix[d];
   base_.fz = radixCands_[0][t.radix[0]];
   base_.fy = radixCands_[1][t.radix[1]];
@@ -753,11 +819,24 @@ float GpuPlan<T>::autotune(T* values, T* space, void* scratch, cudaStream_t stre
         const bool planeOnly = c.spb == base.spb;
         if ((pass == 0 && !zOnly) || (pass == 1 && !planeOnly)) continue;
         for (int d = 0; d < 3; ++d) c.radix[d] = base.radix[d];
+        for (int i = 0; i < 4; ++i) c.split[i] = (i < 2 ? c.spb > 0 : c.path == 2) ? base.split[i] : 0;
         const float ms = time_pair(c);
         if (ms < bestMs) {
           bestMs = ms;
           best = c;
         }
+      }
+    }
+    // the two-pass split of each specialised z and split-y pass: the default or the swapped order
+    for (int i = 0; i < 4; ++i) {
+      const bool swappable = i < 2 ? (zSwap_ && best.spb > 0) : (ySwap_ && best.path == 2);
+      if (!swappable) continue;
+      Tuning c = best;
+      c.split[i] = 1 - c.split[i];
+      const float ms = time_pair(c);
+      if (ms < bestMs) {
+        bestMs = ms;
+        best = c;
       }
     }
     // radix plans of the lengths the generic kernels transform: z without specialised z kernels,

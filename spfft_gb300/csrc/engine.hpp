@@ -76,7 +76,13 @@ public:
     int cpb = 0, rpb = 0;  // split: columns per y block, rows per x forward block
     int rpbB = 0;          // split: rows per x backward block
     int radix[3] = {0, 0, 0};  // generic kernels: radix plan of z, y, x (index into radix_plans())
+    // size-specialised z backward, z forward, split y backward, split y forward passes: 1 runs
+    // the swapped two-pass split of the length (B x A instead of A x B), where it has one
+    int split[4] = {0, 0, 0, 0};
   };
+  // First-pass radix A of the two-pass split (length = A * B) each pass runs with: z backward,
+  // z forward, y backward, y forward, x backward, x forward; 0 for a pass on the generic kernels.
+  void split_radices(int* radices) const;
   // Radix plans available to the generic kernels for the z, y and x lengths (dim 0, 1, 2), and
   // the ones in use.
   const std::vector<RadixPlan>& radix_plans(int dim) const { return radixCands_[dim]; }
@@ -89,7 +95,8 @@ public:
   // Autotuner: times `reps` backward + scaled forward pairs per candidate on `values` / `space`
   // (device buffers of this plan's sizes, overwritten) on `stream`, first over the z shapes with
   // the current plane strategy, then over the plane strategies and tile shapes with the best z
-  // shape, then -- for the lengths that run on the generic kernels -- over their radix plans one
+  // shape, then over the two-pass split (default or swapped) of each specialised z and split-y
+  // pass, then -- for the lengths that run on the generic kernels -- over their radix plans one
   // length at a time, and keeps the fastest. Returns its time per pair in milliseconds. No other
   // work of this plan may run meanwhile.
   float autotune(T* values, T* space, void* scratch, cudaStream_t stream, int reps);
@@ -120,6 +127,8 @@ private:
   int stagedChunks_ = 8;
   std::vector<RadixPlan> radixCands_[3];
   int radixChoice_[3] = {0, 0, 0};
+  int splitChoice_[4] = {0, 0, 0, 0};  // Tuning::split
+  bool zSwap_ = false, ySwap_ = false;  // the z / split y length has a swapped split
   ScratchLayout layout_{};
   T scale_ = T(1);
   int numValues_ = 0;

@@ -365,13 +365,14 @@ struct ZLayout {
 
 // Kernel bodies take their block coordinates as arguments, so the single-transform kernels and the
 // batched kernels (kernels_batch.cuh) share them.
-template <typename S, typename A, int NZ>
+// V selects the two-pass split of the z length (Shape<NZ, V>: 1 the default, 2 the swapped one).
+template <typename S, typename A, int NZ, int V = 1>
 __device__ __forceinline__ void z_backward_body(const PlanView<S>& p, const S* __restrict__ values,
                                                 int spb, int bx, int* sExpPtr) {
   using TT = Types<S, A>;
   using CS = typename TT::CS;
   using CA = typename TT::CA;
-  constexpr int Az = Shape<NZ, 1>::A, Bz = Shape<NZ, 1>::B, PZ = ZLayout<NZ>::pitch;
+  constexpr int Az = Shape<NZ, V>::A, Bz = Shape<NZ, V>::B, PZ = ZLayout<NZ>::pitch;
   int& sExp = *sExpPtr;
   CA* tw = reinterpret_cast<CA*>(g_fast_smem);
   CA* buf = tw + NZ;
@@ -415,7 +416,7 @@ __device__ __forceinline__ void z_backward_body(const PlanView<S>& p, const S* _
 
   for (int i = threadIdx.x; i < nsb * Bz; i += blockDim.x) {
     const int sl = i / Bz, b = i - sl * Bz;
-    fft_pass1<NZ, +1, 1>(buf + sl * PZ, 1, b, tw);
+    fft_pass1<NZ, +1, V>(buf + sl * PZ, 1, b, tw);
   }
   __syncthreads();
   CS* sticks = reinterpret_cast<CS*>(p.sticks) + s0;
@@ -424,7 +425,7 @@ __device__ __forceinline__ void z_backward_body(const PlanView<S>& p, const S* _
   for (int i = threadIdx.x; i < nsb * Az; i += blockDim.x) {
     const int k1 = dns.div(i), sl = i - k1 * nsb;
     CA v[Bz];
-    fft_pass2<NZ, +1, 1>(buf + sl * PZ, 1, k1, v);
+    fft_pass2<NZ, +1, V>(buf + sl * PZ, 1, k1, v);
     if (raw) {
       CA* rs = reinterpret_cast<CA*>(sticks);
 #pragma unroll
@@ -450,20 +451,20 @@ __device__ __forceinline__ void z_backward_body(const PlanView<S>& p, const S* _
   if (raw && threadIdx.x < nsb) p.stickExp[s0 + threadIdx.x] = produced_exp(sExp, k);
 }
 
-template <typename S, typename A, int NZ>
+template <typename S, typename A, int NZ, int V = 1>
 __global__ void __launch_bounds__(kThreads, ZBackwardMinBlocks<A>::value) z_backward(const PlanView<S> p,
                                                        const S* __restrict__ values, int spb) {
   __shared__ int sExp[2];
-  z_backward_body<S, A, NZ>(p, values, spb, blockIdx.x, sExp);
+  z_backward_body<S, A, NZ, V>(p, values, spb, blockIdx.x, sExp);
 }
 
-template <typename S, typename A, int NZ>
+template <typename S, typename A, int NZ, int V = 1>
 __device__ __forceinline__ void z_forward_body(const PlanView<S>& p, S* __restrict__ values, S scale,
                                                int spb, int bx, int* sExpPtr) {
   using TT = Types<S, A>;
   using CS = typename TT::CS;
   using CA = typename TT::CA;
-  constexpr int Az = Shape<NZ, 1>::A, Bz = Shape<NZ, 1>::B, PZ = ZLayout<NZ>::pitch;
+  constexpr int Az = Shape<NZ, V>::A, Bz = Shape<NZ, V>::B, PZ = ZLayout<NZ>::pitch;
   int& sExp = *sExpPtr;
   CA* tw = reinterpret_cast<CA*>(g_fast_smem);
   CA* buf = tw + NZ;
@@ -513,13 +514,13 @@ __device__ __forceinline__ void z_forward_body(const PlanView<S>& p, S* __restri
   }
   for (int i = threadIdx.x; i < nsb * Bz; i += blockDim.x) {
     const int sl = i / Bz, b = i - sl * Bz;
-    fft_pass1<NZ, -1, 1>(buf + sl * PZ, 1, b, tw);
+    fft_pass1<NZ, -1, V>(buf + sl * PZ, 1, b, tw);
   }
   __syncthreads();
   for (int i = threadIdx.x; i < nsb * Az; i += blockDim.x) {
     const int k1 = dns.div(i), sl = i - k1 * nsb;
     CA v[Bz];
-    fft_pass2<NZ, -1, 1>(buf + sl * PZ, 1, k1, v);
+    fft_pass2<NZ, -1, V>(buf + sl * PZ, 1, k1, v);
 #pragma unroll
     for (int k2 = 0; k2 < Bz; ++k2) buf[sl * PZ + k1 * Bz + k2] = v[k2];
   }
@@ -535,7 +536,7 @@ __device__ __forceinline__ void z_forward_body(const PlanView<S>& p, S* __restri
   for (int e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
     const int pos = p.entryPos[e] - base;
     const int sl = pos / NZ;
-    CS v = stored_value<S, A>(buf + sl * PZ + transposed_pos<NZ, 1>(pos - sl * NZ), k, converted);
+    CS v = stored_value<S, A>(buf + sl * PZ + transposed_pos<NZ, V>(pos - sl * NZ), k, converted);
     // scaling multiplies by S(1 / (Nx Ny Nz)) in S, like compress_kernel_scaled
     // (compression_kernels.cu:106-128)
     if (scale != S(0)) v = cscale(v, scale);
@@ -543,11 +544,11 @@ __device__ __forceinline__ void z_forward_body(const PlanView<S>& p, S* __restri
   }
 }
 
-template <typename S, typename A, int NZ>
+template <typename S, typename A, int NZ, int V = 1>
 __global__ void __launch_bounds__(kThreads, ZForwardMinBlocks<A>::value) z_forward(const PlanView<S> p, S* __restrict__ values,
                                                       S scale, int spb) {
   __shared__ int sExp[2];
-  z_forward_body<S, A, NZ>(p, values, scale, spb, blockIdx.x, sExp);
+  z_forward_body<S, A, NZ, V>(p, values, scale, spb, blockIdx.x, sExp);
 }
 
 // ================================================================================================
@@ -1009,6 +1010,8 @@ inline void launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t s
   (void)cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
 }
 
+// `swapped`: run the swapped two-pass split (Shape<N, 2>) where the length has one
+// (has_swapped_split<N>), else the default (Shape<N, 1>).
 template <typename S, typename A, int NZ>
 struct ZKernels {
   using CA = typename Types<S, A>::CA;
@@ -1016,14 +1019,24 @@ struct ZKernels {
   static cudaError_t prepare(size_t maxSmem) {
     cudaError_t e1 = allow_dynamic_smem(z_backward<S, A, NZ>, maxSmem);
     cudaError_t e2 = allow_dynamic_smem(z_forward<S, A, NZ>, maxSmem);
+    if constexpr (has_swapped_split<NZ>()) {
+      if (e1 == cudaSuccess) e1 = allow_dynamic_smem(z_backward<S, A, NZ, 2>, maxSmem);
+      if (e2 == cudaSuccess) e2 = allow_dynamic_smem(z_forward<S, A, NZ, 2>, maxSmem);
+    }
     return e1 != cudaSuccess ? e1 : e2;
   }
-  static void backward(const PlanView<S>& p, int spb, const S* values, cudaStream_t st) {
+  static void backward(const PlanView<S>& p, int spb, const S* values, cudaStream_t st, bool swapped) {
     const int g = (p.numSticks + spb - 1) / spb;
+    if constexpr (has_swapped_split<NZ>()) {
+      if (swapped) return launch_pdl(z_backward<S, A, NZ, 2>, g, kThreads, smem(spb), st, p, values, spb);
+    }
     launch_pdl(z_backward<S, A, NZ>, g, kThreads, smem(spb), st, p, values, spb);
   }
-  static void forward(const PlanView<S>& p, int spb, S* values, S scale, cudaStream_t st) {
+  static void forward(const PlanView<S>& p, int spb, S* values, S scale, cudaStream_t st, bool swapped) {
     const int g = (p.numSticks + spb - 1) / spb;
+    if constexpr (has_swapped_split<NZ>()) {
+      if (swapped) return launch_pdl(z_forward<S, A, NZ, 2>, g, kThreads, smem(spb), st, p, values, scale, spb);
+    }
     launch_pdl(z_forward<S, A, NZ>, g, kThreads, smem(spb), st, p, values, scale, spb);
   }
 };
@@ -1053,13 +1066,14 @@ struct PlaneKernels {
 // plane [z][y][numColumns] in HBM between them. More traffic than the fused plane kernel but many
 // small blocks instead of one large block per plane, so every SM stays busy.
 // ================================================================================================
-// y backward: block (column group, z)
-template <typename S, typename A, int NY>
+// y backward: block (column group, z); V selects the two-pass split of the y length as in the z
+// pass
+template <typename S, typename A, int NY, int V = 1>
 __device__ __forceinline__ void y_backward_body(const PlanView<S>& p, int cpb, int bx, int z, int* sExpPtr) {
   using TT = Types<S, A>;
   using CS = typename TT::CS;
   using CA = typename TT::CA;
-  constexpr int Ay = Shape<NY, 1>::A, By = Shape<NY, 1>::B;
+  constexpr int Ay = Shape<NY, V>::A, By = Shape<NY, V>::B;
   int& sExp = *sExpPtr;
   CA* tw = reinterpret_cast<CA*>(g_fast_smem);
   CA* buf = tw + NY;
@@ -1130,7 +1144,7 @@ __device__ __forceinline__ void y_backward_body(const PlanView<S>& p, int cpb, i
   if (p.r2c && c0 == 0 && p.columnX[0] == 0) line_fill(buf, NY, ncb);
   for (int i = threadIdx.x; i < ncb * By; i += blockDim.x) {
     const int b = dncb.div(i), c = i - b * ncb;
-    fft_pass1<NY, +1, 1>(buf + c, ncb, b, tw);
+    fft_pass1<NY, +1, V>(buf + c, ncb, b, tw);
   }
   __syncthreads();
   CS* planes = reinterpret_cast<CS*>(p.planes) + static_cast<size_t>(z) * NY * nc + c0;
@@ -1139,7 +1153,7 @@ __device__ __forceinline__ void y_backward_body(const PlanView<S>& p, int cpb, i
   for (int i = threadIdx.x; i < ncb * Ay; i += blockDim.x) {
     const int k1 = dncb.div(i), c = i - k1 * ncb;
     CA v[By];
-    fft_pass2<NY, +1, 1>(buf + c, ncb, k1, v);
+    fft_pass2<NY, +1, V>(buf + c, ncb, k1, v);
     if (raw) {
       CA* rp = reinterpret_cast<CA*>(planes);
 #pragma unroll
@@ -1163,20 +1177,20 @@ __device__ __forceinline__ void y_backward_body(const PlanView<S>& p, int cpb, i
   if (raw && threadIdx.x < ncb) p.planeExp[z * nc + c0 + threadIdx.x] = produced_exp(sExp, k);
 }
 
-template <typename S, typename A, int NY>
+template <typename S, typename A, int NY, int V = 1>
 __global__ void __launch_bounds__(kThreads, YMinBlocks<A>::value) y_backward_split(const PlanView<S> p, int cpb,
                                                                                      int z0) {
   __shared__ int sExp[2];
-  y_backward_body<S, A, NY>(p, cpb, blockIdx.x, z0 + blockIdx.y, sExp);
+  y_backward_body<S, A, NY, V>(p, cpb, blockIdx.x, z0 + blockIdx.y, sExp);
 }
 
 // y forward: block (column group, z)
-template <typename S, typename A, int NY>
+template <typename S, typename A, int NY, int V = 1>
 __device__ __forceinline__ void y_forward_body(const PlanView<S>& p, int cpb, int bx, int z, int* sExpPtr) {
   using TT = Types<S, A>;
   using CS = typename TT::CS;
   using CA = typename TT::CA;
-  constexpr int Ay = Shape<NY, 1>::A, By = Shape<NY, 1>::B;
+  constexpr int Ay = Shape<NY, V>::A, By = Shape<NY, V>::B;
   int& sExp = *sExpPtr;
   CA* tw = reinterpret_cast<CA*>(g_fast_smem);
   CA* buf = tw + NY;
@@ -1221,13 +1235,13 @@ __device__ __forceinline__ void y_forward_body(const PlanView<S>& p, int cpb, in
   }
   for (int i = threadIdx.x; i < ncb * By; i += blockDim.x) {
     const int b = dncb.div(i), c = i - b * ncb;
-    fft_pass1<NY, -1, 1>(buf + c, ncb, b, tw);
+    fft_pass1<NY, -1, V>(buf + c, ncb, b, tw);
   }
   __syncthreads();
   for (int i = threadIdx.x; i < ncb * Ay; i += blockDim.x) {
     const int k1 = dncb.div(i), c = i - k1 * ncb;
     CA v[By];
-    fft_pass2<NY, -1, 1>(buf + c, ncb, k1, v);
+    fft_pass2<NY, -1, V>(buf + c, ncb, k1, v);
 #pragma unroll
     for (int k2 = 0; k2 < By; ++k2) buf[(k1 * By + k2) * ncb + c] = v[k2];
   }
@@ -1251,7 +1265,7 @@ __device__ __forceinline__ void y_forward_body(const PlanView<S>& p, int cpb, in
     for (int u = 0; u < 4; ++u) {
       if (pos[u] >= 0) {
         const int y = dnc.div(pos[u]), c = pos[u] - y * nc;
-        const CA* slot = buf + transposed_pos<NY, 1>(y) * ncb + (c - c0);
+        const CA* slot = buf + transposed_pos<NY, V>(y) * ncb + (c - c0);
         if (raw) reinterpret_cast<CA*>(sticks)[st0 + u * blockDim.x] = *slot;
         else sticks[st0 + u * blockDim.x] = stored_value<S, A>(slot, k, converted);
       }
@@ -1261,11 +1275,11 @@ __device__ __forceinline__ void y_forward_body(const PlanView<S>& p, int cpb, in
   if (raw && threadIdx.x < ncb) p.stickExp[z * nc + c0 + threadIdx.x] = sExp == kZeroExp ? kZeroExp : k;
 }
 
-template <typename S, typename A, int NY>
+template <typename S, typename A, int NY, int V = 1>
 __global__ void __launch_bounds__(kThreads, YMinBlocks<A>::value) y_forward_split(const PlanView<S> p, int cpb,
                                                                                     int z0) {
   __shared__ int sExp[2];
-  y_forward_body<S, A, NY>(p, cpb, blockIdx.x, z0 + blockIdx.y, sExp);
+  y_forward_body<S, A, NY, V>(p, cpb, blockIdx.x, z0 + blockIdx.y, sExp);
 }
 
 // Shared memory of the x kernels: twx[NX] | (R2C) twm[M] | colOf[NXF] | P[rows][numColumns] |
@@ -1558,15 +1572,25 @@ struct YSplitKernels {
   static cudaError_t prepare(size_t maxSmem) {
     cudaError_t e1 = allow_dynamic_smem(y_backward_split<S, A, NY>, maxSmem);
     cudaError_t e2 = allow_dynamic_smem(y_forward_split<S, A, NY>, maxSmem);
+    if constexpr (has_swapped_split<NY>()) {
+      if (e1 == cudaSuccess) e1 = allow_dynamic_smem(y_backward_split<S, A, NY, 2>, maxSmem);
+      if (e2 == cudaSuccess) e2 = allow_dynamic_smem(y_forward_split<S, A, NY, 2>, maxSmem);
+    }
     return e1 != cudaSuccess ? e1 : e2;
   }
-  // planes [z0, z0 + nz) (nz < 0: all planes from z0)
-  static void backward(const PlanView<S>& p, int cpb, cudaStream_t st, int z0, int nz) {
+  // planes [z0, z0 + nz) (nz < 0: all planes from z0); `swapped` as in ZKernels
+  static void backward(const PlanView<S>& p, int cpb, cudaStream_t st, int z0, int nz, bool swapped) {
     const dim3 g((p.numColumns + cpb - 1) / cpb, nz < 0 ? p.dimZ - z0 : nz);
+    if constexpr (has_swapped_split<NY>()) {
+      if (swapped) return launch_pdl(y_backward_split<S, A, NY, 2>, g, kThreads, smem(cpb), st, p, cpb, z0);
+    }
     launch_pdl(y_backward_split<S, A, NY>, g, kThreads, smem(cpb), st, p, cpb, z0);
   }
-  static void forward(const PlanView<S>& p, int cpb, cudaStream_t st, int z0, int nz) {
+  static void forward(const PlanView<S>& p, int cpb, cudaStream_t st, int z0, int nz, bool swapped) {
     const dim3 g((p.numColumns + cpb - 1) / cpb, nz < 0 ? p.dimZ - z0 : nz);
+    if constexpr (has_swapped_split<NY>()) {
+      if (swapped) return launch_pdl(y_forward_split<S, A, NY, 2>, g, kThreads, smem(cpb), st, p, cpb, z0);
+    }
     launch_pdl(y_forward_split<S, A, NY>, g, kThreads, smem(cpb), st, p, cpb, z0);
   }
 };
@@ -1595,6 +1619,28 @@ struct XSplitKernels {
     launch_pdl(x_forward_split<S, A, NX, R2C>, g, kThreads, smem_forward(p.numColumns, rpb), st, p, space, rpb, z0);
   }
 };
+
+// First-pass radix A of the two-pass split (N = A * B) a kernel of length N runs (FastOp::SplitRadix):
+// which = 0 z pass, 1 split y pass (swapped: the swapped split; 0 where the length has none),
+// 2 / 3 y pass of the fused plane backward / forward kernel, 4 x pass (R2C: the half-length
+// complex FFT).
+template <int N>
+int split_radix(int which, bool swapped, bool r2c) {
+  switch (which) {
+    case 0:
+    case 1:
+      if (!swapped) return Shape<N, 1>::A;
+      return has_swapped_split<N>() ? Shape<N, 2>::A : 0;
+    case 2:
+      return Shape<N, 1>::A;
+    case 3:
+      return Shape<N>::A;
+    case 4:
+      return r2c ? Shape<PlaneLayout<N, N, true>::LX>::A : Shape<N>::A;
+    default:
+      return 0;
+  }
+}
 
 // Arithmetic type of the specialised kernels for a storage type: float for FP32, double-float
 // for FP64.

@@ -348,6 +348,51 @@ def test_x_backward_rows_per_block(lib, rows, dtype, monkeypatch):
         assert rel_l2(out.cpu().numpy(), want) <= TOL[dtype], (n, ttype, rows)
 
 
+# Default two-pass split (A, B) of the z and split-y kernels per specialised length; the swapped
+# split is (B, A) where B > 1 and A != B.
+DEFAULT_SPLIT = {48: (8, 6), 60: (10, 6), 64: (8, 8), 72: (9, 8), 90: (10, 9), 96: (12, 8),
+                 100: (10, 10), 108: (12, 9), 120: (12, 10), 128: (16, 8), 144: (12, 12),
+                 150: (15, 10), 160: (16, 10), 180: (15, 12), 192: (12, 16), 240: (16, 15),
+                 256: (16, 16)}
+
+
+@pytest.mark.parametrize("dtype", ["float64", "float32"])
+@pytest.mark.parametrize("choice", ["1,1,1,1", "1,0,0,1", "0,1,1,0"])
+def test_swapped_two_pass_splits(lib, dtype, choice, monkeypatch):
+    """The z and split-y kernels in the swapped order of their two radices (SPFFT_GB300_SPLITS, the
+    autotuner's split dimension), per pass, for every specialised length: same results as the
+    oracle, and splits() / radix_plans() report the split each pass runs."""
+    monkeypatch.setenv("SPFFT_GB300_PLANE", "split")
+    monkeypatch.setenv("SPFFT_GB300_SPLITS", choice)
+    want_swap = [c == "1" for c in choice.split(",")]
+    rng = np.random.default_rng(29)
+    lengths = sorted(DEFAULT_SPLIT) if choice == "1,1,1,1" else [96, 150, 192]
+    for i, n in enumerate(lengths):
+        ttype = i % 2
+        dims = (48, n, n)  # x, y, z: y and z on the length under test
+        idx = random_indices(rng, *dims, r2c=ttype == 1, stick_frac=0.3, fill_frac=0.5)
+        tr = _transform(dtype, ttype, dims, idx)
+        assert tr.path_info()["split_plane"]
+        a, b = DEFAULT_SPLIT[n]
+        swappable = b > 1 and a != b
+        got = tr.splits()
+        for name, sw in zip(["z_backward", "z_forward", "y_backward", "y_forward"], want_swap):
+            assert got[name] == ((b, a) if sw and swappable else (a, b)), (n, name, got)
+        plans = tr.radix_plans()
+        assert plans[0] == list(got["z_backward"]) and plans[1] == list(got["y_backward"]), plans
+        vals = _values(rng, len(idx))
+        oracle = pipeline.HostPipeline(ttype, *dims, idx)
+        st = CT[dtype] if ttype == 0 else RT[dtype]
+        out = torch.empty(dims[::-1], dtype=st, device="cuda")
+        tr.backward(torch.from_numpy(vals).to(CT[dtype]).cuda(), out)
+        space = out.cpu().numpy()
+        assert rel_l2(space, oracle.backward(vals)) <= TOL[dtype], (n, ttype, choice)
+        f = torch.empty(len(idx), dtype=CT[dtype], device="cuda")
+        tr.forward(out, f, sp.SPFFT_FULL_SCALING)
+        want_f = oracle.forward(space.astype(np.complex128 if ttype == 0 else np.float64), scaled=True)
+        assert rel_l2(f.cpu().numpy(), want_f) <= TOL[dtype], (n, ttype, choice)
+
+
 @pytest.mark.parametrize("access", ["direct", "copy"])
 @pytest.mark.parametrize("dtype", ["float64", "float32"])
 def test_pinned_host_buffers(lib, access, dtype, monkeypatch):
