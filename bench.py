@@ -148,6 +148,38 @@ def algorithmic_bytes(n: int, npts: int, nsticks: int, ncols: int, r2c: bool, ts
     return {"kernels": kern, "pair": pair}
 
 
+def algorithmic_flops(n: int, nsticks: int, ncols: int, r2c: bool) -> dict:
+    """Algorithmic flops per launch of each kernel and per pair: 5 n log2 n per complex 1D FFT of
+    length n and 2.5 n log2 n per real one, over the z-sticks, the non-empty y columns of every plane
+    and every x row (the pruned transform, not the dense 3D grid)."""
+    c2c = 5.0 * n * np.log2(n)
+    z = nsticks * c2c
+    y = n * ncols * c2c
+    x = n * n * (c2c / 2 if r2c else c2c)
+    kern = {"z_backward": z, "y_backward": y, "x_backward": x, "x_forward": x, "y_forward": y, "z_forward": z}
+    return {"kernels": kern, "pair": 2 * (z + y + x)}
+
+
+def fp64_peak_tflops() -> float:
+    """FP64 throughput of this GPU, measured here: best of five cuBLAS DGEMMs (torch.matmul, float64,
+    4096^3, 2 n^3 flops each) timed with CUDA events after a warm-up."""
+    import torch
+
+    m = 4096
+    a = torch.randn(m, m, dtype=torch.float64, device="cuda")
+    b = torch.randn(m, m, dtype=torch.float64, device="cuda")
+    torch.matmul(a, b)
+    best = float("inf")
+    for _ in range(5):
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        torch.matmul(a, b)
+        e.record()
+        torch.cuda.synchronize()
+        best = min(best, s.elapsed_time(e))
+    return 2.0 * m ** 3 / (best * 1e-3) / 1e12
+
+
 # ---------------------------------------------------------------------------------------------
 # clocks
 # ---------------------------------------------------------------------------------------------
@@ -462,6 +494,20 @@ def measure_gpu(args, rank: int, world: int) -> dict:
                 "limiter": ("instruction issue: FP64 runs as double-float arithmetic on the FP32 pipes "
                             "(GB300's FP64 pipe is 57x slower), so the HBM fraction is not reachable"
                             if dtype == "float64" else "latency of a single small transform")}
+    if dtype == "float64":
+        # FP64 flop roofline: the pruned transform's algorithmic flops against this GPU's measured
+        # FP64 rate. The double-float kernels run on the FP32 pipes, so the fraction exceeds 1.
+        fl = algorithmic_flops(n, nsticks, ncols, r2c)
+        fp64_peak = fp64_peak_tflops()
+        achieved_tf = fl["pair"] * pairs_per_s / world / 1e12
+        roofline["fp64_flops"] = {
+            "algorithmic_flops_per_pair": int(fl["pair"]),
+            "achieved_tflops": round(achieved_tf, 3),
+            "fp64_peak_tflops": round(fp64_peak, 3),
+            "peak_source": "cuBLAS DGEMM 4096^3 (torch.matmul float64), measured in this run",
+            "frac": round(achieved_tf / fp64_peak, 3),
+            "kernel_tflops": {k: round(fl["kernels"][k] / (v * 1e-3) / 1e12, 3) for k, v in kern_ms.items()},
+        }
     pair_gbs = ab["pair"] * pairs_per_s / world / 1e9
 
     # ---- end to end through the public API with pinned host buffers ----------------------------

@@ -165,16 +165,15 @@ __host__ __device__ __forceinline__ ddc cmul_i(ddc a) {
   return SIGN > 0 ? ddc{make_float2(-a.hi.y, a.hi.x), make_float2(-a.lo.y, a.lo.x)}
                   : ddc{make_float2(a.hi.y, -a.hi.x), make_float2(a.lo.y, -a.lo.x)};
 }
-// General complex products (run-time twiddles): part by part in scalar dd arithmetic.
-__host__ __device__ __forceinline__ ddc cmul(ddc a, ddc b) {
-  return make_c(re(a) * re(b) - im(a) * im(b), re(a) * im(b) + im(a) * re(b));
-}
-// a * conj(b)
-__host__ __device__ __forceinline__ ddc cmulc(ddc a, ddc b) {
-  return make_c(re(a) * re(b) + im(a) * im(b), im(a) * re(b) - re(a) * im(b));
-}
-// a * (c + i s) for real constants c, s: a c + (i a) s.
+// a * (c + i s) for real c, s: a c + (i a) s.
 __host__ __device__ __forceinline__ ddc cmul_cs(ddc a, dd c, dd s) { return cfma_r(cmul_i<1>(a), s, cscale(a, c)); }
+// General complex products (run-time twiddles) in the same packed form: a b = a re(b) + (i a) im(b).
+// Every part is the same two-product and two-sum as in the scalar form
+// re(a) re(b) - im(a) im(b), re(a) im(b) + im(a) re(b) (two_sum is exact in either operand order,
+// negation is exact), so the results equal it (up to the sign of a zero) with fewer instructions.
+__host__ __device__ __forceinline__ ddc cmul(ddc a, ddc b) { return cmul_cs(a, re(b), im(b)); }
+// a * conj(b)
+__host__ __device__ __forceinline__ ddc cmulc(ddc a, ddc b) { return cmul_cs(a, re(b), -im(b)); }
 __host__ __device__ __forceinline__ ddc cneg(ddc a) {
   return ddc{make_float2(-a.hi.x, -a.hi.y), make_float2(-a.lo.x, -a.lo.y)};
 }

@@ -382,21 +382,31 @@ __device__ __forceinline__ void z_backward_body(const PlanView<S>& p, const S* _
 
   load_twiddles<S, A>(tw, p.twz, NZ);
   for (int i = threadIdx.x; i < nsb * PZ; i += blockDim.x) buf[i] = czero<A>();
+  // The value map is a plan table (constant from plan creation on): the block's entry range and
+  // this thread's first four entries are read before the wait for the previous kernel.
+  const int e0 = p.stickEntryStart[s0], e1 = p.stickEntryStart[s0 + nsb];
+  const int base = s0 * NZ;
+  int pos0[4], usr0[4];
+#pragma unroll
+  for (int u = 0; u < 4; ++u) {
+    const int eu = e0 + threadIdx.x + u * blockDim.x;
+    pos0[u] = eu < e1 ? p.entryPos[eu] - base : -1;
+    usr0[u] = eu < e1 ? p.entryUser[eu] : 0;
+  }
   __syncthreads();
   pdl_wait();
   pdl_trigger();
 
   const CS* vals = reinterpret_cast<const CS*>(values);
-  const int e0 = p.stickEntryStart[s0], e1 = p.stickEntryStart[s0 + nsb];
-  const int base = s0 * NZ;
   // Index loads four at a time, then asynchronous value copies straight to their stick slots.
   for (int e = e0 + threadIdx.x; e < e1; e += 4 * blockDim.x) {
     int pos[4], usr[4];
+    const bool first = e == e0 + threadIdx.x;
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
       const int eu = e + u * blockDim.x;
-      pos[u] = eu < e1 ? p.entryPos[eu] - base : -1;
-      usr[u] = eu < e1 ? p.entryUser[eu] : 0;
+      pos[u] = first ? pos0[u] : (eu < e1 ? p.entryPos[eu] - base : -1);
+      usr[u] = first ? usr0[u] : (eu < e1 ? p.entryUser[eu] : 0);
     }
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
@@ -1084,24 +1094,49 @@ __device__ __forceinline__ void y_backward_body(const PlanView<S>& p, int cpb, i
   const FastDiv dncb(ncb), dnc(nc);
   load_twiddles<S, A>(tw, p.twy, NY);
   for (int i = threadIdx.x; i < NY * ncb; i += blockDim.x) buf[i] = czero<A>();
+  // Plan tables (constant from plan creation on) are read before the wait for the previous kernel:
+  // the stick range of the column group and this thread's first four stick slots.
+  const int sBegin = p.columnStickStart[c0], sEnd = p.columnStickStart[c0 + ncb];
+  int pos0[4];
+#pragma unroll
+  for (int u = 0; u < 4; ++u) {
+    const int st = sBegin + threadIdx.x + u * blockDim.x;
+    pos0[u] = st < sEnd ? __ldg(p.stickPlanePos + st) : -1;
+  }
+  if (TT::kScaled && p.sticksRaw && threadIdx.x == 0) sExp = kZeroExp;
   __syncthreads();
   pdl_wait();
   pdl_trigger();
   const CS* sticks = reinterpret_cast<const CS*>(p.sticks) + static_cast<size_t>(z) * p.numSticks;
-  const int sBegin = p.columnStickStart[c0], sEnd = p.columnStickStart[c0 + ncb];
   int k = 0;
   if (TT::kScaled && p.sticksRaw) {
     // double-float sticks from the z pass: block scale = smallest stick exponent; each value is
-    // brought to it as it is gathered
-    if (threadIdx.x == 0) sExp = kZeroExp;
-    __syncthreads();
+    // brought to it as it is stored. The first four sticks of every thread (all of them when the
+    // group has at most 4 * blockDim.x sticks) stay in registers from the load to the store, so
+    // the exponents and the values arrive in one round trip.
+    const CA* rs = reinterpret_cast<const CA*>(sticks);
+    int ex0[4];
+    CA val0[4];
     int e = kZeroExp;
-    for (int st = sBegin + threadIdx.x; st < sEnd; st += blockDim.x) e = min(e, p.stickExp[st]);
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int st = sBegin + threadIdx.x + u * blockDim.x;
+      ex0[u] = pos0[u] >= 0 ? p.stickExp[st] : kZeroExp;
+      if (pos0[u] >= 0) val0[u] = rs[st];
+      e = min(e, ex0[u]);
+    }
+    for (int st = sBegin + threadIdx.x + 4 * blockDim.x; st < sEnd; st += blockDim.x) e = min(e, p.stickExp[st]);
     atomicMin(&sExp, e);
     __syncthreads();
     k = sExp == kZeroExp ? 0 : sExp;
-    const CA* rs = reinterpret_cast<const CA*>(sticks);
-    for (int st0 = sBegin + threadIdx.x; st0 < sEnd; st0 += 4 * blockDim.x) {
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      if (pos0[u] >= 0) {
+        const int y = dnc.div(pos0[u]), c = pos0[u] - y * nc;
+        buf[y * ncb + (c - c0)] = scale_pow2(val0[u], k - ex0[u]);
+      }
+    }
+    for (int st0 = sBegin + threadIdx.x + 4 * blockDim.x; st0 < sEnd; st0 += 4 * blockDim.x) {
       int pos[4], ex[4];
       CA val[4];
 #pragma unroll
@@ -1126,7 +1161,7 @@ __device__ __forceinline__ void y_backward_body(const PlanView<S>& p, int cpb, i
 #pragma unroll
       for (int u = 0; u < 4; ++u) {
         const int st = st0 + u * blockDim.x;
-        pos[u] = st < sEnd ? __ldg(p.stickPlanePos + st) : -1;
+        pos[u] = st0 == sBegin + threadIdx.x ? pos0[u] : (st < sEnd ? __ldg(p.stickPlanePos + st) : -1);
       }
 #pragma unroll
       for (int u = 0; u < 4; ++u) {
