@@ -421,7 +421,7 @@ def measure_gpu(args, rank: int, world: int) -> dict:
     if not args.no_autotune:  # plan-time autotuner (outside every timed region)
         tr.autotune(3)
         tuned = tr.tuning()
-        tuned["two_pass_splits"] = {k: None if v is None else f"{v[0]}x{v[1]}" for k, v in tr.splits().items()}
+        tuned["splits"] = {k: None if v is None else "x".join(map(str, v)) for k, v in tr.splits().items()}
     tr.set_stream(stream)
     tr.set_execution_mode(sp.SPFFT_EXEC_ASYNCHRONOUS)
 

@@ -131,8 +131,8 @@ SPFFT_EXPORT SpfftError spfft_gb300_float_transform_path_info(SpfftFloatTransfor
 /* Autotuner (no counterpart in the reference). Times `repetitions` backward + scaled forward pairs
  * of every valid tile shape and plane strategy of the transform (first the sticks per z block with
  * the current plane strategy, then the fused plane pass with each chunk size and thread count and
- * the split passes with each column / row group size, then the two-pass split of each specialised
- * z and split-y pass, spfft_gb300_transform_splits, then the radix plans of the lengths that run
+ * the split passes with each column / row group size, then the split of each specialised z and
+ * split-y pass, spfft_gb300_transform_split_stages, then the radix plans of the lengths that run
  * on the generic kernels, spfft_gb300_transform_radix_plans) on the transform's own device buffers,
  * and keeps the fastest; writes its time per pair in milliseconds to msPerPair (may be NULL).
  * Synchronous; overwrites the grid's internal device space-domain buffer; no other call on the
@@ -158,18 +158,26 @@ SPFFT_EXPORT SpfftError spfft_gb300_float_transform_x_backward_rows(SpfftFloatTr
  * radices[d * 24 + 0 .. numStages[d] - 1] (d = 0 z, 1 y, 2 x; 24 slots per length). For a length
  * on the generic (runtime-radix) kernels, the autotuner chooses among several plans (the default
  * grouping of powers of two into radix 8, the reverse order, radix-4 and radix-2 stages). For a
- * length on the size-specialised kernels, the two radices A, B of the two-pass split its backward
+ * length on the size-specialised kernels, the radices of the two- or three-pass split its backward
  * pass runs (of the complex FFT length: half the x length for the x pass of an R2C transform);
- * spfft_gb300_transform_splits gives every pass. */
-/* Two-pass splits of the size-specialised kernels (no counterpart in the reference): radices[0..5]
+ * spfft_gb300_transform_split_stages gives every pass. */
+/* Splits of the size-specialised kernels (no counterpart in the reference): radices[0..5]
  * = the first-pass radix A of the split A x B (A * B = the pass's complex FFT length) that the z
  * backward, z forward, y backward, y forward, x backward and x forward passes run, 0 for a pass on
  * the generic kernels. The z passes and the split y passes are built in both orders of their two
- * radices wherever the orders differ (192: 12 x 16 and 16 x 12); the autotuner chooses one per pass,
- * and SPFFT_GB300_SPLITS=zb,zf,yb,yf (each 0 for the default order, 1 for the swapped one) at
- * transform creation sets them. The fused plane kernels and the x passes have one fixed split. */
+ * radices wherever the orders differ (192: 12 x 16 and 16 x 12), and, in double precision for the
+ * lengths whose second radix is 12 or 16 (144, 180, 192, 256), as a three-pass split A x B1 x B2
+ * that runs the B-point DFTs as two shared-memory passes (192: 12 x 4 x 4); the autotuner chooses
+ * one per pass, and SPFFT_GB300_SPLITS=zb,zf,yb,yf (each 0 for the default order, 1 for the swapped
+ * one, 2 for the three-pass split) at transform creation sets them. The fused plane kernels and
+ * the x passes have one fixed split. */
 SPFFT_EXPORT SpfftError spfft_gb300_transform_splits(SpfftTransform transform, int* radices);
 SPFFT_EXPORT SpfftError spfft_gb300_float_transform_splits(SpfftFloatTransform transform, int* radices);
+/* Every radix of those splits (no counterpart in the reference): stages[3 * pass + 0..2] for the
+ * six passes in the order above, (A, B, 0) for a two-pass split, (A, B1, B2) for a three-pass split,
+ * (0, 0, 0) for a pass on the generic kernels. */
+SPFFT_EXPORT SpfftError spfft_gb300_transform_split_stages(SpfftTransform transform, int* stages);
+SPFFT_EXPORT SpfftError spfft_gb300_float_transform_split_stages(SpfftFloatTransform transform, int* stages);
 SPFFT_EXPORT SpfftError spfft_gb300_transform_radix_plans(SpfftTransform transform, int* numStages,
                                                           int* radices);
 SPFFT_EXPORT SpfftError spfft_gb300_float_transform_radix_plans(SpfftFloatTransform transform,

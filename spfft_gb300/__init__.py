@@ -135,6 +135,7 @@ def _declare(lib: ctypes.CDLL) -> None:
         getattr(lib, prefix + "transform_tuning").argtypes = [_vp, _ip]
         getattr(lib, prefix + "transform_x_backward_rows").argtypes = [_vp, _ip]
         getattr(lib, prefix + "transform_splits").argtypes = [_vp, _ip]
+        getattr(lib, prefix + "transform_split_stages").argtypes = [_vp, _ip]
         getattr(lib, prefix + "transform_radix_plans").argtypes = [_vp, _ip, _ip]
         getattr(lib, prefix + "transform_adjoint_backward").argtypes = [_vp, _vp, _vp, _vp]
         getattr(lib, prefix + "transform_adjoint_forward").argtypes = [_vp, _vp, _vp, _i, _vp]
@@ -438,17 +439,15 @@ class Transform:
                 "rows_per_x_block": v[5], "rows_per_x_backward_block": xb.value}
 
     def splits(self) -> dict:
-        """Two-pass split (A, B) of each size-specialised pass (None for a generic-kernel pass)."""
-        v = (ctypes.c_int * 6)()
-        _call("spfft_gb300_" + self._p[len("spfft_"):] + "transform_splits", self._h, v)
-        dims = {"z": self.dim_z(), "y": self.dim_y(), "x": self.dim_x()}
+        """Split of each size-specialised pass: (A, B) for a two-pass split, (A, B1, B2) for a
+        three-pass split (None for a generic-kernel pass)."""
+        v = (ctypes.c_int * 18)()
+        _call("spfft_gb300_" + self._p[len("spfft_"):] + "transform_split_stages", self._h, v)
         out = {}
         for i, name in enumerate(["z_backward", "z_forward", "y_backward", "y_forward", "x_backward",
                                   "x_forward"]):
-            n = dims[name[0]]
-            if name[0] == "x" and self._type == SPFFT_TRANS_R2C:
-                n //= 2
-            out[name] = (v[i], n // v[i]) if v[i] > 0 else None
+            st = [v[3 * i + j] for j in range(3)]
+            out[name] = tuple(r for r in st if r > 0) if st[0] > 0 else None
         return out
 
     def radix_plans(self) -> list:

@@ -273,23 +273,26 @@ SPFFT_GB300_GRID_C_API(spfft_float_grid_, GridFloat)
       spfft::TransformAccess::get(t).gpu_plan().split_radices(radices);                           \
     });                                                                                           \
   }                                                                                               \
+  SpfftError GPREFIX##split_stages(void* transform, int* stages) {                               \
+    return with_handle<spfft::TRANSFORM>(transform, [&](spfft::TRANSFORM& t) {                    \
+      if (!stages) throw spfft::InvalidParameterError();                                          \
+      spfft::TransformAccess::get(t).gpu_plan().split_stages(stages);                             \
+    });                                                                                           \
+  }                                                                                               \
   SpfftError GPREFIX##radix_plans(void* transform, int* numStages, int* radices) {                \
     return with_handle<spfft::TRANSFORM>(transform, [&](spfft::TRANSFORM& t) {                    \
       if (!numStages || !radices) throw spfft::InvalidParameterError();                           \
       const auto& plan = spfft::TransformAccess::get(t).gpu_plan();                               \
-      int split[6];                                                                               \
-      plan.split_radices(split);                                                                  \
-      const int dims[3] = {t.dim_z(), t.dim_y(), t.dim_x()};                                      \
+      int split[18];                                                                              \
+      plan.split_stages(split);                                                                   \
       for (int d = 0; d < 3; ++d) {                                                               \
         for (int i = 0; i < spfft::gb300::kMaxStages; ++i) radices[d * spfft::gb300::kMaxStages + i] = 0; \
-        /* size-specialised backward pass of this length: its two-pass split A x B, of the */      \
-        /* complex FFT length (half the x length for the R2C x pass) */                           \
-        const int a = split[d == 0 ? 0 : d == 1 ? 2 : 4];                                         \
-        if (a > 0) {                                                                              \
-          const int len = (d == 2 && t.type() == SPFFT_TRANS_R2C) ? dims[d] / 2 : dims[d];        \
-          numStages[d] = 2;                                                                       \
-          radices[d * spfft::gb300::kMaxStages] = a;                                              \
-          radices[d * spfft::gb300::kMaxStages + 1] = len / a;                                    \
+        /* size-specialised backward pass of this length: the radices of its two- or three-pass */ \
+        /* split, of the complex FFT length (half the x length for the R2C x pass) */             \
+        const int* sp = split + 3 * (d == 0 ? 0 : d == 1 ? 2 : 4);                                 \
+        if (sp[0] > 0) {                                                                          \
+          numStages[d] = sp[2] > 0 ? 3 : 2;                                                       \
+          for (int i = 0; i < numStages[d]; ++i) radices[d * spfft::gb300::kMaxStages + i] = sp[i]; \
           continue;                                                                               \
         }                                                                                         \
         const spfft::gb300::RadixPlan r = plan.radix_plan(d);                                     \

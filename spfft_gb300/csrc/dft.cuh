@@ -192,11 +192,59 @@ constexpr bool has_swapped_split() {
   return Shape<N, 2>::A != Shape<N, 1>::A;
 }
 
-// Position of X[k] after pass 2 stored back in place.
+// Variant 3 is variant 1 run in three passes: the B-point DFT of pass 2 is itself split as
+// B = B1 * B2 (Factor<B>) into a pass of B1-point DFTs (pass 2a, with the w_B twiddles) and a
+// pass of B2-point DFTs (pass 2b), with one more shared-memory exchange between them. No work item
+// then holds more than max(A, B1, B2) values (double-float 16-point DFTs need more registers than
+// three blocks per SM leave a thread), and pass 2 has B2 (2a) and B1 (2b) times as many work items.
+template <int N>
+struct Shape<N, 3> : Shape<N, 1> {};
+template <int R>
+struct HasFactor {
+  static constexpr bool value = false;
+};
+#define SPFFT_GB300_HAS_FACTOR(R_) \
+  template <>                      \
+  struct HasFactor<R_> {           \
+    static constexpr bool value = true; \
+  };
+SPFFT_GB300_HAS_FACTOR(12)
+SPFFT_GB300_HAS_FACTOR(16)
+#undef SPFFT_GB300_HAS_FACTOR
+// Lengths that have the three-pass variant: a second factor of 12 or 16.
+template <int N>
+constexpr bool has_three_pass() {
+  return HasFactor<Shape<N, 1>::B>::value;
+}
+template <int N, bool = has_three_pass<N>()>
+struct Split3 {
+  static constexpr int A = Shape<N, 1>::A, B = Shape<N, 1>::B, B1 = 1, B2 = 1;
+};
+template <int N>
+struct Split3<N, true> {
+  static constexpr int A = Shape<N, 1>::A, B = Shape<N, 1>::B;
+  static constexpr int B1 = Factor<B>::first, B2 = Factor<B>::second;
+};
+
+// Position of X[k] after pass 2 stored back in place: (k mod A) * B + k div A for the two-pass
+// variants; for variant 3, pass 2b leaves X[k1 + A (kk1 + B1 kk2)] at k1 B + kk1 B2 + kk2.
 template <int N, int V = 0>
 __host__ __device__ __forceinline__ int transposed_pos(int k) {
   constexpr int A = Shape<N, V>::A, B = Shape<N, V>::B;
-  return (k % A) * B + k / A;
+  if constexpr (V == 3) {
+    constexpr int B1 = Split3<N>::B1, B2 = Split3<N>::B2;
+    const int k2 = k / A;
+    return (k - k2 * A) * B + (k2 % B1) * B2 + k2 / B1;
+  } else {
+    return (k % A) * B + k / A;
+  }
+}
+// Variant 3: the output index k of the value pass 2b leaves at in-place position e.
+template <int N>
+__host__ __device__ __forceinline__ int three_pass_index(int e) {
+  constexpr int A = Split3<N>::A, B = Split3<N>::B, B1 = Split3<N>::B1, B2 = Split3<N>::B2;
+  const int k1 = e / B, r = e - k1 * B, kk1 = r / B2, kk2 = r - kk1 * B2;
+  return k1 + A * (kk1 + B1 * kk2);
 }
 
 template <int N, int SIGN, int V = 0, typename C>
@@ -231,6 +279,33 @@ __host__ __device__ __forceinline__ void fft_pass2(const C* buf, int stride, int
 #pragma unroll
   for (int b = 0; b < B; ++b) v[b] = buf[(k1 * B + b) * stride];
   Dft<B, SIGN>::run(v);
+}
+
+// Variant 3, pass 2a (one work item per (k1, i2), after pass 1): the B1-point DFTs over
+// b = i1 * B2 + i2 of row k1, times w_B^(kk1 * i2) = w_N^(kk1 * i2 * A) from the same w_N table,
+// stored back in place at k1 * B + kk1 * B2 + i2 (the first half of Dft<B>::run).
+template <int N, int SIGN, typename C>
+__host__ __device__ __forceinline__ void fft_pass2a(C* buf, int stride, int k1, int i2, const C* __restrict__ tw) {
+  constexpr int A = Split3<N>::A, B = Split3<N>::B, B1 = Split3<N>::B1, B2 = Split3<N>::B2;
+  C v[B1];
+#pragma unroll
+  for (int i1 = 0; i1 < B1; ++i1) v[i1] = buf[(k1 * B + i1 * B2 + i2) * stride];
+  Dft<B1, SIGN>::run(v);
+#pragma unroll
+  for (int kk1 = 1; kk1 < B1; ++kk1) v[kk1] = ctw<SIGN>(v[kk1], tw[kk1 * i2 * A]);
+#pragma unroll
+  for (int kk1 = 0; kk1 < B1; ++kk1) buf[(k1 * B + kk1 * B2 + i2) * stride] = v[kk1];
+}
+
+// Variant 3, pass 2b (one work item per (k1, kk1), after pass 2a): the B2-point DFT over i2;
+// v[kk2] = X[k1 + A * (kk1 + B1 * kk2)] (the second half of Dft<B>::run).
+template <int N, int SIGN, typename C>
+__host__ __device__ __forceinline__ void fft_pass2b(const C* buf, int stride, int k1, int kk1,
+                                                    C (&v)[Split3<N>::B2]) {
+  constexpr int B = Split3<N>::B, B2 = Split3<N>::B2;
+#pragma unroll
+  for (int i2 = 0; i2 < B2; ++i2) v[i2] = buf[(k1 * B + kk1 * B2 + i2) * stride];
+  Dft<B2, SIGN>::run(v);
 }
 
 }  // namespace gb300

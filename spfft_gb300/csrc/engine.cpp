@@ -351,9 +351,10 @@ GpuPlan<T>::GpuPlan(const IndexPlan& p, int device) {
         if (c[0] == cpb && c[1] == rpb && c[2] == want) splitRpbB_ = want;
       }
     }
-    // Passes that can run the swapped two-pass split of their length (FastOp::SplitRadix): the
-    // specialised z pass and the split y passes. SPFFT_GB300_SPLITS=zb,zf,yb,yf (each 0 or 1)
-    // chooses it per pass at creation (z backward, z forward, y backward, y forward).
+    // Passes that can run the swapped two-pass split or the three-pass split of their length
+    // (FastOp::SplitRadix): the specialised z pass and the split y passes.
+    // SPFFT_GB300_SPLITS=zb,zf,yb,yf (each 0 default, 1 swapped, 2 three-pass) chooses per pass at
+    // creation (z backward, z forward, y backward, y forward).
     {
       size_t rad = 0;
       a.smemOut = &rad;
@@ -362,14 +363,16 @@ GpuPlan<T>::GpuPlan(const IndexPlan& p, int device) {
       zSwap_ = fastZ_ && fast_dispatch<T>(FastOp::SplitRadix, nz, false, a) && rad > 0;
       a.param = 1;
       ySwap_ = splitOk && fast_dispatch<T>(FastOp::SplitRadix, p.dimY, r2c, a) && rad > 0;
+      a.split = 2;
+      a.param = 0;
+      zThree_ = fastZ_ && fast_dispatch<T>(FastOp::SplitRadix, nz, false, a) && rad > 0;
+      a.param = 1;
+      yThree_ = splitOk && fast_dispatch<T>(FastOp::SplitRadix, p.dimY, r2c, a) && rad > 0;
       a.split = 0;
       if (const char* sw = std::getenv("SPFFT_GB300_SPLITS")) {
         int v[4] = {0, 0, 0, 0};
         if (std::sscanf(sw, "%d,%d,%d,%d", &v[0], &v[1], &v[2], &v[3]) == 4) {
-          for (int i = 0; i < 4; ++i) {
-            const bool ok = i < 2 ? zSwap_ : (ySwap_ && planePath_ == PlanePath::Split);
-            splitChoice_[i] = (v[i] == 1 && ok) ? 1 : 0;
-          }
+          for (int i = 0; i < 4; ++i) splitChoice_[i] = split_valid(i, v[i], i < 2 || planePath_ == PlanePath::Split) ? v[i] : 0;
         }
       }
     }
@@ -721,6 +724,30 @@ void GpuPlan<T>::split_radices(int* radices) const {
 }
 
 template <typename T>
+void GpuPlan<T>::split_stages(int* stages) const {
+  int first[6];
+  split_radices(first);
+  for (int i = 0; i < 18; ++i) stages[i] = 0;
+  const int lens[6] = {base_.dimZ, base_.dimZ, base_.dimY, base_.dimY,
+                       base_.r2c ? base_.dimX / 2 : base_.dimX, base_.r2c ? base_.dimX / 2 : base_.dimX};
+  for (int i = 0; i < 6; ++i) {
+    if (first[i] <= 0) continue;
+    const int b = lens[i] / first[i];
+    stages[3 * i] = first[i];
+    stages[3 * i + 1] = b;
+    if (i < 4 && splitChoice_[i] == 2) {
+      FastArgs<T> a;
+      size_t b1 = 0;
+      a.smemOut = &b1;
+      if (fast_dispatch<T>(FastOp::ThreePassFactor, i < 2 ? base_.dimZ : base_.dimY, base_.r2c != 0, a) && b1 > 0) {
+        stages[3 * i + 1] = static_cast<int>(b1);
+        stages[3 * i + 2] = b / static_cast<int>(b1);
+      }
+    }
+  }
+}
+
+template <typename T>
 std::vector<typename GpuPlan<T>::Tuning> GpuPlan<T>::candidates() const {
   std::vector<int> zs = zCands_;
   if (zs.empty()) zs.push_back(0);
@@ -760,10 +787,7 @@ void GpuPlan<T>::set_tuning(const Tuning& t) {
           c.cpb == t.cpb && c.rpb == t.rpb && c.rpbB == t.rpbB;
   }
   for (int d = 0; d < 3; ++d) ok &= t.radix[d] >= 0 && t.radix[d] < static_cast<int>(radixCands_[d].size());
-  for (int i = 0; i < 4; ++i) {
-    const bool swappable = i < 2 ? (zSwap_ && t.spb > 0) : (ySwap_ && t.path == 2);
-    ok &= t.split[i] == 0 || (t.split[i] == 1 && swappable);
-  }
+  for (int i = 0; i < 4; ++i) ok &= split_valid(i, t.split[i], i < 2 ? t.spb > 0 : t.path == 2);
   if (!ok) throw InvalidParameterError();
   for (int i = 0; i < 4; ++i) splitChoice_[i] = t.split[i];
   for (int d = 0; d < 3; ++d) radixChoice_[d] = t.radix[d];
@@ -827,16 +851,20 @@ float GpuPlan<T>::autotune(T* values, T* space, void* scratch, cudaStream_t stre
         }
       }
     }
-    // the two-pass split of each specialised z and split-y pass: the default or the swapped order
+    // the split of each specialised z and split-y pass: the default order, the swapped order or
+    // three passes
     for (int i = 0; i < 4; ++i) {
-      const bool swappable = i < 2 ? (zSwap_ && best.spb > 0) : (ySwap_ && best.path == 2);
-      if (!swappable) continue;
-      Tuning c = best;
-      c.split[i] = 1 - c.split[i];
-      const float ms = time_pair(c);
-      if (ms < bestMs) {
-        bestMs = ms;
-        best = c;
+      if (i < 2 ? best.spb == 0 : best.path != 2) continue;
+      const int current = best.split[i];
+      for (int v = 0; v < 3; ++v) {
+        if (v == current || !split_valid(i, v, true)) continue;
+        Tuning c = best;
+        c.split[i] = v;
+        const float ms = time_pair(c);
+        if (ms < bestMs) {
+          bestMs = ms;
+          best = c;
+        }
       }
     }
     // radix plans of the lengths the generic kernels transform: z without specialised z kernels,

@@ -77,12 +77,17 @@ public:
     int rpbB = 0;          // split: rows per x backward block
     int radix[3] = {0, 0, 0};  // generic kernels: radix plan of z, y, x (index into radix_plans())
     // size-specialised z backward, z forward, split y backward, split y forward passes: 1 runs
-    // the swapped two-pass split of the length (B x A instead of A x B), where it has one
+    // the swapped two-pass split of the length (B x A instead of A x B), 2 the three-pass split
+    // (A x B1 x B2 with B = B1 * B2), where the length has one
     int split[4] = {0, 0, 0, 0};
   };
-  // First-pass radix A of the two-pass split (length = A * B) each pass runs with: z backward,
+  // First-pass radix A of the split (length = A * B) each pass runs with: z backward,
   // z forward, y backward, y forward, x backward, x forward; 0 for a pass on the generic kernels.
   void split_radices(int* radices) const;
+  // The radices of each pass's split, stages[3 * pass + 0..2]: (A, B, 0) for a two-pass split,
+  // (A, B1, B2) for a three-pass split, zeros for a pass on the generic kernels (pass order as in
+  // split_radices).
+  void split_stages(int* stages) const;
   // Radix plans available to the generic kernels for the z, y and x lengths (dim 0, 1, 2), and
   // the ones in use.
   const std::vector<RadixPlan>& radix_plans(int dim) const { return radixCands_[dim]; }
@@ -129,6 +134,17 @@ private:
   int radixChoice_[3] = {0, 0, 0};
   int splitChoice_[4] = {0, 0, 0, 0};  // Tuning::split
   bool zSwap_ = false, ySwap_ = false;  // the z / split y length has a swapped split
+  bool zThree_ = false, yThree_ = false;  // the z / split y length has a three-pass split
+  // Whether split variant v (0 default, 1 swapped, 2 three-pass) exists for pass i (0 z backward,
+  // 1 z forward, 2 y backward, 3 y forward); `active`: the pass runs on the specialised z kernels
+  // (i < 2) or on the split y kernels (i >= 2). Variant 0 is always valid.
+  bool split_valid(int i, int v, bool active) const {
+    if (v == 0) return true;
+    if (!active) return false;
+    if (v == 1) return i < 2 ? zSwap_ : ySwap_;
+    if (v == 2) return i < 2 ? zThree_ : yThree_;
+    return false;
+  }
   ScratchLayout layout_{};
   T scale_ = T(1);
   int numValues_ = 0;

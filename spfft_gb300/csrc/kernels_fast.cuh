@@ -55,14 +55,15 @@ struct YMinBlocks<dd> {
   static constexpr int value = 3;
 };
 // Minimum resident 256-thread blocks per SM asked of the compiler for the z kernels: double-float
-// z backward two (at most 128 registers), z forward three (at most 80).
-template <typename A>
+// z backward two (at most 128 registers) with a two-pass split, three (at most 80) with the
+// three-pass split (V = 3, at most 12 values per work item), z forward three (at most 80).
+template <typename A, int V = 1>
 struct ZBackwardMinBlocks {
   static constexpr int value = 4;  // FP32: at most 64 registers (the kernel needs about 50)
 };
-template <>
-struct ZBackwardMinBlocks<dd> {
-  static constexpr int value = 2;
+template <int V>
+struct ZBackwardMinBlocks<dd, V> {
+  static constexpr int value = V == 3 ? 3 : 2;
 };
 template <typename A>
 struct ZForwardMinBlocks {
@@ -432,37 +433,66 @@ __device__ __forceinline__ void z_backward_body(const PlanView<S>& p, const S* _
   CS* sticks = reinterpret_cast<CS*>(p.sticks) + s0;
   const bool raw = TT::kScaled && p.sticksRaw;
   const bool park = TT::kScaled && !raw && exact_block(k);
-  for (int i = threadIdx.x; i < nsb * Az; i += blockDim.x) {
-    const int k1 = dns.div(i), sl = i - k1 * nsb;
-    CA v[Bz];
-    fft_pass2<NZ, +1, V>(buf + sl * PZ, 1, k1, v);
-    if (raw) {
-      CA* rs = reinterpret_cast<CA*>(sticks);
+  if constexpr (V == 3) {
+    // pass 2 as pass 2a (B1-point DFTs) and pass 2b (B2-point DFTs); sticks fastest across threads
+    constexpr int B1 = Split3<NZ>::B1, B2 = Split3<NZ>::B2;
+    for (int i = threadIdx.x; i < nsb * Az * B2; i += blockDim.x) {
+      const int r = dns.div(i), sl = i - r * nsb, k1 = r / B2;
+      fft_pass2a<NZ, +1>(buf + sl * PZ, 1, k1, r - k1 * B2, tw);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < nsb * Az * B1; i += blockDim.x) {
+      const int r = dns.div(i), sl = i - r * nsb, k1 = r / B1, kk1 = r - k1 * B1;
+      CA v[B2];
+      fft_pass2b<NZ, +1>(buf + sl * PZ, 1, k1, kk1, v);
 #pragma unroll
-      for (int k2 = 0; k2 < Bz; ++k2) rs[static_cast<size_t>(k1 + Az * k2) * p.numSticks + sl] = v[k2];
-    } else if (park) {
-      // blocks of tiny values: results back into this item's own pass-2 slots, stored exactly below
+      for (int kk2 = 0; kk2 < B2; ++kk2) {
+        const size_t at = static_cast<size_t>(k1 + Az * (kk1 + B1 * kk2)) * p.numSticks + sl;
+        if (raw) reinterpret_cast<CA*>(sticks)[at] = v[kk2];
+        else if (park) buf[sl * PZ + k1 * Bz + kk1 * B2 + kk2] = v[kk2];
+        else sticks[at] = to_storage(v[kk2], k);
+      }
+    }
+  } else {
+    for (int i = threadIdx.x; i < nsb * Az; i += blockDim.x) {
+      const int k1 = dns.div(i), sl = i - k1 * nsb;
+      CA v[Bz];
+      fft_pass2<NZ, +1, V>(buf + sl * PZ, 1, k1, v);
+      if (raw) {
+        CA* rs = reinterpret_cast<CA*>(sticks);
 #pragma unroll
-      for (int k2 = 0; k2 < Bz; ++k2) buf[sl * PZ + k1 * Bz + k2] = v[k2];
-    } else {
+        for (int k2 = 0; k2 < Bz; ++k2) rs[static_cast<size_t>(k1 + Az * k2) * p.numSticks + sl] = v[k2];
+      } else if (park) {
+        // blocks of tiny values: results back into this item's own pass-2 slots, stored exactly below
 #pragma unroll
-      for (int k2 = 0; k2 < Bz; ++k2) {
-        sticks[static_cast<size_t>(k1 + Az * k2) * p.numSticks + sl] = to_storage(v[k2], k);
+        for (int k2 = 0; k2 < Bz; ++k2) buf[sl * PZ + k1 * Bz + k2] = v[k2];
+      } else {
+#pragma unroll
+        for (int k2 = 0; k2 < Bz; ++k2) {
+          sticks[static_cast<size_t>(k1 + Az * k2) * p.numSticks + sl] = to_storage(v[k2], k);
+        }
       }
     }
   }
   if (park) {
     __syncthreads();
     for (int i = threadIdx.x; i < nsb * NZ; i += blockDim.x) {
-      const int sl = i / NZ, e = i - sl * NZ, k1 = e / Bz, k2 = e - k1 * Bz;
-      sticks[static_cast<size_t>(k1 + Az * k2) * p.numSticks + sl] = to_storage_exact(buf[sl * PZ + e], k);
+      const int sl = i / NZ, e = i - sl * NZ;
+      int z;
+      if constexpr (V == 3) {
+        z = three_pass_index<NZ>(e);
+      } else {
+        const int k1 = e / Bz;
+        z = k1 + Az * (e - k1 * Bz);
+      }
+      sticks[static_cast<size_t>(z) * p.numSticks + sl] = to_storage_exact(buf[sl * PZ + e], k);
     }
   }
   if (raw && threadIdx.x < nsb) p.stickExp[s0 + threadIdx.x] = produced_exp(sExp, k);
 }
 
 template <typename S, typename A, int NZ, int V = 1>
-__global__ void __launch_bounds__(kThreads, ZBackwardMinBlocks<A>::value) z_backward(const PlanView<S> p,
+__global__ void __launch_bounds__(kThreads, ZBackwardMinBlocks<A, V>::value) z_backward(const PlanView<S> p,
                                                        const S* __restrict__ values, int spb) {
   __shared__ int sExp[2];
   z_backward_body<S, A, NZ, V>(p, values, spb, blockIdx.x, sExp);
@@ -527,12 +557,28 @@ __device__ __forceinline__ void z_forward_body(const PlanView<S>& p, S* __restri
     fft_pass1<NZ, -1, V>(buf + sl * PZ, 1, b, tw);
   }
   __syncthreads();
-  for (int i = threadIdx.x; i < nsb * Az; i += blockDim.x) {
-    const int k1 = dns.div(i), sl = i - k1 * nsb;
-    CA v[Bz];
-    fft_pass2<NZ, -1, V>(buf + sl * PZ, 1, k1, v);
+  if constexpr (V == 3) {
+    constexpr int B1 = Split3<NZ>::B1, B2 = Split3<NZ>::B2;
+    for (int i = threadIdx.x; i < nsb * Az * B2; i += blockDim.x) {
+      const int r = dns.div(i), sl = i - r * nsb, k1 = r / B2;
+      fft_pass2a<NZ, -1>(buf + sl * PZ, 1, k1, r - k1 * B2, tw);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < nsb * Az * B1; i += blockDim.x) {
+      const int r = dns.div(i), sl = i - r * nsb, k1 = r / B1, kk1 = r - k1 * B1;
+      CA v[B2];
+      fft_pass2b<NZ, -1>(buf + sl * PZ, 1, k1, kk1, v);
 #pragma unroll
-    for (int k2 = 0; k2 < Bz; ++k2) buf[sl * PZ + k1 * Bz + k2] = v[k2];
+      for (int kk2 = 0; kk2 < B2; ++kk2) buf[sl * PZ + k1 * Bz + kk1 * B2 + kk2] = v[kk2];
+    }
+  } else {
+    for (int i = threadIdx.x; i < nsb * Az; i += blockDim.x) {
+      const int k1 = dns.div(i), sl = i - k1 * nsb;
+      CA v[Bz];
+      fft_pass2<NZ, -1, V>(buf + sl * PZ, 1, k1, v);
+#pragma unroll
+      for (int k2 = 0; k2 < Bz; ++k2) buf[sl * PZ + k1 * Bz + k2] = v[k2];
+    }
   }
   __syncthreads();
   CS* out = reinterpret_cast<CS*>(values);
@@ -1020,8 +1066,13 @@ inline void launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t s
   (void)cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
 }
 
-// `swapped`: run the swapped two-pass split (Shape<N, 2>) where the length has one
-// (has_swapped_split<N>), else the default (Shape<N, 1>).
+// `variant`: 0 the default split (Shape<N, 1>), 1 the swapped two-pass split (Shape<N, 2>) where
+// the length has one (has_swapped_split<N>), 2 the three-pass split (Shape<N, 3>) where the length
+// has one and the arithmetic is double-float (has_three<A, N>); otherwise the default.
+template <typename A, int N>
+constexpr bool has_three() {
+  return std::is_same<A, dd>::value && has_three_pass<N>();
+}
 template <typename S, typename A, int NZ>
 struct ZKernels {
   using CA = typename Types<S, A>::CA;
@@ -1033,19 +1084,29 @@ struct ZKernels {
       if (e1 == cudaSuccess) e1 = allow_dynamic_smem(z_backward<S, A, NZ, 2>, maxSmem);
       if (e2 == cudaSuccess) e2 = allow_dynamic_smem(z_forward<S, A, NZ, 2>, maxSmem);
     }
+    if constexpr (has_three<A, NZ>()) {
+      if (e1 == cudaSuccess) e1 = allow_dynamic_smem(z_backward<S, A, NZ, 3>, maxSmem);
+      if (e2 == cudaSuccess) e2 = allow_dynamic_smem(z_forward<S, A, NZ, 3>, maxSmem);
+    }
     return e1 != cudaSuccess ? e1 : e2;
   }
-  static void backward(const PlanView<S>& p, int spb, const S* values, cudaStream_t st, bool swapped) {
+  static void backward(const PlanView<S>& p, int spb, const S* values, cudaStream_t st, int variant) {
     const int g = (p.numSticks + spb - 1) / spb;
     if constexpr (has_swapped_split<NZ>()) {
-      if (swapped) return launch_pdl(z_backward<S, A, NZ, 2>, g, kThreads, smem(spb), st, p, values, spb);
+      if (variant == 1) return launch_pdl(z_backward<S, A, NZ, 2>, g, kThreads, smem(spb), st, p, values, spb);
+    }
+    if constexpr (has_three<A, NZ>()) {
+      if (variant == 2) return launch_pdl(z_backward<S, A, NZ, 3>, g, kThreads, smem(spb), st, p, values, spb);
     }
     launch_pdl(z_backward<S, A, NZ>, g, kThreads, smem(spb), st, p, values, spb);
   }
-  static void forward(const PlanView<S>& p, int spb, S* values, S scale, cudaStream_t st, bool swapped) {
+  static void forward(const PlanView<S>& p, int spb, S* values, S scale, cudaStream_t st, int variant) {
     const int g = (p.numSticks + spb - 1) / spb;
     if constexpr (has_swapped_split<NZ>()) {
-      if (swapped) return launch_pdl(z_forward<S, A, NZ, 2>, g, kThreads, smem(spb), st, p, values, scale, spb);
+      if (variant == 1) return launch_pdl(z_forward<S, A, NZ, 2>, g, kThreads, smem(spb), st, p, values, scale, spb);
+    }
+    if constexpr (has_three<A, NZ>()) {
+      if (variant == 2) return launch_pdl(z_forward<S, A, NZ, 3>, g, kThreads, smem(spb), st, p, values, scale, spb);
     }
     launch_pdl(z_forward<S, A, NZ>, g, kThreads, smem(spb), st, p, values, scale, spb);
   }
@@ -1185,28 +1246,57 @@ __device__ __forceinline__ void y_backward_body(const PlanView<S>& p, int cpb, i
   CS* planes = reinterpret_cast<CS*>(p.planes) + static_cast<size_t>(z) * NY * nc + c0;
   const bool raw = TT::kScaled && p.planesRaw;
   const bool park = TT::kScaled && !raw && exact_block(k);
-  for (int i = threadIdx.x; i < ncb * Ay; i += blockDim.x) {
-    const int k1 = dncb.div(i), c = i - k1 * ncb;
-    CA v[By];
-    fft_pass2<NY, +1, V>(buf + c, ncb, k1, v);
-    if (raw) {
-      CA* rp = reinterpret_cast<CA*>(planes);
+  if constexpr (V == 3) {
+    // pass 2 as pass 2a (B1-point DFTs) and pass 2b (B2-point DFTs); columns fastest across threads
+    constexpr int B1 = Split3<NY>::B1, B2 = Split3<NY>::B2;
+    for (int i = threadIdx.x; i < ncb * Ay * B2; i += blockDim.x) {
+      const int r = dncb.div(i), c = i - r * ncb, k1 = r / B2;
+      fft_pass2a<NY, +1>(buf + c, ncb, k1, r - k1 * B2, tw);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < ncb * Ay * B1; i += blockDim.x) {
+      const int r = dncb.div(i), c = i - r * ncb, k1 = r / B1, kk1 = r - k1 * B1;
+      CA v[B2];
+      fft_pass2b<NY, +1>(buf + c, ncb, k1, kk1, v);
 #pragma unroll
-      for (int k2 = 0; k2 < By; ++k2) rp[static_cast<size_t>(k1 + Ay * k2) * nc + c] = v[k2];
-    } else if (park) {
-      // blocks of tiny values: results back into this item's own pass-2 slots, stored exactly below
+      for (int kk2 = 0; kk2 < B2; ++kk2) {
+        const size_t at = static_cast<size_t>(k1 + Ay * (kk1 + B1 * kk2)) * nc + c;
+        if (raw) reinterpret_cast<CA*>(planes)[at] = v[kk2];
+        else if (park) buf[(k1 * By + kk1 * B2 + kk2) * ncb + c] = v[kk2];
+        else planes[at] = to_storage(v[kk2], k);
+      }
+    }
+  } else {
+    for (int i = threadIdx.x; i < ncb * Ay; i += blockDim.x) {
+      const int k1 = dncb.div(i), c = i - k1 * ncb;
+      CA v[By];
+      fft_pass2<NY, +1, V>(buf + c, ncb, k1, v);
+      if (raw) {
+        CA* rp = reinterpret_cast<CA*>(planes);
 #pragma unroll
-      for (int k2 = 0; k2 < By; ++k2) buf[(k1 * By + k2) * ncb + c] = v[k2];
-    } else {
+        for (int k2 = 0; k2 < By; ++k2) rp[static_cast<size_t>(k1 + Ay * k2) * nc + c] = v[k2];
+      } else if (park) {
+        // blocks of tiny values: results back into this item's own pass-2 slots, stored exactly below
 #pragma unroll
-      for (int k2 = 0; k2 < By; ++k2) planes[static_cast<size_t>(k1 + Ay * k2) * nc + c] = to_storage(v[k2], k);
+        for (int k2 = 0; k2 < By; ++k2) buf[(k1 * By + k2) * ncb + c] = v[k2];
+      } else {
+#pragma unroll
+        for (int k2 = 0; k2 < By; ++k2) planes[static_cast<size_t>(k1 + Ay * k2) * nc + c] = to_storage(v[k2], k);
+      }
     }
   }
   if (park) {
     __syncthreads();
     for (int i = threadIdx.x; i < NY * ncb; i += blockDim.x) {
-      const int e = i / ncb, c = i - e * ncb, k1 = e / By, k2 = e - k1 * By;
-      planes[static_cast<size_t>(k1 + Ay * k2) * nc + c] = to_storage_exact(buf[e * ncb + c], k);
+      const int e = i / ncb, c = i - e * ncb;
+      int y;
+      if constexpr (V == 3) {
+        y = three_pass_index<NY>(e);
+      } else {
+        const int k1 = e / By;
+        y = k1 + Ay * (e - k1 * By);
+      }
+      planes[static_cast<size_t>(y) * nc + c] = to_storage_exact(buf[e * ncb + c], k);
     }
   }
   if (raw && threadIdx.x < ncb) p.planeExp[z * nc + c0 + threadIdx.x] = produced_exp(sExp, k);
@@ -1273,12 +1363,28 @@ __device__ __forceinline__ void y_forward_body(const PlanView<S>& p, int cpb, in
     fft_pass1<NY, -1, V>(buf + c, ncb, b, tw);
   }
   __syncthreads();
-  for (int i = threadIdx.x; i < ncb * Ay; i += blockDim.x) {
-    const int k1 = dncb.div(i), c = i - k1 * ncb;
-    CA v[By];
-    fft_pass2<NY, -1, V>(buf + c, ncb, k1, v);
+  if constexpr (V == 3) {
+    constexpr int B1 = Split3<NY>::B1, B2 = Split3<NY>::B2;
+    for (int i = threadIdx.x; i < ncb * Ay * B2; i += blockDim.x) {
+      const int r = dncb.div(i), c = i - r * ncb, k1 = r / B2;
+      fft_pass2a<NY, -1>(buf + c, ncb, k1, r - k1 * B2, tw);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < ncb * Ay * B1; i += blockDim.x) {
+      const int r = dncb.div(i), c = i - r * ncb, k1 = r / B1, kk1 = r - k1 * B1;
+      CA v[B2];
+      fft_pass2b<NY, -1>(buf + c, ncb, k1, kk1, v);
 #pragma unroll
-    for (int k2 = 0; k2 < By; ++k2) buf[(k1 * By + k2) * ncb + c] = v[k2];
+      for (int kk2 = 0; kk2 < B2; ++kk2) buf[(k1 * By + kk1 * B2 + kk2) * ncb + c] = v[kk2];
+    }
+  } else {
+    for (int i = threadIdx.x; i < ncb * Ay; i += blockDim.x) {
+      const int k1 = dncb.div(i), c = i - k1 * ncb;
+      CA v[By];
+      fft_pass2<NY, -1, V>(buf + c, ncb, k1, v);
+#pragma unroll
+      for (int k2 = 0; k2 < By; ++k2) buf[(k1 * By + k2) * ncb + c] = v[k2];
+    }
   }
   __syncthreads();
   CS* sticks = reinterpret_cast<CS*>(p.sticks) + static_cast<size_t>(z) * p.numSticks;
@@ -1611,20 +1717,30 @@ struct YSplitKernels {
       if (e1 == cudaSuccess) e1 = allow_dynamic_smem(y_backward_split<S, A, NY, 2>, maxSmem);
       if (e2 == cudaSuccess) e2 = allow_dynamic_smem(y_forward_split<S, A, NY, 2>, maxSmem);
     }
+    if constexpr (has_three<A, NY>()) {
+      if (e1 == cudaSuccess) e1 = allow_dynamic_smem(y_backward_split<S, A, NY, 3>, maxSmem);
+      if (e2 == cudaSuccess) e2 = allow_dynamic_smem(y_forward_split<S, A, NY, 3>, maxSmem);
+    }
     return e1 != cudaSuccess ? e1 : e2;
   }
-  // planes [z0, z0 + nz) (nz < 0: all planes from z0); `swapped` as in ZKernels
-  static void backward(const PlanView<S>& p, int cpb, cudaStream_t st, int z0, int nz, bool swapped) {
+  // planes [z0, z0 + nz) (nz < 0: all planes from z0); `variant` as in ZKernels
+  static void backward(const PlanView<S>& p, int cpb, cudaStream_t st, int z0, int nz, int variant) {
     const dim3 g((p.numColumns + cpb - 1) / cpb, nz < 0 ? p.dimZ - z0 : nz);
     if constexpr (has_swapped_split<NY>()) {
-      if (swapped) return launch_pdl(y_backward_split<S, A, NY, 2>, g, kThreads, smem(cpb), st, p, cpb, z0);
+      if (variant == 1) return launch_pdl(y_backward_split<S, A, NY, 2>, g, kThreads, smem(cpb), st, p, cpb, z0);
+    }
+    if constexpr (has_three<A, NY>()) {
+      if (variant == 2) return launch_pdl(y_backward_split<S, A, NY, 3>, g, kThreads, smem(cpb), st, p, cpb, z0);
     }
     launch_pdl(y_backward_split<S, A, NY>, g, kThreads, smem(cpb), st, p, cpb, z0);
   }
-  static void forward(const PlanView<S>& p, int cpb, cudaStream_t st, int z0, int nz, bool swapped) {
+  static void forward(const PlanView<S>& p, int cpb, cudaStream_t st, int z0, int nz, int variant) {
     const dim3 g((p.numColumns + cpb - 1) / cpb, nz < 0 ? p.dimZ - z0 : nz);
     if constexpr (has_swapped_split<NY>()) {
-      if (swapped) return launch_pdl(y_forward_split<S, A, NY, 2>, g, kThreads, smem(cpb), st, p, cpb, z0);
+      if (variant == 1) return launch_pdl(y_forward_split<S, A, NY, 2>, g, kThreads, smem(cpb), st, p, cpb, z0);
+    }
+    if constexpr (has_three<A, NY>()) {
+      if (variant == 2) return launch_pdl(y_forward_split<S, A, NY, 3>, g, kThreads, smem(cpb), st, p, cpb, z0);
     }
     launch_pdl(y_forward_split<S, A, NY>, g, kThreads, smem(cpb), st, p, cpb, z0);
   }
@@ -1655,17 +1771,18 @@ struct XSplitKernels {
   }
 };
 
-// First-pass radix A of the two-pass split (N = A * B) a kernel of length N runs (FastOp::SplitRadix):
-// which = 0 z pass, 1 split y pass (swapped: the swapped split; 0 where the length has none),
-// 2 / 3 y pass of the fused plane backward / forward kernel, 4 x pass (R2C: the half-length
-// complex FFT).
-template <int N>
-int split_radix(int which, bool swapped, bool r2c) {
+// First-pass radix A of the split (N = A * B) a kernel of length N runs (FastOp::SplitRadix):
+// which = 0 z pass, 1 split y pass (variant 0 the default split, 1 the swapped one, 2 the three-pass
+// split; 0 where the length has no such variant), 2 / 3 y pass of the fused plane backward /
+// forward kernel, 4 x pass (R2C: the half-length complex FFT).
+template <int N, typename A>
+int split_radix(int which, int variant, bool r2c) {
   switch (which) {
     case 0:
     case 1:
-      if (!swapped) return Shape<N, 1>::A;
-      return has_swapped_split<N>() ? Shape<N, 2>::A : 0;
+      if (variant == 1) return has_swapped_split<N>() ? Shape<N, 2>::A : 0;
+      if (variant == 2) return has_three<A, N>() ? Shape<N, 3>::A : 0;
+      return Shape<N, 1>::A;
     case 2:
       return Shape<N, 1>::A;
     case 3:
@@ -1675,6 +1792,12 @@ int split_radix(int which, bool swapped, bool r2c) {
     default:
       return 0;
   }
+}
+// The first factor B1 of B = B1 * B2 in the three-pass split of the z and split-y passes
+// (FastOp::ThreePassFactor); 0 where the length has no three-pass variant.
+template <int N, typename A>
+int three_pass_factor() {
+  return has_three<A, N>() ? Split3<N>::B1 : 0;
 }
 
 // Arithmetic type of the specialised kernels for a storage type: float for FP32, double-float

@@ -36,10 +36,14 @@ enum class FastOp {
   // batched fused plane passes (n = the cubic plane size; param = rows per x chunk)
   BatchPlaneBackward,
   BatchPlaneForward,
-  // first-pass radix A of a kernel's two-pass split N = A * B into *smemOut (0: no such split);
-  // param: 0 z pass, 1 split y pass (both with args.split), 2 / 3 y pass of the fused plane
-  // backward / forward kernel, 4 x pass (C2C, or R2C with r2c set: the half-length complex FFT)
-  SplitRadix
+  // first-pass radix A of a kernel's split N = A * B into *smemOut (0: no such split);
+  // param: 0 z pass, 1 split y pass (both with args.split: 0 default, 1 swapped, 2 three-pass),
+  // 2 / 3 y pass of the fused plane backward / forward kernel, 4 x pass (C2C, or R2C with r2c
+  // set: the half-length complex FFT)
+  SplitRadix,
+  // first factor B1 of B = B1 * B2 of the three-pass split of the z and split-y passes into
+  // *smemOut (0: the length has no three-pass split in this precision)
+  ThreePassFactor
 };
 
 // Threads of a batched fused plane block (two blocks per SM): 384 in FP32 (80 registers), 256 in
@@ -53,7 +57,7 @@ template <typename T>
 struct FastArgs {
   const PlanView<T>* plan = nullptr;
   int param = 0;  // sticks per block (z) or rows per chunk (plane)
-  int split = 0;  // z and split y passes: 1 runs the swapped two-pass split where the length has one
+  int split = 0;  // z and split y passes: 1 the swapped two-pass split, 2 the three-pass split
   int param2 = 0;  // batched plane forward: rows of the chunk buffer (2 * param double-buffers)
   int groups = 1;  // batched plane passes: independent row groups of the x pass
   int zBegin = 0, zCount = -1;  // split y and x passes: plane range (zCount < 0: to the last plane)

@@ -23,6 +23,8 @@ underflow. Tolerance: relative L2 <= 1e-12 (FP64), every output finite where the
 """
 from __future__ import annotations
 
+import os
+
 import numpy as np
 import pytest
 
@@ -41,29 +43,47 @@ UP = 600  # exact scale for the oracle on tiny inputs
 
 
 def _workload(name):
-    """(transform type, dims, triplets): two on the size-specialised double-float kernels, one on
-    the generic native-FP64 kernels."""
+    """(transform type, dims, triplets, creation environment): two on the size-specialised
+    double-float kernels, one on them with the three-pass split of the z and y lengths (144 =
+    12 x 4 x 3) on the split plane passes, one on the generic native-FP64 kernels."""
     if name == "c2c_64_sphere16":
-        return sp.SPFFT_TRANS_C2C, (64, 64, 64), sphere_indices(64, 16)
+        return sp.SPFFT_TRANS_C2C, (64, 64, 64), sphere_indices(64, 16), {}
     if name == "r2c_48_sphere12":
-        return sp.SPFFT_TRANS_R2C, (48, 48, 48), sphere_indices(48, 12, r2c=True)
+        return sp.SPFFT_TRANS_R2C, (48, 48, 48), sphere_indices(48, 12, r2c=True), {}
+    if name == "r2c_48_144_144_three_pass":
+        rng = np.random.default_rng(23)
+        return (sp.SPFFT_TRANS_R2C, (48, 144, 144),
+                random_indices(rng, 48, 144, 144, r2c=True, stick_frac=0.2, fill_frac=0.3),
+                {"SPFFT_GB300_PLANE": "split", "SPFFT_GB300_SPLITS": "2,2,2,2"})
     if name == "c2c_22_26_34":
         rng = np.random.default_rng(17)
         return sp.SPFFT_TRANS_C2C, (22, 26, 34), random_indices(rng, 22, 26, 34, r2c=False,
-                                                               stick_frac=0.5, fill_frac=0.6)
+                                                               stick_frac=0.5, fill_frac=0.6), {}
     raise KeyError(name)
 
 
-WORKLOADS = ["c2c_64_sphere16", "r2c_48_sphere12", "c2c_22_26_34"]
+WORKLOADS = ["c2c_64_sphere16", "r2c_48_sphere12", "r2c_48_144_144_three_pass", "c2c_22_26_34"]
 
 
 class Case:
     def __init__(self, name, dtype="float64"):
-        self.ttype, self.dims, self.idx = _workload(name)
+        self.ttype, self.dims, self.idx, env = _workload(name)
         self.dtype = dtype
         self.oracle = pipeline.HostPipeline(self.ttype, *self.dims, self.idx)
-        self.tr = sp.Transform(1, sp.SPFFT_PU_GPU, self.ttype, *self.dims, len(self.idx),
-                               sp.SPFFT_INDEX_TRIPLETS, self.idx, dtype=dtype)
+        saved = {k: os.environ.get(k) for k in env}
+        os.environ.update(env)
+        try:
+            self.tr = sp.Transform(1, sp.SPFFT_PU_GPU, self.ttype, *self.dims, len(self.idx),
+                                   sp.SPFFT_INDEX_TRIPLETS, self.idx, dtype=dtype)
+        finally:
+            for k, v in saved.items():
+                if v is None:
+                    os.environ.pop(k, None)
+                else:
+                    os.environ[k] = v
+        if "SPFFT_GB300_SPLITS" in env and dtype == "float64":
+            assert self.tr.splits()["z_backward"] == (12, 4, 3), self.tr.splits()
+            assert self.tr.splits()["y_forward"] == (12, 4, 3), self.tr.splits()
         self.ct = torch.complex128 if dtype == "float64" else torch.complex64
         self.st = self.ct if self.ttype == sp.SPFFT_TRANS_C2C else (
             torch.float64 if dtype == "float64" else torch.float32)

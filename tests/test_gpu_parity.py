@@ -393,6 +393,53 @@ def test_swapped_two_pass_splits(lib, dtype, choice, monkeypatch):
         assert rel_l2(f.cpu().numpy(), want_f) <= TOL[dtype], (n, ttype, choice)
 
 
+# Three-pass split (A, B1, B2) of the double-precision z and split-y kernels: the lengths whose
+# second radix B is 12 or 16, with B = B1 * B2.
+THREE_PASS = {144: (12, 4, 3), 180: (15, 4, 3), 192: (12, 4, 4), 256: (16, 4, 4)}
+
+
+@pytest.mark.parametrize("dtype", ["float64", "float32"])
+@pytest.mark.parametrize("choice", ["2,2,2,2", "2,0,1,2", "0,2,2,1"])
+def test_three_pass_splits(lib, dtype, choice, monkeypatch):
+    """The z and split-y kernels with the three-pass split (SPFFT_GB300_SPLITS value 2), per pass,
+    mixed with the default and swapped splits, for every length that has it: same results as the
+    oracle, and splits() / radix_plans() report (A, B1, B2). Single precision has no three-pass
+    kernels: a request for one keeps the default split."""
+    monkeypatch.setenv("SPFFT_GB300_PLANE", "split")
+    monkeypatch.setenv("SPFFT_GB300_SPLITS", choice)
+    want = [int(c) for c in choice.split(",")]
+    rng = np.random.default_rng(31)
+    for i, n in enumerate(sorted(THREE_PASS)):
+        ttype = i % 2
+        dims = (48, n, n)
+        idx = random_indices(rng, *dims, r2c=ttype == 1, stick_frac=0.3, fill_frac=0.5)
+        tr = _transform(dtype, ttype, dims, idx)
+        assert tr.path_info()["split_plane"]
+        a, b = DEFAULT_SPLIT[n]
+        got = tr.splits()
+        for name, v in zip(["z_backward", "z_forward", "y_backward", "y_forward"], want):
+            if v == 2 and dtype == "float64":
+                expect = THREE_PASS[n]
+            elif v == 1 and b > 1 and a != b:
+                expect = (b, a)
+            else:
+                expect = (a, b)
+            assert got[name] == expect, (n, name, got)
+        plans = tr.radix_plans()
+        assert plans[0] == list(got["z_backward"]) and plans[1] == list(got["y_backward"]), plans
+        vals = _values(rng, len(idx))
+        oracle = pipeline.HostPipeline(ttype, *dims, idx)
+        st = CT[dtype] if ttype == 0 else RT[dtype]
+        out = torch.empty(dims[::-1], dtype=st, device="cuda")
+        tr.backward(torch.from_numpy(vals).to(CT[dtype]).cuda(), out)
+        space = out.cpu().numpy()
+        assert rel_l2(space, oracle.backward(vals)) <= TOL[dtype], (n, ttype, choice)
+        f = torch.empty(len(idx), dtype=CT[dtype], device="cuda")
+        tr.forward(out, f, sp.SPFFT_FULL_SCALING)
+        want_f = oracle.forward(space.astype(np.complex128 if ttype == 0 else np.float64), scaled=True)
+        assert rel_l2(f.cpu().numpy(), want_f) <= TOL[dtype], (n, ttype, choice)
+
+
 @pytest.mark.parametrize("access", ["direct", "copy"])
 @pytest.mark.parametrize("dtype", ["float64", "float32"])
 def test_pinned_host_buffers(lib, access, dtype, monkeypatch):
