@@ -419,7 +419,7 @@ def measure_gpu(args, rank: int, world: int) -> dict:
     stream = torch.cuda.Stream()
     tuned = None
     if not args.no_autotune:  # plan-time autotuner (outside every timed region)
-        tr.autotune(3)
+        tr.autotune(10)
         tuned = tr.tuning()
         tuned["splits"] = {k: None if v is None else "x".join(map(str, v)) for k, v in tr.splits().items()}
     tr.set_stream(stream)

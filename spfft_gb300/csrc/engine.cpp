@@ -224,7 +224,9 @@ GpuPlan<T>::GpuPlan(const IndexPlan& p, int device) {
         fastZ_ = true;
         fastSpb_ = spb;
       }
-      for (int cand : {32, 24, 16, 12, 8}) {
+      // autotuner candidates: also 6 sticks, which with three z blocks per SM (the three-pass
+      // double-float z kernels) spreads a few thousand sticks over more than one wave
+      for (int cand : {32, 24, 16, 12, 8, 6}) {
         a.param = cand;
         fast_dispatch<T>(FastOp::ZSmem, nz, false, a);
         if (sm <= optin) zCands_.push_back(cand);
@@ -833,8 +835,9 @@ float GpuPlan<T>::autotune(T* values, T* space, void* scratch, cudaStream_t stre
   float bestMs = 0.0f;
   try {
     bestMs = time_pair(best);
-    // z shapes with the current plane strategy, then plane strategies with the best z shape
-    for (int pass = 0; pass < 2; ++pass) {
+    // pass 0: z shapes with the current plane strategy; pass 1: plane strategies with the best z
+    // shape (the split choices carry over where the candidate keeps the pass on the same kernels)
+    auto descend = [&](int pass) {
       const Tuning base = best;
       for (Tuning c : candidates()) {
         const bool zOnly = c.path == base.path && c.fusedRows == base.fusedRows &&
@@ -842,6 +845,7 @@ float GpuPlan<T>::autotune(T* values, T* space, void* scratch, cudaStream_t stre
                            c.rpbB == base.rpbB;
         const bool planeOnly = c.spb == base.spb;
         if ((pass == 0 && !zOnly) || (pass == 1 && !planeOnly)) continue;
+        if (pass == 0 && c.spb == base.spb) continue;
         for (int d = 0; d < 3; ++d) c.radix[d] = base.radix[d];
         for (int i = 0; i < 4; ++i) c.split[i] = (i < 2 ? c.spb > 0 : c.path == 2) ? base.split[i] : 0;
         const float ms = time_pair(c);
@@ -850,7 +854,9 @@ float GpuPlan<T>::autotune(T* values, T* space, void* scratch, cudaStream_t stre
           best = c;
         }
       }
-    }
+    };
+    descend(0);
+    descend(1);
     // the split of each specialised z and split-y pass: the default order, the swapped order or
     // three passes
     for (int i = 0; i < 4; ++i) {
@@ -867,6 +873,8 @@ float GpuPlan<T>::autotune(T* values, T* space, void* scratch, cudaStream_t stre
         }
       }
     }
+    // z shapes again with the chosen splits (a three-pass z kernel fits more blocks per SM)
+    descend(0);
     // radix plans of the lengths the generic kernels transform: z without specialised z kernels,
     // y and x on the generic plane path
     const bool generic[3] = {best.spb == 0, best.path == 0, best.path == 0};
