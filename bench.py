@@ -328,29 +328,33 @@ def load_traffic_table() -> dict:
 
 def load_instruction_table() -> dict:
     """Warp instructions per launch measured by ncu (smsp__inst_executed.sum,
-    profiles/instructions.txt), keyed by (kernel, workload, dtype)."""
+    profiles/instructions.txt), keyed by (kernel, workload, dtype, split): the split is the
+    kernel's radix split ("12x16", "12x4x4", ...)."""
     f = ROOT / "profiles" / "instructions.txt"
     out = {}
     if f.exists():
         for line in f.read_text().splitlines():
             parts = line.split()
-            if len(parts) >= 4 and not line.startswith("#"):
-                out[(parts[0], parts[1], parts[2])] = float(parts[3])
+            if len(parts) >= 5 and not line.startswith("#"):
+                out[(parts[0], parts[1], parts[2], parts[3])] = float(parts[4])
     return out
 
 
-def issue_fractions(kern_ms: dict, workload: str, dtype: str, sm_mhz: float | None) -> dict:
-    """Instruction-issue roofline per kernel: its warp instructions (ncu count per launch) over the
-    issue slots of its CUDA-event time, 152 SMs x 4 schedulers x one instruction per clock at the
-    SM clock sampled during the timed region (the maximum clock when no sample exists)."""
+def issue_fractions(kern_ms: dict, workload: str, dtype: str, sm_mhz: float | None,
+                    splits: dict | None = None) -> dict:
+    """Instruction-issue roofline per kernel: its warp instructions (ncu count per launch, for the
+    split the kernel ran with) over the issue slots of its CUDA-event time, 152 SMs x 4 schedulers
+    x one instruction per clock at the SM clock sampled during the timed region (the maximum clock
+    when no sample exists)."""
     table = load_instruction_table()
     mhz = sm_mhz or 2070.0
     out = {}
     for k, ms in kern_ms.items():
-        inst = table.get((k, workload, dtype))
+        split = (splits or {}).get(k)
+        inst = table.get((k, workload, dtype, split)) if split else None
         if inst and ms > 0:
             slots = 152 * 4 * mhz * 1e6 * ms * 1e-3
-            out[k] = {"warp_instructions": int(inst), "issue_frac": round(inst / slots, 4)}
+            out[k] = {"split": split, "warp_instructions": int(inst), "issue_frac": round(inst / slots, 4)}
     return {"sm_mhz": mhz, "kernels": out,
             "source": "profiles/instructions.txt (ncu smsp__inst_executed.sum per launch)"} if out else {}
 
@@ -490,7 +494,9 @@ def measure_gpu(args, rank: int, world: int) -> dict:
                 "traffic": traffic, "algorithmic_bytes": ab["kernels"][dominant],
                 "kernel_ms": {k: round(v, 4) for k, v in kern_ms.items()},
                 "kernel_gbs": {k: round(ab["kernels"][k] / (v * 1e-3) / 1e9, 1) for k, v in kern_ms.items()},
-                "issue": issue_fractions(kern_ms, args.workload, dtype, clocks.summary().get("sm_mhz")),
+                "issue": issue_fractions(kern_ms, args.workload, dtype, clocks.summary().get("sm_mhz"),
+                                         {k: None if v is None else "x".join(map(str, v))
+                                          for k, v in tr.splits().items()}),
                 "limiter": ("instruction issue: FP64 runs as double-float arithmetic on the FP32 pipes "
                             "(GB300's FP64 pipe is 57x slower), so the HBM fraction is not reachable"
                             if dtype == "float64" else "latency of a single small transform")}

@@ -625,8 +625,22 @@ struct PlaneLayout {
   static constexpr int Bx = Shape<LX>::B, Ax = Shape<LX>::A;
   static constexpr int PAD = (Bx % 2 == 0 && Bx > 1) ? 1 : 0;
   static constexpr int ROW = LX + PAD * Ax;
-  static constexpr int WP = ROW + ((Bx % 16) - ROW % 16 + 16) % 16;
+  // For LX = 12 x 8 (the x pass of 192 R2C and 96 C2C) pass 2 also conflicts at that pitch (a
+  // half-warp of its work items spans two rows whose slots meet); a pitch of 12 (mod 16) keeps pass
+  // 2 free of conflicts and, with the rows of pass 1 taken as 0, 2, 1, 3 within each group of four
+  // (pass1_row), pass 1 too. Modelled shared-memory wavefronts of a pass-1 + pass-2 row chunk: 432
+  // -> 288 for 8-byte and 224 -> 192 for 16-byte elements; every other shape is at its minimum
+  // with the rule above.
+  static constexpr bool kPermute1 = Ax == 12 && Bx == 8;
+  static constexpr int WP = kPermute1 ? ROW + (12 - ROW % 16 + 16) % 16 : ROW + ((Bx % 16) - ROW % 16 + 16) % 16;
   __host__ __device__ static constexpr int wpos(int e) { return e + PAD * (e / Bx); }
+  // Row (of the nr rows of a chunk) of pass-1 work-item row q: q itself, or 0, 2, 1, 3 within each
+  // complete group of four rows for the permuted layout.
+  __host__ __device__ static int pass1_row(int q, int nr) {
+    if (!kPermute1) return q;
+    const int g = q & ~3;
+    return g + 3 < nr ? g + (((q & 1) << 1) | ((q & 2) >> 1)) : q;
+  }
   template <typename CA>
   static size_t bytes(int numColumns, int rows) {
     const size_t c = sizeof(CA);
@@ -794,7 +808,7 @@ __device__ __forceinline__ void plane_backward_body(const PlanView<S>& p, S* __r
       rg.sync();
     }
     for (int i = rg.t; i < nr * Bx; i += rg.threads) {
-      const int rl = i / Bx, b = i - rl * Bx;
+      const int q = i / Bx, b = i - q * Bx, rl = L::pass1_row(q, nr);
       const CA* prow = s.P + transposed_pos<NY, 1>(r0 + rl) * nc;
       CA* wrow = W + rl * L::WP;
       CA v[Ax];
@@ -940,7 +954,7 @@ __device__ __forceinline__ void plane_forward_body(const PlanView<S>& p, const S
       rg.sync();
     }
     for (int i = rg.t; i < nr * Bx; i += rg.threads) {
-      const int rl = i / Bx, b = i - rl * Bx;
+      const int q = i / Bx, b = i - q * Bx, rl = L::pass1_row(q, nr);
       // padded row: element a*Bx + b sits at a*(Bx + PAD) + b (raw storage values until here)
       CA* wrow = wbase + rl * L::WP;
       CA v[Ax];
@@ -1522,7 +1536,7 @@ __device__ __forceinline__ void x_backward_body(const PlanView<S>& p, S* __restr
     __syncthreads();
   }
   for (int i = threadIdx.x; i < nr * Bx; i += blockDim.x) {
-    const int rl = i / Bx, b = i - rl * Bx;
+    const int q = i / Bx, b = i - q * Bx, rl = L::pass1_row(q, nr);
     const CA* prow = s.P + rl * nc;
     CA* wrow = s.W + rl * L::WP;
     CA v[Ax];
@@ -1633,7 +1647,7 @@ __device__ __forceinline__ void x_forward_body(const PlanView<S>& p, const S* __
   }
   const CA* twl = R2C ? s.twm : s.twx;
   for (int i = threadIdx.x; i < nr * Bx; i += blockDim.x) {
-    const int rl = i / Bx, b = i - rl * Bx;
+    const int q = i / Bx, b = i - q * Bx, rl = L::pass1_row(q, nr);
     CA* wrow = s.W + rl * L::WP;
     CA v[Ax];
 #pragma unroll
