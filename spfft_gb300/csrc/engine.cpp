@@ -231,6 +231,11 @@ GpuPlan<T>::GpuPlan(const IndexPlan& p, int device) {
         fast_dispatch<T>(FastOp::ZSmem, nz, false, a);
         if (sm <= optin) zCands_.push_back(cand);
       }
+      // SPFFT_GB300_Z_STICKS=n: sticks per z block, where n is one of the candidates
+      if (const char* zs = std::getenv("SPFFT_GB300_Z_STICKS")) {
+        const int want = std::atoi(zs);
+        if (fastZ_ && std::find(zCands_.begin(), zCands_.end(), want) != zCands_.end()) fastSpb_ = want;
+      }
     }
     const bool r2c = p.type == SPFFT_TRANS_R2C;
     // Candidate plane strategies. SPFFT_GB300_PLANE=fused|split|generic forces one (when it is
