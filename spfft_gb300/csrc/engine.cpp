@@ -863,23 +863,27 @@ float GpuPlan<T>::autotune(T* values, T* space, void* scratch, cudaStream_t stre
     descend(0);
     descend(1);
     // the split of each specialised z and split-y pass: the default order, the swapped order or
-    // three passes
+    // three passes; for the z passes jointly with the sticks per z block (a three-pass z kernel
+    // fits more blocks per SM, so its best block shape differs)
     for (int i = 0; i < 4; ++i) {
       if (i < 2 ? best.spb == 0 : best.path != 2) continue;
-      const int current = best.split[i];
+      const Tuning base = best;
+      const std::vector<int> shapes = i < 2 ? zCands_ : std::vector<int>{base.spb};
       for (int v = 0; v < 3; ++v) {
-        if (v == current || !split_valid(i, v, true)) continue;
-        Tuning c = best;
-        c.split[i] = v;
-        const float ms = time_pair(c);
-        if (ms < bestMs) {
-          bestMs = ms;
-          best = c;
+        if (!split_valid(i, v, true)) continue;
+        for (int spb : shapes) {
+          if (v == base.split[i] && spb == base.spb) continue;
+          Tuning c = best;
+          c.split[i] = v;
+          c.spb = spb;
+          const float ms = time_pair(c);
+          if (ms < bestMs) {
+            bestMs = ms;
+            best = c;
+          }
         }
       }
     }
-    // z shapes again with the chosen splits (a three-pass z kernel fits more blocks per SM)
-    descend(0);
     // radix plans of the lengths the generic kernels transform: z without specialised z kernels,
     // y and x on the generic plane path
     const bool generic[3] = {best.spb == 0, best.path == 0, best.path == 0};

@@ -645,21 +645,26 @@ struct PlaneLayout {
   static size_t bytes(int numColumns, int rows) {
     const size_t c = sizeof(CA);
     size_t b = round16((NY + NX + (R2C ? M : 0)) * c);
-    b += col_table_bytes();
+    b += col_table_bytes<CA>();
     b += static_cast<size_t>(NY) * numColumns * c;
     b += 2 * static_cast<size_t>(rows) * WP * c;
     return b;
   }
-  // colOf[NXF] (int, padded to 16 bytes), colInfo[NXF] (int4), colExp[NXF] (int, padded). The tables start on a 16-byte
-  // boundary (the twiddle tables before them are padded to one), so colInfo and the buffers after
-  // it are 16-byte aligned for every length (20 * N bytes of FP32 twiddles are not, for N = 90).
+  // colOf[NXF] (int), colSlots[NXF] (int), colTw[NXF] (complex), colExp[NXF] (int), each padded to
+  // 16 bytes. The tables start on a 16-byte boundary (the twiddle tables before them are padded to
+  // one), so every table and the buffers after them are 16-byte aligned for every length (20 * N
+  // bytes of FP32 twiddles are not, for N = 90).
   __host__ __device__ static constexpr size_t round16(size_t b) { return (b + 15) / 16 * 16; }
+  template <typename CA>
   __host__ __device__ static constexpr size_t col_table_bytes() {
-    return round16(NXF * sizeof(int)) + NXF * 16 + round16(NXF * sizeof(int));
+    return 3 * round16(NXF * sizeof(int)) + round16(NXF * sizeof(CA));
   }
-  // R2C forward: W slots of Z[k] and Z[M-k] for the output column with x = k, and k itself
-  __host__ __device__ static int4 col_info(int kk) {
-    return make_int4(wpos(transposed_pos<LX>(kk % M)), wpos(transposed_pos<LX>((M - kk) % M)), kk, 0);
+  // R2C forward, per output column with x = k: the W slots of Z[k] (low 16 bits) and Z[M-k] (high
+  // 16 bits) in one int, and the column's twiddle e^{-2 pi i k/N} beside it (colTw), so that an
+  // unpacking work item reads 4 + sizeof(complex) bytes of tables instead of an int4 and a
+  // dependent twiddle.
+  __host__ __device__ static int col_slots(int kk) {
+    return wpos(transposed_pos<LX>(kk % M)) | (wpos(transposed_pos<LX>((M - kk) % M)) << 16);
   }
 };
 
@@ -670,7 +675,8 @@ struct PlaneSmem {
   CA* twx;
   CA* twm;
   int* colOf;
-  int4* colInfo;
+  int* colSlots;
+  CA* colTw;
   CA* P;
   CA* W;
   __device__ __forceinline__ explicit PlaneSmem(int numColumns) {
@@ -678,8 +684,9 @@ struct PlaneSmem {
     twx = twy + NY;
     twm = twx + NX;
     colOf = reinterpret_cast<int*>(g_fast_smem + L::round16((NY + NX + (R2C ? L::M : 0)) * sizeof(CA)));
-    colInfo = reinterpret_cast<int4*>(reinterpret_cast<unsigned char*>(colOf) + L::round16(L::NXF * sizeof(int)));
-    P = reinterpret_cast<CA*>(reinterpret_cast<unsigned char*>(colOf) + L::col_table_bytes());
+    colSlots = reinterpret_cast<int*>(reinterpret_cast<unsigned char*>(colOf) + L::round16(L::NXF * sizeof(int)));
+    colTw = reinterpret_cast<CA*>(reinterpret_cast<unsigned char*>(colSlots) + L::round16(L::NXF * sizeof(int)));
+    P = reinterpret_cast<CA*>(reinterpret_cast<unsigned char*>(colOf) + L::template col_table_bytes<CA>());
     W = P + NY * numColumns;
   }
 };
@@ -700,7 +707,10 @@ __device__ __forceinline__ void plane_load_tables(const PlanView<S>& p,
   for (int c = threadIdx.x; c < p.numColumns; c += blockDim.x) {
     const int kk = p.columnX[c];
     s.colOf[kk] = c;
-    if (R2C) s.colInfo[c] = L::col_info(kk);
+    if (R2C) {
+      s.colSlots[c] = L::col_slots(kk);
+      s.colTw[c] = tw_arith(reinterpret_cast<const CS*>(p.twx)[kk]);
+    }
   }
 }
 
@@ -990,13 +1000,14 @@ __device__ __forceinline__ void plane_forward_body(const PlanView<S>& p, const S
       // X[k] = (Z[k] + conj Z[M-k]) / 2 - i/2 e^{-2 pi i k/N} (Z[k] - conj Z[M-k]), Z[M] = Z[0]
       for (int i = rg.t; i < nr * nc; i += rg.threads) {
         const int rl = dnc.div(i), c = i - rl * nc;
-        const int4 ci = s.colInfo[c];
+        const int sl = s.colSlots[c];
+        const CA tw = s.colTw[c];
         const CA* wrow = wbase + rl * L::WP;
-        const CA zk = wrow[ci.x];
-        const CA zm = wrow[ci.y];
+        const CA zk = wrow[sl & 0xffff];
+        const CA zm = wrow[sl >> 16];
         const CA zmc = cconj(zm);
         const CA dif = csub(zk, zmc);  // (zk.x - zm.x, zk.y + zm.y)
-        const CA u = cmul(dif, s.twx[ci.z]);
+        const CA u = cmul(dif, tw);
         s.P[(r0 + rl) * nc + c] = chalf(csub(cadd(zk, zmc), cmul_i<1>(u)));
       }
       rg.sync();
@@ -1445,7 +1456,8 @@ struct RowSmem {
   CA* twx;
   CA* twm;
   int* colOf;
-  int4* colInfo;
+  int* colSlots;
+  CA* colTw;
   int* colExp;
   CA* P;
   CA* W;
@@ -1455,15 +1467,16 @@ struct RowSmem {
     twx = reinterpret_cast<CA*>(g_fast_smem);
     twm = twx + NX;
     colOf = reinterpret_cast<int*>(g_fast_smem + L::round16((NX + (R2C ? L::M : 0)) * sizeof(CA)));
-    colInfo = reinterpret_cast<int4*>(reinterpret_cast<unsigned char*>(colOf) + L::round16(L::NXF * sizeof(int)));
-    colExp = reinterpret_cast<int*>(colInfo + L::NXF);
-    P = reinterpret_cast<CA*>(reinterpret_cast<unsigned char*>(colOf) + L::col_table_bytes());
+    colSlots = reinterpret_cast<int*>(reinterpret_cast<unsigned char*>(colOf) + L::round16(L::NXF * sizeof(int)));
+    colTw = reinterpret_cast<CA*>(reinterpret_cast<unsigned char*>(colSlots) + L::round16(L::NXF * sizeof(int)));
+    colExp = reinterpret_cast<int*>(reinterpret_cast<unsigned char*>(colTw) + L::round16(L::NXF * sizeof(CA)));
+    P = reinterpret_cast<CA*>(reinterpret_cast<unsigned char*>(colOf) + L::template col_table_bytes<CA>());
     W = P + (withP ? rows * numColumns : 0);
   }
   template <typename CAT>
   static size_t bytes(int numColumns, int rows, bool withP = true) {
     const size_t c = sizeof(CAT);
-    return L::round16((NX + (R2C ? L::M : 0)) * c) + L::col_table_bytes() +
+    return L::round16((NX + (R2C ? L::M : 0)) * c) + L::template col_table_bytes<CAT>() +
            (withP ? static_cast<size_t>(rows) * numColumns * c : 0) + static_cast<size_t>(rows) * L::WP * c;
   }
 };
@@ -1482,7 +1495,10 @@ __device__ __forceinline__ void row_load_tables(const PlanView<S>& p, RowSmem<ty
   for (int c = threadIdx.x; c < p.numColumns; c += blockDim.x) {
     const int kk = p.columnX[c];
     s.colOf[kk] = c;
-    if (R2C) s.colInfo[c] = L::col_info(kk);
+    if (R2C) {
+      s.colSlots[c] = L::col_slots(kk);
+      s.colTw[c] = tw_arith(reinterpret_cast<const CS*>(p.twx)[kk]);
+    }
   }
 }
 
@@ -1686,13 +1702,14 @@ __device__ __forceinline__ void x_forward_body(const PlanView<S>& p, const S* __
     with_store(k, [&](auto conv) {
       for (int i = threadIdx.x; i < nr * nc; i += blockDim.x) {
         const int rl = dnc.div(i), c = i - rl * nc;
-        const int4 ci = s.colInfo[c];
+        const int sl = s.colSlots[c];
+        const CA tw = s.colTw[c];
         const CA* wrow = s.W + rl * L::WP;
-        const CA zk = wrow[ci.x];
-        const CA zm = wrow[ci.y];
+        const CA zk = wrow[sl & 0xffff];
+        const CA zm = wrow[sl >> 16];
         const CA zmc = cconj(zm);
         const CA dif = csub(zk, zmc);  // (zk.x - zm.x, zk.y + zm.y)
-        const CA u = cmul(dif, s.twx[ci.z]);
+        const CA u = cmul(dif, tw);
         const CA xv = chalf(csub(cadd(zk, zmc), cmul_i<1>(u)));
         if (raw) rawPlanes[i] = xv;
         else planes[i] = conv(xv, k);
