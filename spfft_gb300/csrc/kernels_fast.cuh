@@ -77,6 +77,19 @@ template <>
 struct BatchPlaneThreads<dd> {
   static constexpr int value = batch_plane_threads<double>();
 };
+// Threads of a split x backward block. The double-float R2C kernel (72 registers) is held to two
+// blocks per SM by its shared memory (compact rows and FFT rows of 32 rows), not by registers, so
+// its blocks take 384 threads: 24 warps per SM instead of 16, and pass 2 (12 work items per row of
+// the 12 x 8 split of 192) fills the block. The C2C kernel (about 100 registers) would fit only one
+// such block per SM and keeps 256.
+template <typename A, bool R2C>
+struct XBackwardThreads {
+  static constexpr int value = kThreads;
+};
+template <>
+struct XBackwardThreads<dd, true> {
+  static constexpr int value = 384;
+};
 
 extern __shared__ __align__(16) unsigned char g_fast_smem[];
 
@@ -1599,7 +1612,7 @@ __device__ __forceinline__ void x_backward_body(const PlanView<S>& p, S* __restr
 
 // Planes z0 + blockIdx.y (z0 > 0 when a plane range is transformed on its own).
 template <typename S, typename A, int NX, bool R2C>
-__global__ void __launch_bounds__(kThreads) x_backward_split(const PlanView<S> p, S* __restrict__ space,
+__global__ void __launch_bounds__(XBackwardThreads<A, R2C>::value) x_backward_split(const PlanView<S> p, S* __restrict__ space,
                                                              int rpb, int z0) {
   __shared__ int sExp[2];
   x_backward_body<S, A, NX, R2C>(p, space, rpb, blockIdx.x, z0 + blockIdx.y, sExp);
@@ -1794,7 +1807,8 @@ struct XSplitKernels {
   // planes [z0, z0 + nz) (nz < 0: all planes from z0)
   static void backward(const PlanView<S>& p, int rpb, S* space, cudaStream_t st, int z0, int nz) {
     const dim3 g((p.dimY + rpb - 1) / rpb, nz < 0 ? p.dimZ - z0 : nz);
-    launch_pdl(x_backward_split<S, A, NX, R2C>, g, kThreads, smem(p.numColumns, rpb), st, p, space, rpb, z0);
+    launch_pdl(x_backward_split<S, A, NX, R2C>, g, XBackwardThreads<A, R2C>::value, smem(p.numColumns, rpb), st, p, space, rpb,
+               z0);
   }
   static void forward(const PlanView<S>& p, int rpb, const S* space, cudaStream_t st, int z0, int nz) {
     const dim3 g((p.dimY + rpb - 1) / rpb, nz < 0 ? p.dimZ - z0 : nz);
