@@ -507,6 +507,33 @@ def test_every_specialised_length(lib, dtype):
 
 
 @pytest.mark.parametrize("dtype", ["float64", "float32"])
+@pytest.mark.parametrize("xb_rows", ["32", "24"])
+def test_x_chunk_layout_partial_row_groups(lib, dtype, xb_rows, monkeypatch):
+    """The x-pass chunk layout of 12 x 8 rows (the x pass of 192 R2C and 96 C2C) takes pass-1 rows
+    as 0, 2, 1, 3 within each complete group of four and in order in a last incomplete group: y
+    lengths that leave chunks of 26, 22 and 18 rows on the split plane passes match the oracle."""
+    monkeypatch.setenv("SPFFT_GB300_PLANE", "split")
+    monkeypatch.setenv("SPFFT_GB300_XB_ROWS", xb_rows)
+    rng = np.random.default_rng(47)
+    for dims, ttype in [((192, 90, 48), 1), ((96, 150, 48), 0)]:
+        idx = random_indices(rng, *dims, r2c=ttype == 1, stick_frac=0.4, fill_frac=0.5)
+        tr = _transform(dtype, ttype, dims, idx)
+        assert tr.path_info()["split_plane"], dims
+        assert tr.tuning()["rows_per_x_backward_block"] == int(xb_rows)
+        vals = _values(rng, len(idx))
+        oracle = pipeline.HostPipeline(ttype, *dims, idx)
+        st = CT[dtype] if ttype == 0 else RT[dtype]
+        out = torch.empty(dims[::-1], dtype=st, device="cuda")
+        tr.backward(torch.from_numpy(vals).to(CT[dtype]).cuda(), out)
+        space = out.cpu().numpy()
+        assert rel_l2(space, oracle.backward(vals)) <= TOL[dtype], (dims, xb_rows)
+        f = torch.empty(len(idx), dtype=CT[dtype], device="cuda")
+        tr.forward(out, f, sp.SPFFT_FULL_SCALING)
+        want_f = oracle.forward(space.astype(np.complex128 if ttype == 0 else np.float64), scaled=True)
+        assert rel_l2(f.cpu().numpy(), want_f) <= TOL[dtype], (dims, xb_rows)
+
+
+@pytest.mark.parametrize("dtype", ["float64", "float32"])
 def test_autotune_keeps_results(lib, dtype):
     """The autotuner picks one of the valid tile shapes and plane strategies; results after tuning
     still match the oracle."""
