@@ -526,6 +526,8 @@ __device__ __forceinline__ void z_forward_body(const PlanView<S>& p, S* __restri
   const FastDiv dns(nsb);
 
   load_twiddles<S, A>(tw, p.twz, NZ);
+  // the block's value range (a plan table, read before the wait for the previous kernel)
+  const int e0 = p.stickEntryStart[s0], e1 = p.stickEntryStart[s0 + nsb];
   pdl_wait();
   pdl_trigger();
   const CS* sticks = reinterpret_cast<const CS*>(p.sticks) + s0;
@@ -595,21 +597,32 @@ __device__ __forceinline__ void z_forward_body(const PlanView<S>& p, S* __restri
   }
   __syncthreads();
   CS* out = reinterpret_cast<CS*>(values);
-  const int e0 = p.stickEntryStart[s0], e1 = p.stickEntryStart[s0 + nsb];
   const int base = s0 * NZ;
   const bool converted = TT::kScaled && exact_block(k);
   if (converted) {
     convert_exact_in_place<S, A>(buf, nsb * PZ, k, threadIdx.x, blockDim.x);
     __syncthreads();
   }
-  for (int e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
-    const int pos = p.entryPos[e] - base;
-    const int sl = pos / NZ;
-    CS v = stored_value<S, A>(buf + sl * PZ + transposed_pos<NZ, V>(pos - sl * NZ), k, converted);
-    // scaling multiplies by S(1 / (Nx Ny Nz)) in S, like compress_kernel_scaled
-    // (compression_kernels.cu:106-128)
-    if (scale != S(0)) v = cscale(v, scale);
-    out[p.entryUser[e]] = v;
+  // Index loads four at a time (their latencies overlap), then the gathers and stores.
+  for (int e = e0 + threadIdx.x; e < e1; e += 4 * blockDim.x) {
+    int pos[4], usr[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int eu = e + u * blockDim.x;
+      pos[u] = eu < e1 ? p.entryPos[eu] - base : -1;
+      usr[u] = eu < e1 ? p.entryUser[eu] : 0;
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      if (pos[u] >= 0) {
+        const int sl = pos[u] / NZ;
+        CS v = stored_value<S, A>(buf + sl * PZ + transposed_pos<NZ, V>(pos[u] - sl * NZ), k, converted);
+        // scaling multiplies by S(1 / (Nx Ny Nz)) in S, like compress_kernel_scaled
+        // (compression_kernels.cu:106-128)
+        if (scale != S(0)) v = cscale(v, scale);
+        out[usr[u]] = v;
+      }
+    }
   }
 }
 
