@@ -472,6 +472,32 @@ def test_pinned_host_buffers(lib, access, dtype, monkeypatch):
             assert rel_l2(buf.numpy(), want) <= TOL[dtype]
 
 
+@pytest.mark.parametrize("access", ["direct", "copy"])
+def test_pinned_host_buffers_three_pass(lib, access, monkeypatch):
+    """Pinned host buffers on the split plane passes with the three-pass z and y splits: the
+    staged paths run the y and x passes plane chunk by plane chunk (while the space domain crosses
+    the host link), so the three-pass y kernels run on plane ranges; same results as the oracle."""
+    monkeypatch.setenv("SPFFT_GB300_HOST_ACCESS", access)
+    monkeypatch.setenv("SPFFT_GB300_PLANE", "split")
+    monkeypatch.setenv("SPFFT_GB300_SPLITS", "2,2,2,2")
+    rng = np.random.default_rng(53)
+    for dims, ttype in [((48, 144, 144), 1), ((48, 192, 192), 0)]:
+        idx = random_indices(rng, *dims, r2c=ttype == 1, stick_frac=0.2, fill_frac=0.4)
+        tr = _transform("float64", ttype, dims, idx)
+        assert tr.path_info()["split_plane"]
+        assert len(tr.splits()["y_backward"]) == 3 and len(tr.splits()["z_forward"]) == 3, tr.splits()
+        oracle = pipeline.HostPipeline(ttype, *dims, idx)
+        vals = _values(rng, len(idx))
+        hv = torch.from_numpy(vals).pin_memory()
+        hs = torch.empty(dims[::-1], dtype=torch.complex128 if ttype == 0 else torch.float64).pin_memory()
+        tr.backward(hv, hs)
+        assert rel_l2(hs.numpy(), oracle.backward(vals)) <= TOL["float64"], (dims, access)
+        hf = torch.empty_like(hv)
+        tr.forward(hs, hf, sp.SPFFT_FULL_SCALING)
+        want_f = oracle.forward(hs.numpy().astype(np.complex128 if ttype == 0 else np.float64), scaled=True)
+        assert rel_l2(hf.numpy(), want_f) <= TOL["float64"], (dims, access)
+
+
 @pytest.mark.parametrize("dtype", ["float64", "float32"])
 def test_every_specialised_length(lib, dtype):
     """Every length with size-specialised kernels, C2C and R2C, single transforms and one batch
