@@ -239,6 +239,29 @@ __host__ __device__ __forceinline__ int transposed_pos(int k) {
     return (k % A) * B + k / A;
   }
 }
+// Rotated in-place outputs of the two-pass variants: pass-2 work item k1 stores X[k1 + A k2] at
+// k1 B + (k2 + k1 mod B) mod B, still inside its own B slots. Unrotated, the outputs of consecutive
+// k1 sit B slots apart, all in one shared-memory bank when B is a multiple of 16; rotated,
+// consecutive outputs fall in different banks, and a gather in output order (192 = 12 x 16, 8-byte
+// values) takes about 2 wavefronts per half-warp instead of 10. Variant 3 keeps transposed_pos
+// (its pass 2b items own B2 slots each, too few to rotate within).
+template <int N, int V = 0>
+__host__ __device__ __forceinline__ int rotated_slot(int k1, int k2) {
+  constexpr int A = Shape<N, V>::A, B = Shape<N, V>::B;
+  const int r = A <= B ? k1 : k1 % B;
+  const int q = k2 + r;
+  return k1 * B + (q >= B ? q - B : q);
+}
+template <int N, int V = 0>
+__host__ __device__ __forceinline__ int rotated_pos(int k) {
+  if constexpr (V == 3) {
+    return transposed_pos<N, V>(k);
+  } else {
+    constexpr int A = Shape<N, V>::A;
+    const int k2 = k / A;
+    return rotated_slot<N, V>(k - k2 * A, k2);
+  }
+}
 // Variant 3: the output index k of the value pass 2b leaves at in-place position e.
 template <int N>
 __host__ __device__ __forceinline__ int three_pass_index(int e) {
@@ -257,6 +280,25 @@ __host__ __device__ __forceinline__ void fft_pass1(C* buf, int stride, int b, co
   if (B > 1) {
 #pragma unroll
     for (int k1 = 1; k1 < A; ++k1) v[k1] = ctw<SIGN>(v[k1], tw[k1 * b]);
+  }
+#pragma unroll
+  for (int k1 = 0; k1 < A; ++k1) buf[(k1 * B + b) * stride] = v[k1];
+}
+
+// Pass 1 with its twiddles in pass-1 order, tw1[k1 * B + b] = w^(k1 b): the work items b of a
+// warp read consecutive entries (no bank conflicts; tw[k1 * b] puts b and b + 16 / gcd(k1, 16) in
+// one bank) at constant offsets from tw1 + b.
+template <int N, int SIGN, int V = 0, typename C>
+__host__ __device__ __forceinline__ void fft_pass1_ordered(C* buf, int stride, int b, const C* __restrict__ tw1) {
+  constexpr int A = Shape<N, V>::A, B = Shape<N, V>::B;
+  C v[A];
+#pragma unroll
+  for (int a = 0; a < A; ++a) v[a] = buf[(a * B + b) * stride];
+  Dft<A, SIGN>::run(v);
+  if (B > 1) {
+    const C* t = tw1 + b;
+#pragma unroll
+    for (int k1 = 1; k1 < A; ++k1) v[k1] = ctw<SIGN>(v[k1], t[k1 * B]);
   }
 #pragma unroll
   for (int k1 = 0; k1 < A; ++k1) buf[(k1 * B + b) * stride] = v[k1];

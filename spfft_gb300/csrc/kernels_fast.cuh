@@ -372,6 +372,21 @@ __device__ __forceinline__ void load_twiddles(typename Types<S, A>::CA* dst, con
 // ================================================================================================
 // z pass
 // ================================================================================================
+// The z twiddles in pass-1 order (tw1[k1 * B + b] = w^(k1 b)) and, for the three-pass split, in
+// power order as well (pass 2a reads w^(kk1 i2 A)).
+template <typename S, typename A, int NZ, int V>
+__device__ __forceinline__ void load_z_twiddles(typename Types<S, A>::CA* tw1, typename Types<S, A>::CA* tw,
+                                                const S* src) {
+  using CS = typename Types<S, A>::CS;
+  constexpr int Bz = Shape<NZ, V>::B;
+  const CS* s = reinterpret_cast<const CS*>(src);
+  for (int i = threadIdx.x; i < NZ; i += blockDim.x) {
+    const int k1 = i / Bz;
+    tw1[i] = tw_arith(s[k1 * (i - k1 * Bz)]);
+    if constexpr (V == 3) tw[i] = tw_arith(s[i]);
+  }
+}
+
 template <int NZ>
 struct ZLayout {
   static constexpr int pitch = NZ | 1;  // odd: conflict-free column access across sticks
@@ -388,13 +403,14 @@ __device__ __forceinline__ void z_backward_body(const PlanView<S>& p, const S* _
   using CA = typename TT::CA;
   constexpr int Az = Shape<NZ, V>::A, Bz = Shape<NZ, V>::B, PZ = ZLayout<NZ>::pitch;
   int& sExp = *sExpPtr;
-  CA* tw = reinterpret_cast<CA*>(g_fast_smem);
+  CA* tw1 = reinterpret_cast<CA*>(g_fast_smem);  // pass-1 order
+  CA* tw = tw1 + NZ;                              // power order (pass 2a of variant 3)
   CA* buf = tw + NZ;
   const int s0 = bx * spb;
   const int nsb = min(spb, p.numSticks - s0);
   const FastDiv dns(nsb);
 
-  load_twiddles<S, A>(tw, p.twz, NZ);
+  load_z_twiddles<S, A, NZ, V>(tw1, tw, p.twz);
   for (int i = threadIdx.x; i < nsb * PZ; i += blockDim.x) buf[i] = czero<A>();
   // The value map is a plan table (constant from plan creation on): the block's entry range and
   // this thread's first four entries are read before the wait for the previous kernel.
@@ -440,7 +456,7 @@ __device__ __forceinline__ void z_backward_body(const PlanView<S>& p, const S* _
 
   for (int i = threadIdx.x; i < nsb * Bz; i += blockDim.x) {
     const int sl = i / Bz, b = i - sl * Bz;
-    fft_pass1<NZ, +1, V>(buf + sl * PZ, 1, b, tw);
+    fft_pass1_ordered<NZ, +1, V>(buf + sl * PZ, 1, b, tw1);
   }
   __syncthreads();
   CS* sticks = reinterpret_cast<CS*>(p.sticks) + s0;
@@ -519,13 +535,14 @@ __device__ __forceinline__ void z_forward_body(const PlanView<S>& p, S* __restri
   using CA = typename TT::CA;
   constexpr int Az = Shape<NZ, V>::A, Bz = Shape<NZ, V>::B, PZ = ZLayout<NZ>::pitch;
   int& sExp = *sExpPtr;
-  CA* tw = reinterpret_cast<CA*>(g_fast_smem);
+  CA* tw1 = reinterpret_cast<CA*>(g_fast_smem);  // pass-1 order
+  CA* tw = tw1 + NZ;                              // power order (pass 2a of variant 3)
   CA* buf = tw + NZ;
   const int s0 = bx * spb;
   const int nsb = min(spb, p.numSticks - s0);
   const FastDiv dns(nsb);
 
-  load_twiddles<S, A>(tw, p.twz, NZ);
+  load_z_twiddles<S, A, NZ, V>(tw1, tw, p.twz);
   // the block's value range (a plan table, read before the wait for the previous kernel)
   const int e0 = p.stickEntryStart[s0], e1 = p.stickEntryStart[s0 + nsb];
   pdl_wait();
@@ -569,7 +586,7 @@ __device__ __forceinline__ void z_forward_body(const PlanView<S>& p, S* __restri
   }
   for (int i = threadIdx.x; i < nsb * Bz; i += blockDim.x) {
     const int sl = i / Bz, b = i - sl * Bz;
-    fft_pass1<NZ, -1, V>(buf + sl * PZ, 1, b, tw);
+    fft_pass1_ordered<NZ, -1, V>(buf + sl * PZ, 1, b, tw1);
   }
   __syncthreads();
   if constexpr (V == 3) {
@@ -592,7 +609,7 @@ __device__ __forceinline__ void z_forward_body(const PlanView<S>& p, S* __restri
       CA v[Bz];
       fft_pass2<NZ, -1, V>(buf + sl * PZ, 1, k1, v);
 #pragma unroll
-      for (int k2 = 0; k2 < Bz; ++k2) buf[sl * PZ + k1 * Bz + k2] = v[k2];
+      for (int k2 = 0; k2 < Bz; ++k2) buf[sl * PZ + rotated_slot<NZ, V>(k1, k2)] = v[k2];
     }
   }
   __syncthreads();
@@ -616,7 +633,7 @@ __device__ __forceinline__ void z_forward_body(const PlanView<S>& p, S* __restri
     for (int u = 0; u < 4; ++u) {
       if (pos[u] >= 0) {
         const int sl = pos[u] / NZ;
-        CS v = stored_value<S, A>(buf + sl * PZ + transposed_pos<NZ, V>(pos[u] - sl * NZ), k, converted);
+        CS v = stored_value<S, A>(buf + sl * PZ + rotated_pos<NZ, V>(pos[u] - sl * NZ), k, converted);
         // scaling multiplies by S(1 / (Nx Ny Nz)) in S, like compress_kernel_scaled
         // (compression_kernels.cu:106-128)
         if (scale != S(0)) v = cscale(v, scale);
@@ -1127,7 +1144,7 @@ constexpr bool has_three() {
 template <typename S, typename A, int NZ>
 struct ZKernels {
   using CA = typename Types<S, A>::CA;
-  static size_t smem(int spb) { return (NZ + static_cast<size_t>(spb) * ZLayout<NZ>::pitch) * sizeof(CA); }
+  static size_t smem(int spb) { return (2 * NZ + static_cast<size_t>(spb) * ZLayout<NZ>::pitch) * sizeof(CA); }
   static cudaError_t prepare(size_t maxSmem) {
     cudaError_t e1 = allow_dynamic_smem(z_backward<S, A, NZ>, maxSmem);
     cudaError_t e2 = allow_dynamic_smem(z_forward<S, A, NZ>, maxSmem);
