@@ -315,6 +315,19 @@ __host__ __device__ __forceinline__ void fft_pass1_regs(C (&v)[Shape<N, V>::A], 
   }
 }
 
+// fft_pass1_regs with the twiddles in pass-1 order (tw1[k1 * B + b] = w^(k1 b), as for
+// fft_pass1_ordered).
+template <int N, int SIGN, int V = 0, typename C>
+__host__ __device__ __forceinline__ void fft_pass1_regs_ordered(C (&v)[Shape<N, V>::A], int b, const C* __restrict__ tw1) {
+  constexpr int A = Shape<N, V>::A, B = Shape<N, V>::B;
+  Dft<A, SIGN>::run(v);
+  if (B > 1) {
+    const C* t = tw1 + b;
+#pragma unroll
+    for (int k1 = 1; k1 < A; ++k1) v[k1] = ctw<SIGN>(v[k1], t[k1 * B]);
+  }
+}
+
 template <int N, int SIGN, int V = 0, typename C>
 __host__ __device__ __forceinline__ void fft_pass2(const C* buf, int stride, int k1, C (&v)[Shape<N, V>::B]) {
   constexpr int B = Shape<N, V>::B;

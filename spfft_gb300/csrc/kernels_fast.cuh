@@ -734,17 +734,28 @@ struct PlaneSmem {
   }
 };
 
+// The twiddles of pass 1 of the x rows in pass-1 order: entry k1 * Bx + b = w_LX^(k1 b), with
+// LX = NX (C2C) or M = NX / 2 (R2C, w_M = w_NX^2). In C2C this is the only use of twx; the R2C
+// packing reads w_NX in power order from twx and pass 1 reads twm.
+template <typename S, typename A, int NX, bool R2C>
+__device__ __forceinline__ void load_x_pass1_twiddles(typename Types<S, A>::CA* dst, const S* src) {
+  using CS = typename Types<S, A>::CS;
+  constexpr int LX = R2C ? NX / 2 : NX, Bx = Shape<LX>::B, step = R2C ? 2 : 1;
+  const CS* tx = reinterpret_cast<const CS*>(src);
+  for (int i = threadIdx.x; i < LX; i += blockDim.x) {
+    const int k1 = i / Bx;
+    dst[i] = tw_arith(tx[step * k1 * (i - k1 * Bx)]);
+  }
+}
+
 template <typename S, typename A, int NX, int NY, bool R2C>
 __device__ __forceinline__ void plane_load_tables(const PlanView<S>& p,
                                                   PlaneSmem<typename Types<S, A>::CA, NX, NY, R2C>& s) {
   using L = PlaneLayout<NX, NY, R2C>;
   using CS = typename Types<S, A>::CS;
   load_twiddles<S, A>(s.twy, p.twy, NY);
-  load_twiddles<S, A>(s.twx, p.twx, NX);
-  if (R2C) {
-    const CS* tx = reinterpret_cast<const CS*>(p.twx);
-    for (int i = threadIdx.x; i < L::M; i += blockDim.x) s.twm[i] = tw_arith(tx[2 * i]);  // w_M = w_N^2
-  }
+  if (R2C) load_twiddles<S, A>(s.twx, p.twx, NX);
+  load_x_pass1_twiddles<S, A, NX, R2C>(R2C ? s.twm : s.twx, p.twx);
   for (int i = threadIdx.x; i < L::NXF; i += blockDim.x) s.colOf[i] = -1;
   __syncthreads();
   for (int c = threadIdx.x; c < p.numColumns; c += blockDim.x) {
@@ -875,7 +886,7 @@ __device__ __forceinline__ void plane_backward_body(const PlanView<S>& p, S* __r
           v[a] = wrow[a * (Bx + L::PAD) + b];  // L::wpos(kk), b < Bx
         }
       }
-      fft_pass1_regs<L::LX, +1>(v, b, twl);
+      fft_pass1_regs_ordered<L::LX, +1>(v, b, twl);
 #pragma unroll
       for (int k1 = 0; k1 < Ax; ++k1) wrow[k1 * (Bx + L::PAD) + b] = v[k1];  // L::wpos(k1 * Bx + b)
     }
@@ -1016,7 +1027,7 @@ __device__ __forceinline__ void plane_forward_body(const PlanView<S>& p, const S
         const int slot = a * (Bx + L::PAD) + b;
         v[a] = pre ? wrow[slot] : to_arith(reinterpret_cast<const CS*>(wrow)[slot], k);
       }
-      fft_pass1_regs<L::LX, -1>(v, b, twl);
+      fft_pass1_regs_ordered<L::LX, -1>(v, b, twl);
 #pragma unroll
       for (int k1 = 0; k1 < Ax; ++k1) wrow[k1 * (Bx + L::PAD) + b] = v[k1];
     }
@@ -1528,11 +1539,8 @@ template <typename S, typename A, int NX, bool R2C>
 __device__ __forceinline__ void row_load_tables(const PlanView<S>& p, RowSmem<typename Types<S, A>::CA, NX, R2C>& s) {
   using L = PlaneLayout<NX, 2, R2C>;
   using CS = typename Types<S, A>::CS;
-  load_twiddles<S, A>(s.twx, p.twx, NX);
-  if (R2C) {
-    const CS* tx = reinterpret_cast<const CS*>(p.twx);
-    for (int i = threadIdx.x; i < L::M; i += blockDim.x) s.twm[i] = tw_arith(tx[2 * i]);
-  }
+  if (R2C) load_twiddles<S, A>(s.twx, p.twx, NX);
+  load_x_pass1_twiddles<S, A, NX, R2C>(R2C ? s.twm : s.twx, p.twx);
   for (int i = threadIdx.x; i < L::NXF; i += blockDim.x) s.colOf[i] = -1;
   __syncthreads();
   for (int c = threadIdx.x; c < p.numColumns; c += blockDim.x) {
@@ -1609,7 +1617,7 @@ __device__ __forceinline__ void x_backward_body(const PlanView<S>& p, S* __restr
         v[a] = wrow[L::wpos(kk)];
       }
     }
-    fft_pass1_regs<L::LX, +1>(v, b, twl);
+    fft_pass1_regs_ordered<L::LX, +1>(v, b, twl);
 #pragma unroll
     for (int k1 = 0; k1 < Ax; ++k1) wrow[k1 * (Bx + L::PAD) + b] = v[k1];  // L::wpos(k1 * Bx + b)
   }
@@ -1714,7 +1722,7 @@ __device__ __forceinline__ void x_forward_body(const PlanView<S>& p, const S* __
       const int slot = a * (Bx + L::PAD) + b;
       v[a] = pre ? wrow[slot] : to_arith(reinterpret_cast<const CS*>(wrow)[slot], k);
     }
-    fft_pass1_regs<L::LX, -1>(v, b, twl);
+    fft_pass1_regs_ordered<L::LX, -1>(v, b, twl);
 #pragma unroll
     for (int k1 = 0; k1 < Ax; ++k1) wrow[k1 * (Bx + L::PAD) + b] = v[k1];
   }
