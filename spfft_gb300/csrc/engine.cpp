@@ -64,6 +64,28 @@ constexpr size_t kFastZBudget = 56 * 1024;
 
 inline int odd_pitch(int n) { return n % 2 == 0 ? n + 1 : n; }
 
+// Plane counts of the staged chunks in the backward's order. By default they double from about
+// nz / 24 planes (192: 8, 16, 32, 64, 72): the backward's pipeline fills over a short first chunk
+// (its y and x passes run before the first copy can start) and the forward, taking the chunks in
+// reverse, drains over a short last one (its passes and the z pass run after the last copy), while
+// every other chunk's passes, about a quarter of its copy time on the host link, hide under the
+// neighbouring chunk's copy; fewer chunks than equal ones of that first size also mean fewer copy
+// calls. `uniform` > 0 asks for that many equal chunks instead.
+std::vector<int> staged_chunk_sizes(int nz, int uniform) {
+  std::vector<int> sizes;
+  if (uniform > 0) {
+    const int per = (nz + uniform - 1) / uniform;
+    for (int z0 = 0; z0 < nz; z0 += per) sizes.push_back(std::min(per, nz - z0));
+    return sizes;
+  }
+  for (int size = std::max(1, (nz + 12) / 24), rem = nz; rem > 0; size *= 2) {
+    const int take = std::min(size, rem);
+    sizes.push_back(take);
+    rem -= take;
+  }
+  return sizes;
+}
+
 template <typename T>
 LaunchConfig choose_launch_config(const IndexPlan& p, int device) {
   const size_t c = 2 * sizeof(T);
@@ -419,10 +441,12 @@ GpuPlan<T>::GpuPlan(const IndexPlan& p, int device) {
   }
   numValues_ = nv;
 
+  int uniform = 0;
   if (const char* env = std::getenv("SPFFT_GB300_STAGED_CHUNKS")) {
     const int want = std::atoi(env);
-    if (want >= 1 && want <= kMaxStagedChunks) stagedChunks_ = want;
+    if (want >= 1 && want <= kMaxStagedChunks) uniform = want;
   }
+  stagedSizes_ = staged_chunk_sizes(p.dimZ, uniform);
 
   // Forward scaling factor T(1 / (Nx Ny Nz)) computed in double (execution_gpu.cpp:58-59).
   scale_ = static_cast<T>(1.0 / (static_cast<double>(p.dimX) * p.dimY * p.dimZ));
@@ -594,7 +618,7 @@ bool GpuPlan<T>::forward_staged(const T* hostSpace, T* devSpace, T* values, bool
   if (planePath_ != PlanePath::Split || !aligned) return false;
   const PlanView<T> v = view(scratch);
   const size_t plane = static_cast<size_t>(base_.dimX) * base_.dimY * (base_.r2c ? 1 : 2);
-  const int nz = base_.dimZ, per = (nz + stagedChunks_ - 1) / stagedChunks_;
+  const int nChunks = static_cast<int>(stagedSizes_.size());
   // the copies overwrite devSpace: start them after the work already on `stream`
   check_cuda(cudaEventRecord(events[kMaxStagedChunks], stream));
   check_cuda(cudaStreamWaitEvent(copyStream, events[kMaxStagedChunks], 0));
@@ -605,8 +629,9 @@ bool GpuPlan<T>::forward_staged(const T* hostSpace, T* devSpace, T* values, bool
   a.in = devSpace;
   // each chunk's x and y passes run while the next chunk is copied (the y-FFT of plane z needs
   // only plane z)
-  for (int c = 0, z0 = 0; z0 < nz; ++c, z0 += per) {
-    const int cnt = std::min(per, nz - z0);
+  // the chunks in decreasing size: the passes left after the last copy are the smallest chunk's
+  for (int c = 0, z0 = 0; c < nChunks; z0 += stagedSizes_[nChunks - 1 - c], ++c) {
+    const int cnt = stagedSizes_[nChunks - 1 - c];
     check_cuda(cudaMemcpyAsync(devSpace + z0 * plane, hostSpace + z0 * plane, cnt * plane * sizeof(T),
                                cudaMemcpyHostToDevice, copyStream));
     check_cuda(cudaEventRecord(events[c], copyStream));
@@ -657,11 +682,11 @@ bool GpuPlan<T>::backward_staged(const T* values, T* devSpace, T* hostSpace, voi
   }
   check_launch(cudaGetLastError());
   const size_t plane = static_cast<size_t>(base_.dimX) * base_.dimY * (base_.r2c ? 1 : 2);
-  const int nz = base_.dimZ, per = (nz + stagedChunks_ - 1) / stagedChunks_;
   a.out = devSpace;
-  // each chunk's y and x passes, then its copy back, which overlaps the next chunk's passes
-  for (int c = 0, z0 = 0; z0 < nz; ++c, z0 += per) {
-    const int cnt = std::min(per, nz - z0);
+  // each chunk's y and x passes, then its copy back, which overlaps the next chunk's passes (the
+  // chunks in increasing size: the first copy waits for the smallest chunk's passes only)
+  for (int c = 0, z0 = 0; c < static_cast<int>(stagedSizes_.size()); z0 += stagedSizes_[c], ++c) {
+    const int cnt = stagedSizes_[c];
     a.zBegin = z0;
     a.zCount = cnt;
     a.param = splitCpb_;

@@ -43,10 +43,11 @@ public:
   // chunk c back while the x pass of chunk c + 1 runs. `events` holds kStagedEvents events. Both
   // return false, doing nothing, when the plan has no split x pass (the caller then copies the
   // whole domain at once).
-  // Chunks per staged transform: 8 by default, SPFFT_GB300_STAGED_CHUNKS=n (1 .. kMaxStagedChunks)
-  // at plan creation.
+  // Plane chunks per staged transform (stagedSizes_, in the backward's order; the forward takes them
+  // in reverse): by default sizes doubling from about dimZ / 24 planes; SPFFT_GB300_STAGED_CHUNKS=n
+  // (1 .. kMaxStagedChunks) at plan creation selects n equal chunks.
   static constexpr int kMaxStagedChunks = 32, kStagedEvents = kMaxStagedChunks + 1;
-  int staged_chunks() const { return stagedChunks_; }
+  int staged_chunks() const { return static_cast<int>(stagedSizes_.size()); }
   bool forward_staged(const T* hostSpace, T* devSpace, T* values, bool scaled, void* scratch,
                       cudaStream_t stream, cudaStream_t copyStream, cudaEvent_t* events) const;
   bool backward_staged(const T* values, T* devSpace, T* hostSpace, void* scratch, cudaStream_t stream,
@@ -129,7 +130,7 @@ private:
   std::vector<std::pair<int, int>> fusedCands_;  // (rows, threads)
   std::vector<std::array<int, 3>> splitCands_;  // (cpb, rpb, rpbB)
   int fastSpb_ = 0, fastRows_ = 0, splitCpb_ = 0, splitRpb_ = 0, splitRpbB_ = 0, fusedThreads_ = 512;
-  int stagedChunks_ = 8;
+  std::vector<int> stagedSizes_;
   std::vector<RadixPlan> radixCands_[3];
   int radixChoice_[3] = {0, 0, 0};
   int splitChoice_[4] = {0, 0, 0, 0};  // Tuning::split
