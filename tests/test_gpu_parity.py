@@ -472,6 +472,33 @@ def test_pinned_host_buffers(lib, access, dtype, monkeypatch):
             assert rel_l2(buf.numpy(), want) <= TOL[dtype]
 
 
+@pytest.mark.parametrize("chunks", [None, "1", "7", "32"])
+def test_pinned_host_buffers_chunk_schedules(lib, chunks, monkeypatch):
+    """The staged host-buffer paths with the default plane chunks (doubling in size; 90 planes:
+    4, 8, 16, 32, 30, taken in reverse by the forward) and with n equal chunks
+    (SPFFT_GB300_STAGED_CHUNKS: 1, 7 of 13 planes and a last of 12, 30 of 3): same results."""
+    if chunks is None:
+        monkeypatch.delenv("SPFFT_GB300_STAGED_CHUNKS", raising=False)
+    else:
+        monkeypatch.setenv("SPFFT_GB300_STAGED_CHUNKS", chunks)
+    monkeypatch.setenv("SPFFT_GB300_PLANE", "split")
+    rng = np.random.default_rng(61)
+    for dims, ttype in [((48, 60, 90), 1), ((60, 48, 90), 0)]:
+        idx = random_indices(rng, *dims, r2c=ttype == 1, stick_frac=0.3, fill_frac=0.4)
+        tr = _transform("float64", ttype, dims, idx)
+        assert tr.path_info()["split_plane"]
+        oracle = pipeline.HostPipeline(ttype, *dims, idx)
+        vals = _values(rng, len(idx))
+        hv = torch.from_numpy(vals).pin_memory()
+        hs = torch.empty(dims[::-1], dtype=torch.complex128 if ttype == 0 else torch.float64).pin_memory()
+        tr.backward(hv, hs)
+        assert rel_l2(hs.numpy(), oracle.backward(vals)) <= TOL["float64"], (dims, chunks)
+        hf = torch.empty_like(hv)
+        tr.forward(hs, hf, sp.SPFFT_FULL_SCALING)
+        want_f = oracle.forward(hs.numpy().astype(np.complex128 if ttype == 0 else np.float64), scaled=True)
+        assert rel_l2(hf.numpy(), want_f) <= TOL["float64"], (dims, chunks)
+
+
 @pytest.mark.parametrize("access", ["direct", "copy"])
 def test_pinned_host_buffers_three_pass(lib, access, monkeypatch):
     """Pinned host buffers on the split plane passes with the three-pass z and y splits: the
